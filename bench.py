@@ -1,0 +1,315 @@
+"""Benchmark of the film-drainage path on GB300 (one JSON line on stdout).
+
+Workload (the plain method at scale): one bubble at resolution 2048 (2048 theta x 4096 phi =
+8.4 M cells), f32 thickness h = 550 nm + 16 seeded smooth modes clamped to [100, 1000] nm,
+surfactant 0.5 +- 0.1, reference fluid defaults, dt 1 ms. A bench step is one full run of
+10,000 drainage steps of the GPUDrainageSimulator semantics (h and surfactant co-evolve,
+drainage.wgsl) with the FP64 film-volume check fused into every 100th step. Inputs are
+synthetic (seeded); the field keeps evolving from step to step. L2 (129 MB) is flushed with a
+512 MB write before every bench step.
+
+value: cell-steps/s over the K timed bench steps, device-resident, CUDA events on the
+handle's stream. e2e: the same through the C ABI with host buffers: each step uploads h and
+surfactant from pinned host memory, runs, and reads both fields and the volumes back.
+roofline: the step kernel at 16 algorithmic bytes per cell-step (read h, Gamma; write h, Gamma).
+cpu_baseline: the oracle's f64 restatement of DrainageSimulator::step (drainage.rs:298-392) on
+all host cores, on a bounded sample of the same field (a few dozen steps).
+
+--impl reference: times that CPU restatement alone (the reference is Rust and cannot be
+built here), same metric and config.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+RES = 2048
+STEPS_PER_RUN = 10_000
+CHECK_EVERY = 100
+BYTES_PER_CELL_STEP = 16  # read h + Gamma, write h + Gamma (f32)
+METRIC = "drainage cell-steps/s, plain vs surrogate at <=1e-3 rel h error; % HBM roofline"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU baseline sample length")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the step kernel from the committed ncu summary (or None)."""
+    path = os.path.join(ROOT, "profiles", "drain_step_wgsl_c1.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(float(line.split(":", 1)[1]))
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.rows = []
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, n in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def cpu_baseline(h: np.ndarray, target_s: float, threads: int):
+    """The oracle's f64 DrainageSimulator::step on `threads` host cores over a bounded sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+
+    sim = orc.CpuSim(resolution=RES, precision="f64", threads=threads)
+    sim.set_field(h.astype(np.float64))
+    t0 = time.perf_counter()
+    sim.step(0.001)
+    one = time.perf_counter() - t0
+    n = int(max(2, min(400, target_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    sim.step_n(0.001, n)
+    dt = time.perf_counter() - t0
+    cells = h.size
+    return {"value": cells * n / dt, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{n} steps of DrainageSimulator::step (f64, drainage.rs:298-392) on the 2048 x 4096 field, "
+                      f"{dt:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from soap_bubble_simulation_gb300 import synthetic
+
+    h, _ = synthetic.bubble_c1(RES)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_baseline(h, 0.5, threads)
+    vals = [cpu_baseline(h, args.cpu_seconds / max(args.steps, 1), threads) for _ in range(args.steps)]
+    v = statistics.median(x["value"] for x in vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "cell-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": h.size * STEPS_PER_RUN / v * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "bubble resolution 2048 (2048 x 4096 cells), 10,000 steps, fluid defaults, "
+                                   "dt 1e-3 s; reference CPU path (DrainageSimulator::step) on a bounded sample"},
+            "cpu_baseline": {**vals[-1], "value": v},
+            "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank, world, local = dist_env()
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    import soap_bubble_simulation_gb300 as sbs
+    from soap_bubble_simulation_gb300 import _native as N
+    from soap_bubble_simulation_gb300 import synthetic
+
+    h0, c0 = synthetic.bubble_c1(RES)
+    nt, np_ = h0.shape
+    cells = h0.size
+    sim = sbs.GPUDrainageSimulator(None, 550e-9, np_, nt)
+    stream = torch.cuda.ExternalStream(sim.stream())
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident throughput ------------------------------------------------------
+    sim.set_thickness_array(h0)
+    sim.set_concentration_array(c0)
+    vols = None
+    for _ in range(args.warmup):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        vols = sim.run_checked(0.0, STEPS_PER_RUN, CHECK_EVERY)
+    barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        start_all = torch.cuda.Event(enable_timing=True)
+        end_all = torch.cuda.Event(enable_timing=True)
+        barrier()
+        start_all.record(stream)
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            ev[k][0].record(stream)
+            vols = sim.run_checked(0.0, STEPS_PER_RUN, CHECK_EVERY)
+            ev[k][1].record(stream)
+        end_all.record(stream)
+        barrier()
+    total_ms = start_all.elapsed_time(end_all)
+    kern_ms = sum(a.elapsed_time(b) for a, b in ev)
+    t = torch.tensor([total_ms, kern_ms], dtype=torch.float64)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    total_ms, kern_ms = float(t[0]), float(t[1])
+    value = world * cells * STEPS_PER_RUN * args.steps / (total_ms / 1e3)
+    launch_us = kern_ms * 1e3 / (args.steps * STEPS_PER_RUN)
+    peak, peak_kind = hbm_peak()
+    achieved = BYTES_PER_CELL_STEP * cells / (launch_us * 1e-6) / 1e9
+    traffic = ncu_traffic()
+    vol_drift = float(abs(vols[-1] - vols[0]) / vols[0]) if vols is not None and len(vols) else None
+
+    # ---- end to end through the C ABI with host buffers -------------------------------------
+    hp = torch.from_numpy(np.ascontiguousarray(h0)).pin_memory()
+    cp = torch.from_numpy(np.ascontiguousarray(c0)).pin_memory()
+    ho = torch.empty_like(hp).pin_memory()
+    co = torch.empty_like(cp).pin_memory()
+    e2e_steps = max(1, min(args.steps, 2))
+
+    def e2e_once():
+        N.call("sbs_drainage_set_thickness", sim.handle, ctypes.c_void_p(hp.data_ptr()), cells, N.MEM_HOST)
+        N.call("sbs_drainage_set_concentration", sim.handle, ctypes.c_void_p(cp.data_ptr()), cells, N.MEM_HOST)
+        v = np.zeros(STEPS_PER_RUN // CHECK_EVERY)
+        N.call("sbs_drainage_run_checked", sim.handle, 0.0, STEPS_PER_RUN, CHECK_EVERY, N.dptr(v))
+        N.call("sbs_drainage_get_thickness_field", sim.handle, ctypes.c_void_p(ho.data_ptr()), cells, N.MEM_HOST)
+        N.call("sbs_drainage_get_concentration_field", sim.handle, ctypes.c_void_p(co.data_ptr()), cells,
+               N.MEM_HOST)
+        return v
+
+    e2e_once()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_once()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        tt = torch.tensor([e2e_s], dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(tt[0])
+    e2e_value = world * cells * STEPS_PER_RUN * e2e_steps / e2e_s
+
+    # ---- the reference's CPU semantics on the GPU, for context (compensated f32x2) --------------
+    cfg = sbs.SimulationConfig()
+    cfg.resolution = RES
+    cpu_sem = sbs.DrainageSimulator(cfg)
+    cpu_sem.set_thickness_array(h0)
+    cpu_sem.step_n(0.001, 200)
+    torch.cuda.synchronize()
+    cs = torch.cuda.ExternalStream(cpu_sem.stream())
+    a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a_ev.record(cs)
+    cpu_sem.step_n(0.001, 2000)
+    b_ev.record(cs)
+    torch.cuda.synchronize()
+    cpu_sem_ms = a_ev.elapsed_time(b_ev)
+    cpu_sem_rate = cells * 2000 / (cpu_sem_ms / 1e3)
+
+    base = None
+    if rank == 0 and world == 1:
+        base = cpu_baseline(h0, args.cpu_seconds, os.cpu_count() or 1)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "bubble resolution 2048 (2048 theta x 4096 phi = 8.4M cells), h 550 nm + 16 "
+                                   "seeded modes, surfactant 0.5+-0.1, fluid defaults, dt 1e-3 s, 10,000 steps of "
+                                   "GPUDrainageSimulator semantics per bench step, FP64 volume check every 100 steps",
+                       "cells": cells, "drainage_steps_per_bench_step": STEPS_PER_RUN, "check_every": CHECK_EVERY,
+                       "l2": "512 MB write before every bench step (working set 128 MB)",
+                       "replicas": world},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "peak_kind": peak_kind, "bytes_per_cell_step": BYTES_PER_CELL_STEP,
+                         "launch_us": launch_us, "kernel": "drain_step_kernel<WGSL>"},
+            "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": 2 * cells * 4,
+                    "d2h_bytes_per_step": 2 * cells * 4 + 8 * (STEPS_PER_RUN // CHECK_EVERY)},
+            "gpu_launches": args.steps * STEPS_PER_RUN,
+            "clocks": clk.summary(),
+            "volume_rel_drift_per_run": vol_drift,
+            "cpu_semantics": {"value": cpu_sem_rate, "unit": "cell-steps/s", "storage": "f32x2 (16 B/cell-step)",
+                              "frac_hbm": BYTES_PER_CELL_STEP * cells * 2000 / (cpu_sem_ms / 1e3) / 1e9 / peak},
+            "cpu_baseline": base,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

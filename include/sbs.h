@@ -1,0 +1,323 @@
+/*
+ * sbs.h - C ABI of the GB300 soap-film physics library (libsbs.so).
+ *
+ * The library replaces, one for one, the data-parallel physics path of the
+ * soap-bubble simulation: the film-drainage time step on the bubble's
+ * theta-phi thickness grid and the thin-film interference evaluation. Every
+ * entry point below names the reference item it replaces (path:line inside
+ * the reference project). All compute runs as CUDA kernels on one GPU; there
+ * is no CPU fallback, and a missing or unusable GPU makes calls fail with
+ * SBS_E_CUDA.
+ *
+ * Conventions
+ *  - Every function returns SBS_OK (0) or a negative SBS_E_* code; the text of
+ *    the last error of the calling thread is sbs_last_error().
+ *  - A drainage handle owns its device memory and one CUDA stream. It is used
+ *    by one thread at a time (the reference takes &mut self). Different
+ *    handles are independent.
+ *  - Host pointers are borrowed for the duration of the call. Calls that take
+ *    or return host data are synchronous.
+ *  - Stateless batch calls take `int mem` (SBS_MEM_HOST or SBS_MEM_DEVICE) and
+ *    `void *stream` (a cudaStream_t, NULL = the legacy default stream). With
+ *    SBS_MEM_HOST the call copies in, computes, copies out and synchronises.
+ *    With SBS_MEM_DEVICE all pointers are device pointers and the call only
+ *    enqueues work on `stream` (asynchronous).
+ *  - Thickness is in metres on the drainage side and in nanometres on the
+ *    interference side, as in the reference.
+ */
+#ifndef SBS_H
+#define SBS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SBS_OK 0
+#define SBS_E_INVALID (-1)   /* bad argument or size */
+#define SBS_E_CUDA (-2)      /* CUDA runtime error, or no usable GPU */
+#define SBS_E_TIMEOUT (-3)   /* a bounded device-side wait ran out */
+#define SBS_E_NONFINITE (-4) /* a result was NaN or infinite where the caller asked for a check */
+#define SBS_E_NOMEM (-5)     /* device or host allocation failed */
+#define SBS_E_STATE (-6)     /* call not valid for this handle's semantics or state */
+
+#define SBS_MEM_HOST 0
+#define SBS_MEM_DEVICE 1
+
+/* Which reference solver a drainage handle reproduces. */
+#define SBS_CPU_SEMANTICS 0  /* DrainageSimulator (drainage.rs:212-614): pole ring means, TFE fronts */
+#define SBS_WGSL_SEMANTICS 1 /* GPUDrainageSimulator + drainage.wgsl: surfactant field, frozen poles */
+
+/* Interference arithmetic precision. */
+#define SBS_PREC_F64 0 /* same f64 arithmetic as InterferenceCalculator */
+#define SBS_PREC_F32 1 /* f32 arithmetic (within 1e-4 of f64 on RGB) */
+
+/* LUT lookup addressing. */
+#define SBS_LOOKUP_GRID 0  /* bilinear in index space: entry i sits at tmin + i*(tmax-tmin)/(T-1) */
+#define SBS_LOOKUP_TEXEL 1 /* texture addressing: texel centres at (i+0.5)/W, clamp to edge */
+
+const char *sbs_last_error(void);
+const char *sbs_version(void);
+/* Number of CUDA devices visible, or a negative code. */
+int sbs_device_count(int *out);
+
+/* ------------------------------------------------------------------ */
+/* Configuration: SimulationConfig (config.rs:283-302) and its         */
+/* defaults (config.rs:26-35, 56-66, 93-103, 305-316).                 */
+/* ------------------------------------------------------------------ */
+typedef struct sbs_config {
+    /* BubbleParameters (config.rs:12-24) */
+    double diameter;              /* m */
+    double film_thickness_nm;     /* initial uniform thickness */
+    double critical_thickness_nm; /* cells thinner than this are frozen */
+    double refractive_index;
+    /* FluidParameters (config.rs:38-54) */
+    double viscosity;                /* Pa s */
+    double surface_tension;          /* N/m (not used by either drainage solver, as in the reference) */
+    double density;                  /* kg/m^3 */
+    double surfactant_diffusion;     /* m^2/s; the thickness diffusion coefficient (drainage.rs:277) */
+    double surfactant_concentration; /* initial Gamma for the WGSL-semantics solver */
+    /* EnvironmentParameters (config.rs:70-88) */
+    double gravity;     /* m/s^2 */
+    double temperature; /* K */
+    double pressure;    /* Pa */
+    double dt;          /* s */
+    uint32_t resolution; /* N_theta = resolution, N_phi = 2*resolution */
+    uint32_t _reserved;
+} sbs_config;
+
+/* SimulationConfig::default (config.rs:305-316). */
+int sbs_config_default(sbs_config *out);
+
+/* DrainageParams (gpu_drainage.rs:12-44), 64 bytes, same field order. */
+typedef struct sbs_drainage_params {
+    float dt;
+    float gravity;
+    float viscosity;
+    float density;
+    float diffusion_coeff;
+    float bubble_radius;
+    float critical_thickness;
+    uint32_t grid_width;  /* phi points */
+    uint32_t grid_height; /* theta points */
+    uint32_t marangoni_enabled;
+    float gamma_air;
+    float gamma_reduction;
+    float surfactant_diffusion;
+    float marangoni_coeff;
+    uint32_t _padding1;
+    uint32_t _padding2;
+} sbs_drainage_params;
+
+/* DrainageParams::default (gpu_drainage.rs:46-68). */
+int sbs_drainage_params_default(sbs_drainage_params *out);
+
+/* ------------------------------------------------------------------ */
+/* Drainage handle                                                     */
+/* ------------------------------------------------------------------ */
+typedef struct sbs_drainage sbs_drainage;
+
+/* DrainageSimulator::new (drainage.rs:263-288): CPU semantics, uniform field
+ * film_thickness_nm*1e-9, marginal regeneration on, TFE ratio 0.85, first
+ * front at t = 0.5 s, compensated f32x2 storage. resolution >= 3. */
+int sbs_drainage_create(const sbs_config *cfg, sbs_drainage **out);
+
+/* Thickness storage of a CPU-semantics handle. */
+#define SBS_DRAIN_F32 0   /* one f32 word per cell: 8 B per cell-step */
+#define SBS_DRAIN_F32X2 1 /* compensated hi + lo f32 words: ~48 significant bits, 16 B per cell-step */
+
+/* DrainageSimulator::new with an explicit thickness storage. The reference
+ * integrates in f64; with SBS_DRAIN_F32 the gravity increment of a 500 nm
+ * film (~1e-3 of an f32 ulp per 1 ms step) is lost, with SBS_DRAIN_F32X2 (the
+ * default of sbs_drainage_create) it is kept. */
+int sbs_drainage_create_ex(const sbs_config *cfg, int precision, sbs_drainage **out);
+int sbs_drainage_precision(const sbs_drainage *h, int *out);
+
+/* GPUDrainageSimulator::new (gpu_drainage.rs:118-331): WGSL semantics,
+ * grid_width (phi) x grid_height (theta), thickness initial_thickness (m),
+ * concentration 0.5, DrainageParams::default otherwise, enabled = false,
+ * time_scale 100, steps_per_frame 10. grid_height >= 3, grid_width >= 3. */
+int sbs_gpu_drainage_create(float initial_thickness, uint32_t grid_width, uint32_t grid_height,
+                            sbs_drainage **out);
+
+int sbs_drainage_destroy(sbs_drainage *h);
+
+/* Semantics (SBS_CPU_SEMANTICS / SBS_WGSL_SEMANTICS), grid size (theta rows, phi columns). */
+int sbs_drainage_semantics(const sbs_drainage *h, int *out);
+/* GPUDrainageSimulator::grid_size (gpu_drainage.rs:482-484) returns (width, height). */
+int sbs_drainage_grid_size(const sbs_drainage *h, uint32_t *num_theta, uint32_t *num_phi);
+
+/* DrainageSimulator::step (drainage.rs:298-392): one forward-Euler step of
+ * size dt, pole rings averaged, TFE fronts applied, time advanced by dt.
+ * CPU semantics only. */
+int sbs_drainage_step(sbs_drainage *h, double dt);
+
+/* n consecutive calls of sbs_drainage_step(h, dt), replayed as CUDA graphs in
+ * chunks. CPU semantics only. */
+int sbs_drainage_step_n(sbs_drainage *h, double dt, uint32_t n);
+
+/* GPUDrainageSimulator::step (gpu_drainage.rs:338-370): if enabled, runs
+ * steps_per_frame passes of drainage_step with params.dt and advances the
+ * clock by frame_dt*time_scale/steps_per_frame per pass. WGSL semantics only. */
+int sbs_gpu_drainage_step(sbs_drainage *h, float frame_dt);
+
+/* Runs `passes` WGSL-semantics passes (each uses params.dt and advances the
+ * clock by params.dt), independent of `enabled`. WGSL semantics only. */
+int sbs_gpu_drainage_run(sbs_drainage *h, uint32_t passes);
+
+/* The film-volume conservation run: advances n steps (CPU semantics: of size
+ * dt; WGSL semantics: passes with params.dt, dt ignored) and computes the FP64
+ * film volume V = sum h R^2 sin(theta) dtheta dphi of the field after every
+ * `check_every`-th step, fused into that step's kernel. volumes_out (host)
+ * receives n / check_every values. check_every = 0 disables the check. */
+int sbs_drainage_run_checked(sbs_drainage *h, double dt, uint32_t n, uint32_t check_every,
+                             double *volumes_out);
+
+/* Field I/O. Fields are row-major [theta][phi], num_theta*num_phi f32 values
+ * in metres (thickness) or 0..1 (concentration). mem = SBS_MEM_HOST or
+ * SBS_MEM_DEVICE. In f32x2 storage the f32 setter clears the low words and
+ * the f32 getter returns the high words (the value rounded to f32); the f64
+ * calls carry the full value. Replaces ThicknessField::data/data_mut (drainage.rs:195-203)
+ * and the buffer getters (gpu_drainage.rs:458-480). */
+int sbs_drainage_set_thickness(sbs_drainage *h, const float *src, size_t n, int mem);
+int sbs_drainage_get_thickness_field(sbs_drainage *h, float *dst, size_t n, int mem);
+int sbs_drainage_set_concentration(sbs_drainage *h, const float *src, size_t n, int mem);
+int sbs_drainage_get_concentration_field(sbs_drainage *h, float *dst, size_t n, int mem);
+/* f64 host convenience for the reference's f64 ThicknessField. */
+int sbs_drainage_set_thickness_f64(sbs_drainage *h, const double *src, size_t n);
+int sbs_drainage_get_thickness_field_f64(sbs_drainage *h, double *dst, size_t n);
+
+/* Device view of the current fields: pitch in elements (row stride). The
+ * pointers stay valid until the next step/run/set call on the handle.
+ * which = 0: the most recent output; which = 1: the buffer the reference's
+ * GPUDrainageSimulator::current_buffer() (gpu_drainage.rs:473-479) hands out,
+ * which after a step is the previous pass's input (one pass stale). */
+int sbs_drainage_thickness_device(sbs_drainage *h, int which, const float **ptr, size_t *pitch);
+int sbs_drainage_concentration_device(sbs_drainage *h, int which, const float **ptr, size_t *pitch);
+/* The handle's CUDA stream (a cudaStream_t). */
+int sbs_drainage_stream(const sbs_drainage *h, void **out);
+
+/* DrainageSimulator::get_thickness (drainage.rs:516-552): bilinear query, theta
+ * clamped to [0,pi], phi wrapped with rem_euclid. f64 arithmetic on the GPU. */
+int sbs_drainage_get_thickness(sbs_drainage *h, double theta, double phi, double *out);
+/* Batched get_thickness. theta/phi/out: n values in `mem`. */
+int sbs_drainage_query_batch(sbs_drainage *h, const double *theta, const double *phi, double *out, size_t n,
+                             int mem);
+
+/* current_time (drainage.rs:560), has_critical_region (:565),
+ * critical_thickness (:570), ThicknessField::min/max_thickness (:180-193). */
+int sbs_drainage_current_time(const sbs_drainage *h, double *out);
+int sbs_drainage_has_critical_region(sbs_drainage *h, int *out);
+int sbs_drainage_critical_thickness(const sbs_drainage *h, double *out);
+int sbs_drainage_min_max(sbs_drainage *h, double *min_out, double *max_out);
+/* FP64 film volume of the current field. */
+int sbs_drainage_film_volume(sbs_drainage *h, double *out);
+
+/* reset (drainage.rs:575-583); for WGSL semantics GPUDrainageSimulator::reset
+ * (gpu_drainage.rs:418-433): both buffers, concentration back to 0.5. */
+int sbs_drainage_reset(sbs_drainage *h, double initial_thickness);
+
+/* Marginal regeneration control (drainage.rs:588-613). CPU semantics. */
+int sbs_drainage_set_marginal_regeneration(sbs_drainage *h, int enabled);
+int sbs_drainage_marginal_regeneration_enabled(const sbs_drainage *h, int *out);
+int sbs_drainage_set_tfe_thickness_ratio(sbs_drainage *h, double ratio); /* clamped to [0.5, 0.95] */
+int sbs_drainage_tfe_thickness_ratio(const sbs_drainage *h, double *out);
+int sbs_drainage_active_tfe_count(const sbs_drainage *h, uint32_t *out);
+
+/* GPUDrainageSimulator setters (gpu_drainage.rs:377-456). WGSL semantics. */
+int sbs_gpu_drainage_update_params(sbs_drainage *h, const sbs_drainage_params *p);
+int sbs_gpu_drainage_params(const sbs_drainage *h, sbs_drainage_params *out);
+int sbs_gpu_drainage_set_dt(sbs_drainage *h, float dt);
+int sbs_gpu_drainage_set_physics(sbs_drainage *h, float viscosity, float density, float gravity, float diffusion);
+int sbs_gpu_drainage_set_bubble_radius(sbs_drainage *h, float radius);
+int sbs_gpu_drainage_set_marangoni_enabled(sbs_drainage *h, int enabled);
+int sbs_gpu_drainage_set_marangoni_params(sbs_drainage *h, float gamma_air, float gamma_reduction,
+                                          float surfactant_diffusion, float marangoni_coeff);
+/* Public fields of GPUDrainageSimulator (gpu_drainage.rs:100-107). */
+int sbs_gpu_drainage_set_enabled(sbs_drainage *h, int enabled);
+int sbs_gpu_drainage_set_time_scale(sbs_drainage *h, float time_scale);
+int sbs_gpu_drainage_set_steps_per_frame(sbs_drainage *h, uint32_t steps);
+
+/* ------------------------------------------------------------------ */
+/* Film volume of a bare device field                                  */
+/* ------------------------------------------------------------------ */
+/* V = sum_{i,j} h[i*pitch+j] R^2 sin(i*pi/(nt-1)) (pi/(nt-1)) (2pi/np), FP64
+ * accumulation, deterministic order. h: device pointer. Synchronous. The
+ * per-block partial sums live in memory this call allocates. No reference
+ * counterpart (the reference has no conservation check). */
+int sbs_film_volume_device(const float *h, uint32_t num_theta, uint32_t num_phi, size_t pitch, double radius,
+                           double *out, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Interference (interference.rs:127-512)                              */
+/* ------------------------------------------------------------------ */
+/* calculate_interference_color (gamma=1) / _linear (gamma=0) (interference.rs:380-426)
+ * for n points: rgb[3*k+c] for thickness t_nm[k] and cos_i[k]. wl: the three
+ * channel wavelengths in nm (650/532/450 by default; with_custom_wavelengths
+ * :165-176). prec: SBS_PREC_F64 / SBS_PREC_F32. rgb is f64 when prec = F64
+ * and f32 when prec = F32; t_nm/cos_i are f64 for F64 and f32 for F32. */
+int sbs_interference_color_batch(double n_film, const double wl[3], const void *t_nm, const void *cos_i, size_t n,
+                                 int gamma, int prec, void *rgb, int mem, void *stream);
+
+/* Per-wavelength terms of calculate_reflected_intensity for n points (f64):
+ * out[8*k + 0..7] = cos_t (:197), opd (:226), phase (:248), Rs, Rp, R (:266),
+ * intensity (:312), and 0 (pad). */
+int sbs_interference_terms_batch(double n_film, double wl_nm, const double *t_nm, const double *cos_i, size_t n,
+                                 double *out, int mem, void *stream);
+
+/* calculate_optical_path_difference (interference.rs:226-238) for n triples:
+ * opd[k] = 2 n t_nm[k] cos_t[k] + wl[k]/2 (f64). */
+int sbs_optical_path_batch(double n_film, const double *t_nm, const double *cos_t, const double *wl, size_t n,
+                           double *opd, int mem, void *stream);
+/* calculate_phase_difference (interference.rs:248-254): phase[k] = 2 pi opd[k] / wl[k] (f64). */
+int sbs_phase_difference_batch(const double *opd_nm, const double *wl, size_t n, double *phase, int mem,
+                               void *stream);
+
+/* generate_color_lookup_table (interference.rs:461-477): count gamma-corrected
+ * colours over [tmin, tmax] at cos_i. rgb: count*3 f64. */
+int sbs_lut1d_build(double n_film, const double wl[3], double tmin, double tmax, uint32_t count, double cos_i,
+                    double *rgb, int mem, void *stream);
+
+/* generate_2d_color_lookup_table (interference.rs:491-512): [T][A][3] f64,
+ * cos_j = j/(A-1). T, A >= 1. */
+int sbs_lut2d_build(double n_film, const double wl[3], double tmin, double tmax, uint32_t T, uint32_t A,
+                    double *rgb, int mem, void *stream);
+
+/* generate_interference_lut (interference_lut.rs:18-41): RGBA8 [64 angle][256
+ * thickness][4], thickness 0..2000 nm, f32 arithmetic, truncating quantiser. */
+#define SBS_LUT_THICKNESS_SAMPLES 256
+#define SBS_LUT_ANGLE_SAMPLES 64
+#define SBS_LUT_MAX_THICKNESS_NM 2000.0f
+int sbs_interference_lut_rgba8(float n_film, float intensity, uint8_t *out, int mem, void *stream);
+
+/* Schlick reflectance with transmitted Airy (wall.wgsl:176-207) at three
+ * wavelengths: out[3k+c] for t_nm[k], cos_i[k]; f32. */
+int sbs_schlick_rgb_batch(float n_film, const float wl[3], const float *t_nm, const float *cos_i, size_t n,
+                          float *out, int mem, void *stream);
+
+/* LUT lookups. RGBA8 lookup: thin_film_interference of bubble.wgsl:425-439
+ * (u = t/max_nm, v = cos, bilinear, * intensity, clamp) with addressing
+ * SBS_LOOKUP_TEXEL (the sampler of pipeline.rs:350-359) or SBS_LOOKUP_GRID.
+ * lut: W x H RGBA8 texels [H][W][4]. */
+int sbs_lut_rgba8_lookup_batch(const uint8_t *lut, uint32_t W, uint32_t H, float max_nm, float intensity,
+                               int addressing, const float *t_nm, const float *cos_i, size_t n, float *rgb,
+                               int mem, void *stream);
+/* Grid-aligned bilinear read of a [T][A][3] f64 LUT over [tmin,tmax] x cos[0,1]. */
+int sbs_lut2d_lookup_batch(const double *lut, uint32_t T, uint32_t A, double tmin, double tmax, const double *t_nm,
+                           const double *cos_i, size_t n, double *rgb, int mem, void *stream);
+
+/* Vertex colouring: each unit vertex (x,y,z) gets theta = acos(y), phi =
+ * atan2(z,x) mod 2pi (geometry.rs:40-60, 184-186), t = get_thickness(theta,
+ * phi) in nm from the handle's current field, cos = |z| (view along +z), and
+ * rgb from a grid-aligned read of a [T][A][3] f64 LUT. One fused kernel.
+ * xyz: 3*nv f64, rgb: 3*nv f64, lut: T*A*3 f64, all in `mem`. */
+int sbs_drainage_vertex_colors(sbs_drainage *h, const double *xyz, size_t nv, const double *lut, uint32_t T,
+                               uint32_t A, double tmin, double tmax, double *rgb, int mem);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SBS_H */

@@ -1,0 +1,156 @@
+/*
+ * Parity oracle for the soap-film physics path: a plain C++17 restatement of
+ * the reference's CPU and WGSL arithmetic, compiled with gcc and
+ * -ffp-contract=off so that every product and sum rounds exactly as the
+ * reference's Rust (which never contracts to FMA) does.
+ *
+ * This is TEST INFRASTRUCTURE. Only tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / reference legs of bench.py load it, and only as the checker or
+ * as the timed CPU baseline. The product library (libsbs) never links it.
+ *
+ * Pinning: the reference ships no numeric golden vectors for this path and
+ * cannot be built here (Rust/wgpu, no toolchain). The oracle is pinned by the
+ * reference's own known-answer unit tests (drainage.rs:621-719,
+ * interference.rs:619-790, interference_lut.rs:170-204, config.rs:431-464),
+ * ported as tests/test_oracle_*.py, plus analytic checks (uniform-field ODE,
+ * sphere area). The WGSL semantics (drainage.wgsl) has no numeric test in the
+ * reference at all: its parity is "unpinned" beyond this restatement.
+ *
+ * Precision modes of the drainage restatements:
+ *   f64 faithful    - drainage.rs:298-503 exactly (f64, libm sin/cos).
+ *   f32 kernel-order- the exact f32 arithmetic of the CUDA kernel (per-row
+ *                     coefficients computed in f64 then rounded, explicit fmaf),
+ *                     used for bitwise GPU parity.
+ *   f32 WGSL        - drainage.wgsl:72-202 in its own operation order (IEEE
+ *                     f32 division, sinf/cosf of an f32 angle).
+ */
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* CPU-semantics drainage simulator (drainage.rs:212-614)              */
+/* ------------------------------------------------------------------ */
+typedef struct orc_sim orc_sim;
+
+typedef struct orc_sim_params {
+    uint32_t resolution;          /* N_theta = resolution, N_phi = 2*resolution (drainage.rs:264-265) */
+    double diameter;              /* m; radius = diameter/2 (config.rs:357) */
+    double film_thickness_nm;     /* initial uniform thickness (config.rs:368) */
+    double critical_thickness_nm; /* drainage.rs:278 */
+    double density;
+    double gravity;
+    double viscosity;
+    double surfactant_diffusion;  /* used as the thickness diffusion coefficient (drainage.rs:277) */
+} orc_sim_params;
+
+/* precision: 0 = f64 faithful, 1 = f32 kernel-order, 2 = compensated f32x2 kernel-order
+ * (hi + lo words, TwoSum update, compensated ring sums). threads: OpenMP threads for the
+ * stencil loop (0 = OpenMP default, 1 = sequential like the reference). */
+orc_sim *orc_sim_new(const orc_sim_params *p, int precision, int threads);
+void orc_sim_free(orc_sim *s);
+uint32_t orc_sim_num_theta(const orc_sim *s);
+uint32_t orc_sim_num_phi(const orc_sim *s);
+void orc_sim_set_field(orc_sim *s, const double *h);   /* N_theta*N_phi, meters */
+void orc_sim_get_field(const orc_sim *s, double *h);
+void orc_sim_step(orc_sim *s, double dt);
+void orc_sim_step_n(orc_sim *s, double dt, uint32_t n);
+double orc_sim_get_thickness(const orc_sim *s, double theta, double phi);
+double orc_sim_current_time(const orc_sim *s);
+int orc_sim_has_critical_region(const orc_sim *s);
+double orc_sim_min_thickness(const orc_sim *s);
+double orc_sim_max_thickness(const orc_sim *s);
+void orc_sim_reset(orc_sim *s, double h0);
+void orc_sim_set_marginal_regeneration(orc_sim *s, int enabled);
+void orc_sim_set_tfe_thickness_ratio(orc_sim *s, double ratio);
+double orc_sim_tfe_thickness_ratio(const orc_sim *s);
+uint32_t orc_sim_active_tfe_count(const orc_sim *s);
+/* fronts as 4 doubles each: phi_center, extent, width, velocity; returns count */
+uint32_t orc_sim_get_fronts(const orc_sim *s, double *out, uint32_t cap);
+
+/* ------------------------------------------------------------------ */
+/* WGSL-semantics drainage step (drainage.wgsl:72-202)                 */
+/* ------------------------------------------------------------------ */
+typedef struct orc_wgsl_params { /* mirrors DrainageParams, gpu_drainage.rs:12-44 */
+    float dt, gravity, viscosity, density, diffusion_coeff, bubble_radius, critical_thickness;
+    uint32_t grid_width, grid_height, marangoni_enabled;
+    float gamma_air, gamma_reduction, surfactant_diffusion, marangoni_coeff;
+    uint32_t _padding1, _padding2;
+} orc_wgsl_params;
+
+/* mode 0 = WGSL operation order (IEEE f32), mode 1 = CUDA kernel order. n passes, ping-pong
+ * internally; results land in h_out/c_out. threads as above. */
+void orc_wgsl_run(const orc_wgsl_params *p, int mode, const float *h_in, const float *c_in,
+                  float *h_out, float *c_out, uint32_t passes, int threads);
+
+/* ------------------------------------------------------------------ */
+/* Film volume (no reference counterpart): sum h * R^2 sin(theta) dth dphi */
+/* ------------------------------------------------------------------ */
+double orc_film_volume_f64(const double *h, uint32_t n_theta, uint32_t n_phi, double radius);
+double orc_film_volume_f32(const float *h, uint32_t n_theta, uint32_t n_phi, double radius);
+
+/* ------------------------------------------------------------------ */
+/* InterferenceCalculator (interference.rs:127-512), f64               */
+/* ------------------------------------------------------------------ */
+double orc_transmission_angle_cos(double n_film, double cos_i);
+double orc_optical_path_difference(double n_film, double t_nm, double cos_t, double wl_nm);
+double orc_phase_difference(double opd_nm, double wl_nm);
+void orc_fresnel(double n_film, double cos_i, double out3[3]); /* s, p, average */
+double orc_reflected_intensity(double n_film, double t_nm, double cos_i, double wl_nm);
+/* gamma: 1 = calculate_interference_color, 0 = _linear */
+void orc_interference_color(double n_film, const double wl[3], double t_nm, double cos_i, int gamma,
+                            double rgb[3]);
+void orc_interference_color_batch(double n_film, const double wl[3], const double *t_nm,
+                                  const double *cos_i, size_t n, int gamma, double *rgb);
+void orc_lut1d(double n_film, const double wl[3], double tmin, double tmax, uint32_t count,
+               double cos_i, double *rgb /*count*3*/);
+void orc_lut2d(double n_film, const double wl[3], double tmin, double tmax, uint32_t T, uint32_t A,
+               double *rgb /*T*A*3, [thickness][angle][c]*/);
+
+/* ------------------------------------------------------------------ */
+/* generate_interference_lut (interference_lut.rs:18-163), f32 -> RGBA8 */
+/* ------------------------------------------------------------------ */
+void orc_interference_lut_rgba8(float n_film, float intensity, uint8_t *out /*64*256*4*/);
+void orc_thin_film_interference7(float t_nm, float cos_t, float n_film, float intensity,
+                                 float out3[3]);
+float orc_lut_snells_law(float cos_i, float n_film);
+float orc_lut_fresnel_unpolarized(float cos_i, float cos_t, float n1, float n2);
+
+/* ------------------------------------------------------------------ */
+/* Schlick / transmitted Airy path (wall.wgsl:176-207), f32            */
+/* ------------------------------------------------------------------ */
+float orc_schlick_interference(float t_nm, float wl_nm, float cos_i, float n_film);
+
+/* ------------------------------------------------------------------ */
+/* LUT lookups (bubble.wgsl:425-439 and the grid-aligned 2-D LUT read) */
+/* ------------------------------------------------------------------ */
+/* texel-centre bilinear lookup of the RGBA8 LUT ([angle][thickness][4], W x H texels), the
+ * ClampToEdge/Linear sampler of pipeline.rs:350-359; result * intensity clamped to [0,1]. */
+void orc_lut_rgba8_sample(const uint8_t *lut, uint32_t W, uint32_t H, float t_nm, float cos_i,
+                          float max_nm, float intensity, float out3[3]);
+/* grid-aligned bilinear read of a [T][A][3] f64 LUT over [tmin,tmax] x cos in [0,1]. */
+void orc_lut2d_lookup(const double *lut, uint32_t T, uint32_t A, double tmin, double tmax,
+                      double t_nm, double cos_i, double out3[3]);
+
+/* C0 vertex colouring: for each unit vertex (x,y,z): theta = acos(y), phi = atan2(z,x) mod 2pi
+ * (geometry.rs:40-60), t = get_thickness(theta,phi)*1e9 on an f64 field, cos = |z| (view +z),
+ * rgb = grid-aligned lookup into the [T][A][3] LUT. */
+void orc_vertex_colors(const double *field, uint32_t n_theta, uint32_t n_phi, const double *xyz,
+                       size_t nv, const double *lut, uint32_t T, uint32_t A, double tmin,
+                       double tmax, double *rgb);
+
+/* ------------------------------------------------------------------ */
+/* Spectral interference (81 wavelengths) against a CMF, f64           */
+/* ------------------------------------------------------------------ */
+/* per point: R(l) = Airy reflectance (interference_lut.rs:45-93 formulation with full Fresnel,
+ * phase + pi) at wavelength l; rgb[c] = sum_l R(l) * cmf[l][c]. */
+void orc_spectral_rgb(const float *t_nm, const float *cos_i, const float *n_film, size_t n,
+                      const double *wl, uint32_t nl, const double *cmf /*nl*3*/, double *rgb);
+
+#ifdef __cplusplus
+}
+#endif

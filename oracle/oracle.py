@@ -1,0 +1,339 @@
+"""ctypes binding of the parity oracle (oracle/_build/liboracle.so).
+
+Test infrastructure: only tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline legs import this module. See oracle.h for what each function
+restates and how the oracle is pinned.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+if _HERE not in sys.path:
+    sys.path.insert(0, _HERE)
+import build_oracle  # noqa: E402
+
+_lib = None
+
+_P = C.c_void_p
+_D = C.c_double
+_F = C.c_float
+_U32 = C.c_uint32
+_SZ = C.c_size_t
+_I = C.c_int
+
+
+class OrcSimParams(C.Structure):
+    _fields_ = [
+        ("resolution", C.c_uint32),
+        ("diameter", C.c_double),
+        ("film_thickness_nm", C.c_double),
+        ("critical_thickness_nm", C.c_double),
+        ("density", C.c_double),
+        ("gravity", C.c_double),
+        ("viscosity", C.c_double),
+        ("surfactant_diffusion", C.c_double),
+    ]
+
+
+class OrcWgslParams(C.Structure):
+    _fields_ = [
+        ("dt", C.c_float),
+        ("gravity", C.c_float),
+        ("viscosity", C.c_float),
+        ("density", C.c_float),
+        ("diffusion_coeff", C.c_float),
+        ("bubble_radius", C.c_float),
+        ("critical_thickness", C.c_float),
+        ("grid_width", C.c_uint32),
+        ("grid_height", C.c_uint32),
+        ("marangoni_enabled", C.c_uint32),
+        ("gamma_air", C.c_float),
+        ("gamma_reduction", C.c_float),
+        ("surfactant_diffusion", C.c_float),
+        ("marangoni_coeff", C.c_float),
+        ("_padding1", C.c_uint32),
+        ("_padding2", C.c_uint32),
+    ]
+
+
+_SIGS = {
+    "orc_sim_new": ([C.POINTER(OrcSimParams), _I, _I], _P),
+    "orc_sim_free": ([_P], None),
+    "orc_sim_num_theta": ([_P], _U32),
+    "orc_sim_num_phi": ([_P], _U32),
+    "orc_sim_set_field": ([_P, _P], None),
+    "orc_sim_get_field": ([_P, _P], None),
+    "orc_sim_step": ([_P, _D], None),
+    "orc_sim_step_n": ([_P, _D, _U32], None),
+    "orc_sim_get_thickness": ([_P, _D, _D], _D),
+    "orc_sim_current_time": ([_P], _D),
+    "orc_sim_has_critical_region": ([_P], _I),
+    "orc_sim_min_thickness": ([_P], _D),
+    "orc_sim_max_thickness": ([_P], _D),
+    "orc_sim_reset": ([_P, _D], None),
+    "orc_sim_set_marginal_regeneration": ([_P, _I], None),
+    "orc_sim_set_tfe_thickness_ratio": ([_P, _D], None),
+    "orc_sim_tfe_thickness_ratio": ([_P], _D),
+    "orc_sim_active_tfe_count": ([_P], _U32),
+    "orc_sim_get_fronts": ([_P, _P, _U32], _U32),
+    "orc_wgsl_run": ([C.POINTER(OrcWgslParams), _I, _P, _P, _P, _P, _U32, _I], None),
+    "orc_film_volume_f64": ([_P, _U32, _U32, _D], _D),
+    "orc_film_volume_f32": ([_P, _U32, _U32, _D], _D),
+    "orc_transmission_angle_cos": ([_D, _D], _D),
+    "orc_optical_path_difference": ([_D, _D, _D, _D], _D),
+    "orc_phase_difference": ([_D, _D], _D),
+    "orc_fresnel": ([_D, _D, _P], None),
+    "orc_reflected_intensity": ([_D, _D, _D, _D], _D),
+    "orc_interference_color": ([_D, _P, _D, _D, _I, _P], None),
+    "orc_interference_color_batch": ([_D, _P, _P, _P, _SZ, _I, _P], None),
+    "orc_lut1d": ([_D, _P, _D, _D, _U32, _D, _P], None),
+    "orc_lut2d": ([_D, _P, _D, _D, _U32, _U32, _P], None),
+    "orc_interference_lut_rgba8": ([_F, _F, _P], None),
+    "orc_thin_film_interference7": ([_F, _F, _F, _F, _P], None),
+    "orc_lut_snells_law": ([_F, _F], _F),
+    "orc_lut_fresnel_unpolarized": ([_F, _F, _F, _F], _F),
+    "orc_schlick_interference": ([_F, _F, _F, _F], _F),
+    "orc_lut_rgba8_sample": ([_P, _U32, _U32, _F, _F, _F, _F, _P], None),
+    "orc_lut2d_lookup": ([_P, _U32, _U32, _D, _D, _D, _D, _P], None),
+    "orc_vertex_colors": ([_P, _U32, _U32, _P, _SZ, _P, _U32, _U32, _D, _D, _P], None),
+    "orc_spectral_rgb": ([_P, _P, _P, _SZ, _P, _U32, _P, _P], None),
+}
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle.build()
+        L = C.CDLL(path)
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray) -> C.c_void_p:
+    assert a.flags["C_CONTIGUOUS"]
+    return C.c_void_p(a.ctypes.data)
+
+
+class CpuSim:
+    """DrainageSimulator restatement (drainage.rs:212-614). precision 'f64' (faithful), 'f32k'
+    (the CUDA kernel's plain f32 operation order) or 'f32x2' (its compensated hi + lo order)."""
+
+    def __init__(self, resolution=128, diameter=0.05, film_thickness_nm=500.0, critical_thickness_nm=10.0,
+                 density=1000.0, gravity=9.81, viscosity=0.001, surfactant_diffusion=1e-9, precision="f64",
+                 threads=1):
+        p = OrcSimParams(resolution, diameter, film_thickness_nm, critical_thickness_nm, density, gravity, viscosity,
+                         surfactant_diffusion)
+        mode = {"f64": 0, "f32k": 1, "f32x2": 2}[precision]
+        self._h = lib().orc_sim_new(C.byref(p), mode, int(threads))
+        if not self._h:
+            raise ValueError("bad oracle parameters")
+        self.nt = lib().orc_sim_num_theta(self._h)
+        self.np = lib().orc_sim_num_phi(self._h)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_sim_free(self._h)
+            self._h = None
+
+    def set_field(self, h):
+        a = np.ascontiguousarray(h, dtype=np.float64).reshape(-1)
+        assert a.size == self.nt * self.np
+        lib().orc_sim_set_field(self._h, _p(a))
+
+    def field(self) -> np.ndarray:
+        a = np.empty(self.nt * self.np, dtype=np.float64)
+        lib().orc_sim_get_field(self._h, _p(a))
+        return a.reshape(self.nt, self.np)
+
+    def step(self, dt):
+        lib().orc_sim_step(self._h, float(dt))
+
+    def step_n(self, dt, n):
+        lib().orc_sim_step_n(self._h, float(dt), int(n))
+
+    def get_thickness(self, theta, phi):
+        return lib().orc_sim_get_thickness(self._h, float(theta), float(phi))
+
+    def current_time(self):
+        return lib().orc_sim_current_time(self._h)
+
+    def has_critical_region(self):
+        return bool(lib().orc_sim_has_critical_region(self._h))
+
+    def min_thickness(self):
+        return lib().orc_sim_min_thickness(self._h)
+
+    def max_thickness(self):
+        return lib().orc_sim_max_thickness(self._h)
+
+    def reset(self, h0):
+        lib().orc_sim_reset(self._h, float(h0))
+
+    def set_marginal_regeneration(self, en):
+        lib().orc_sim_set_marginal_regeneration(self._h, 1 if en else 0)
+
+    def set_tfe_thickness_ratio(self, r):
+        lib().orc_sim_set_tfe_thickness_ratio(self._h, float(r))
+
+    def tfe_thickness_ratio(self):
+        return lib().orc_sim_tfe_thickness_ratio(self._h)
+
+    def active_tfe_count(self):
+        return lib().orc_sim_active_tfe_count(self._h)
+
+    def fronts(self) -> np.ndarray:
+        out = np.zeros((8, 4), dtype=np.float64)
+        n = lib().orc_sim_get_fronts(self._h, _p(out), 8)
+        return out[:n]
+
+
+def wgsl_params(**kw) -> OrcWgslParams:
+    """DrainageParams::default (gpu_drainage.rs:46-68) with overrides."""
+    d = dict(dt=0.001, gravity=9.81, viscosity=0.001, density=1000.0, diffusion_coeff=1e-9, bubble_radius=0.025,
+             critical_thickness=30e-9, grid_width=128, grid_height=64, marangoni_enabled=0, gamma_air=0.072,
+             gamma_reduction=0.045, surfactant_diffusion=1e-9, marangoni_coeff=0.01, _padding1=0, _padding2=0)
+    d.update(kw)
+    p = OrcWgslParams()
+    for k, v in d.items():
+        setattr(p, k, v)
+    return p
+
+
+def wgsl_run(params: OrcWgslParams, h, c, passes: int, mode: str = "wgsl", threads: int = 0):
+    """drainage.wgsl passes; mode 'wgsl' (its own op order) or 'kernel' (CUDA op order)."""
+    h = np.ascontiguousarray(h, dtype=np.float32)
+    c = np.ascontiguousarray(c, dtype=np.float32)
+    ho = np.empty_like(h)
+    co = np.empty_like(c)
+    lib().orc_wgsl_run(C.byref(params), 0 if mode == "wgsl" else 1, _p(h), _p(c), _p(ho), _p(co), int(passes),
+                       int(threads))
+    return ho, co
+
+
+def film_volume(h, radius: float) -> float:
+    a = np.ascontiguousarray(h)
+    nt, np_ = a.shape
+    if a.dtype == np.float32:
+        return lib().orc_film_volume_f32(_p(a), nt, np_, float(radius))
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return lib().orc_film_volume_f64(_p(a), nt, np_, float(radius))
+
+
+def transmission_angle_cos(n, ci):
+    return lib().orc_transmission_angle_cos(float(n), float(ci))
+
+
+def optical_path_difference(n, t, ct, wl):
+    return lib().orc_optical_path_difference(float(n), float(t), float(ct), float(wl))
+
+
+def phase_difference(opd, wl):
+    return lib().orc_phase_difference(float(opd), float(wl))
+
+
+def fresnel(n, ci):
+    out = np.zeros(3)
+    lib().orc_fresnel(float(n), float(ci), _p(out))
+    return out
+
+
+def reflected_intensity(n, t, ci, wl):
+    return lib().orc_reflected_intensity(float(n), float(t), float(ci), float(wl))
+
+
+def interference_color(n, t, ci, gamma=True, wl=(650.0, 532.0, 450.0)):
+    w = np.asarray(wl, dtype=np.float64)
+    out = np.zeros(3)
+    lib().orc_interference_color(float(n), _p(w), float(t), float(ci), 1 if gamma else 0, _p(out))
+    return out
+
+
+def interference_color_batch(n, t, ci, gamma=True, wl=(650.0, 532.0, 450.0)):
+    w = np.asarray(wl, dtype=np.float64)
+    t = np.ascontiguousarray(t, dtype=np.float64).reshape(-1)
+    ci = np.ascontiguousarray(ci, dtype=np.float64).reshape(-1)
+    out = np.zeros((t.size, 3))
+    lib().orc_interference_color_batch(float(n), _p(w), _p(t), _p(ci), t.size, 1 if gamma else 0, _p(out))
+    return out
+
+
+def lut1d(n, tmin, tmax, count, ci, wl=(650.0, 532.0, 450.0)):
+    w = np.asarray(wl, dtype=np.float64)
+    out = np.zeros((count, 3))
+    lib().orc_lut1d(float(n), _p(w), float(tmin), float(tmax), int(count), float(ci), _p(out))
+    return out
+
+
+def lut2d(n, tmin, tmax, T, A, wl=(650.0, 532.0, 450.0)):
+    w = np.asarray(wl, dtype=np.float64)
+    out = np.zeros((T, A, 3))
+    lib().orc_lut2d(float(n), _p(w), float(tmin), float(tmax), int(T), int(A), _p(out))
+    return out
+
+
+def interference_lut_rgba8(n, intensity):
+    out = np.zeros(64 * 256 * 4, dtype=np.uint8)
+    lib().orc_interference_lut_rgba8(float(n), float(intensity), _p(out))
+    return out
+
+
+def thin_film_interference7(t, ci, n, intensity):
+    out = np.zeros(3, dtype=np.float32)
+    lib().orc_thin_film_interference7(float(t), float(ci), float(n), float(intensity), _p(out))
+    return out
+
+
+def lut_snells_law(ci, n):
+    return lib().orc_lut_snells_law(float(ci), float(n))
+
+
+def lut_fresnel_unpolarized(ci, ct, n1, n2):
+    return lib().orc_lut_fresnel_unpolarized(float(ci), float(ct), float(n1), float(n2))
+
+
+def schlick_interference(t, wl, ci, n):
+    return lib().orc_schlick_interference(float(t), float(wl), float(ci), float(n))
+
+
+def lut_rgba8_sample(lut, W, H, t, ci, max_nm=2000.0, intensity=1.0):
+    L = np.ascontiguousarray(lut, dtype=np.uint8).reshape(-1)
+    out = np.zeros(3, dtype=np.float32)
+    lib().orc_lut_rgba8_sample(_p(L), int(W), int(H), float(t), float(ci), float(max_nm), float(intensity), _p(out))
+    return out
+
+
+def lut2d_lookup(lut, tmin, tmax, t, ci):
+    L = np.ascontiguousarray(lut, dtype=np.float64)
+    out = np.zeros(3)
+    lib().orc_lut2d_lookup(_p(L), L.shape[0], L.shape[1], float(tmin), float(tmax), float(t), float(ci), _p(out))
+    return out
+
+
+def vertex_colors(field, xyz, lut, tmin, tmax):
+    F = np.ascontiguousarray(field, dtype=np.float64)
+    X = np.ascontiguousarray(xyz, dtype=np.float64)
+    L = np.ascontiguousarray(lut, dtype=np.float64)
+    out = np.zeros((X.shape[0], 3))
+    lib().orc_vertex_colors(_p(F), F.shape[0], F.shape[1], _p(X), X.shape[0], _p(L), L.shape[0], L.shape[1],
+                            float(tmin), float(tmax), _p(out))
+    return out
+
+
+def spectral_rgb(t, ci, n, wl, cmf):
+    t = np.ascontiguousarray(t, dtype=np.float32)
+    ci = np.ascontiguousarray(ci, dtype=np.float32)
+    n = np.ascontiguousarray(n, dtype=np.float32)
+    wl = np.ascontiguousarray(wl, dtype=np.float64)
+    cmf = np.ascontiguousarray(cmf, dtype=np.float64)
+    out = np.zeros((t.size, 3))
+    lib().orc_spectral_rgb(_p(t), _p(ci), _p(n), t.size, _p(wl), wl.size, _p(cmf), _p(out))
+    return out

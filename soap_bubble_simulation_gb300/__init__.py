@@ -1,0 +1,25 @@
+"""GB300-native film-drainage and thin-film-interference path of the soap-bubble simulation.
+
+Drop-in for the reference's `physics::drainage`, `physics::interference` and
+`render::{gpu_drainage, interference_lut}` APIs, computed by hand-written
+CUDA kernels for sm_103a behind the C ABI in include/sbs.h (libsbs.so).
+"""
+from . import _native
+from .config import (BubbleParameters, ConfigError, EnvironmentParameters, FluidParameters,
+                     SimulationConfig)
+from .drainage import (DeviceField, DrainageParams, DrainageSimulator, GPUDrainageSimulator,
+                       ThicknessField, film_volume_device)
+from .interference import (LUT_ANGLE_SAMPLES, LUT_MAX_THICKNESS_NM, LUT_THICKNESS_SAMPLES,
+                           FresnelCoefficients, InterferenceCalculator, RgbColor, constants,
+                           generate_interference_lut, generate_interference_lut_array, lookup_2d,
+                           sample_interference_lut, schlick_interference_rgb, wavelengths)
+from ._native import SbsError
+
+__all__ = [
+    "BubbleParameters", "ConfigError", "EnvironmentParameters", "FluidParameters", "SimulationConfig",
+    "DeviceField", "DrainageParams", "DrainageSimulator", "GPUDrainageSimulator", "ThicknessField",
+    "film_volume_device", "LUT_ANGLE_SAMPLES", "LUT_MAX_THICKNESS_NM", "LUT_THICKNESS_SAMPLES",
+    "FresnelCoefficients", "InterferenceCalculator", "RgbColor", "constants", "generate_interference_lut",
+    "generate_interference_lut_array", "lookup_2d", "sample_interference_lut", "schlick_interference_rgb",
+    "wavelengths", "SbsError",
+]

@@ -1,0 +1,101 @@
+// Error reporting, version, device probe and configuration defaults.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+
+#include "sbs_internal.h"
+
+namespace sbs {
+
+namespace {
+thread_local char g_last_error[1024] = "";
+}
+
+int set_error(int code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+void clear_error() { g_last_error[0] = '\0'; }
+
+int require_device() {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(SBS_E_CUDA, "no usable CUDA device: %s", cudaGetErrorString(e));
+    }
+    if (n <= 0) return set_error(SBS_E_CUDA, "no CUDA device visible");
+    return SBS_OK;
+}
+
+}  // namespace sbs
+
+extern "C" {
+
+const char *sbs_last_error(void) { return sbs::g_last_error; }
+
+const char *sbs_version(void) { return "sbs 0.1.0 (sm_103a)"; }
+
+int sbs_device_count(int *out) {
+    SBS_CHECK_ARG(out != nullptr, "out is null");
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *out = 0;
+        return sbs::set_error(SBS_E_CUDA, "cudaGetDeviceCount: %s", cudaGetErrorString(e));
+    }
+    *out = n;
+    return SBS_OK;
+}
+
+// SimulationConfig::default (config.rs:305-316) with BubbleParameters (:26-35),
+// FluidParameters (:56-66) and EnvironmentParameters (:93-103) defaults.
+int sbs_config_default(sbs_config *out) {
+    SBS_CHECK_ARG(out != nullptr, "out is null");
+    std::memset(out, 0, sizeof(*out));
+    out->diameter = 0.05;
+    out->film_thickness_nm = 500.0;
+    out->critical_thickness_nm = 10.0;
+    out->refractive_index = 1.33;
+    out->viscosity = 0.001;
+    out->surface_tension = 0.025;
+    out->density = 1000.0;
+    out->surfactant_diffusion = 1e-9;
+    out->surfactant_concentration = 0.5;
+    out->gravity = 9.81;
+    out->temperature = 293.15;
+    out->pressure = 101325.0;
+    out->dt = 0.001;
+    out->resolution = 128;
+    return SBS_OK;
+}
+
+// DrainageParams::default (gpu_drainage.rs:46-68).
+int sbs_drainage_params_default(sbs_drainage_params *out) {
+    SBS_CHECK_ARG(out != nullptr, "out is null");
+    std::memset(out, 0, sizeof(*out));
+    out->dt = 0.001f;
+    out->gravity = 9.81f;
+    out->viscosity = 0.001f;
+    out->density = 1000.0f;
+    out->diffusion_coeff = 1e-9f;
+    out->bubble_radius = 0.025f;
+    out->critical_thickness = 30e-9f;
+    out->grid_width = 128;
+    out->grid_height = 64;
+    out->marangoni_enabled = 0;
+    out->gamma_air = 0.072f;
+    out->gamma_reduction = 0.045f;
+    out->surfactant_diffusion = 1e-9f;
+    out->marangoni_coeff = 0.01f;
+    return SBS_OK;
+}
+
+}  // extern "C"

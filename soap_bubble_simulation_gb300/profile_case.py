@@ -1,0 +1,50 @@
+"""Runs one drainage workload for a fixed number of steps, for profilers (ncu) to attach to.
+
+    python -m soap_bubble_simulation_gb300.profile_case --case wgsl --res 2048 --steps 20
+
+Cases: `wgsl` (GPUDrainageSimulator semantics, h + surfactant), `cpu` (DrainageSimulator
+semantics, compensated f32x2), `cpu32` (plain f32). The field is the seeded smooth-mode field of
+the 2048-resolution workload, built at the requested resolution. Steps launch one kernel each
+(graph replay for runs of 8 or more).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+
+from . import _native as N
+from . import synthetic
+from .config import SimulationConfig
+from .drainage import DrainageSimulator, GPUDrainageSimulator, _Handle
+
+
+def main(argv=None) -> None:
+    p = argparse.ArgumentParser()
+    p.add_argument("--case", default="wgsl", choices=["wgsl", "cpu", "cpu32"])
+    p.add_argument("--res", type=int, default=2048)
+    p.add_argument("--steps", type=int, default=20)
+    a = p.parse_args(argv)
+    h, c = synthetic.bubble_c1(a.res)
+    if a.case == "wgsl":
+        sim = GPUDrainageSimulator(None, 550e-9, 2 * a.res, a.res)
+        sim.set_thickness_array(h)
+        sim.set_concentration_array(c)
+        sim.run(a.steps)
+    else:
+        cfg = SimulationConfig()
+        cfg.resolution = a.res
+        cc = cfg.to_c()
+        hh = ctypes.c_void_p()
+        prec = N.DRAIN_F32X2 if a.case == "cpu" else N.DRAIN_F32
+        N.call("sbs_drainage_create_ex", ctypes.byref(cc), prec, ctypes.byref(hh))
+        sim = DrainageSimulator.__new__(DrainageSimulator)
+        _Handle.__init__(sim)
+        sim._h = hh
+        sim.set_thickness_array(h)
+        sim.step_n(cfg.dt, a.steps)
+    sim.close()
+    print(f"ran {a.steps} steps of case {a.case} at resolution {a.res}")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,85 @@
+"""Seeded synthetic inputs for the benchmark workloads (no datasets exist for this path).
+
+All generators use numpy's PCG64 with fixed seeds, so every run and every
+machine builds the same inputs:
+
+* bubble_c0: one bubble, resolution 128 (128 x 256), h = 500 nm (1 + 0.05 U[-1,1]), seed 0.
+* bubble_c1: resolution 2048 (2048 x 4096), h = 550 nm + 16 smooth modes
+  a_k cos(m_k theta + psi_k) cos(n_k phi + chi_k), a_k ~ N(0, 60 nm), m_k in 1..8,
+  n_k in 0..8, clamped to [100, 1000] nm; surfactant 0.5 + U[-0.1, 0.1].
+* icosphere(5): the 10242 unit vertices of a subdivision-5 icosphere.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def rng(seed: int) -> np.random.Generator:
+    return np.random.Generator(np.random.PCG64(seed))
+
+
+def bubble_c0(resolution: int = 128, seed: int = 0, h0: float = 500e-9, noise: float = 0.05) -> np.ndarray:
+    """Initial thickness [theta][phi] (metres, f64)."""
+    g = rng(seed)
+    nt, np_ = resolution, 2 * resolution
+    return h0 * (1.0 + noise * g.uniform(-1.0, 1.0, size=(nt, np_)))
+
+
+def smooth_modes(nt: int, np_: int, seed: int = 1, modes: int = 16, base: float = 550e-9, amp: float = 60e-9,
+                 lo: float = 100e-9, hi: float = 1000e-9) -> np.ndarray:
+    """Sum of separable cosine modes on the theta-phi grid (f64, metres)."""
+    g = rng(seed)
+    a = g.normal(0.0, amp, size=modes)
+    m = g.integers(1, 9, size=modes)
+    n = g.integers(0, 9, size=modes)
+    psi = g.uniform(0.0, 2 * math.pi, size=modes)
+    chi = g.uniform(0.0, 2 * math.pi, size=modes)
+    theta = np.arange(nt) * (math.pi / (nt - 1))
+    phi = np.arange(np_) * (2 * math.pi / np_)
+    U = a[None, :] * np.cos(m[None, :] * theta[:, None] + psi[None, :])  # [nt, modes]
+    V = np.cos(n[None, :] * phi[:, None] + chi[None, :])  # [np, modes]
+    h = base + U @ V.T
+    return np.clip(h, lo, hi)
+
+
+def surfactant_noise(nt: int, np_: int, seed: int = 2, mean: float = 0.5, spread: float = 0.1) -> np.ndarray:
+    g = rng(seed)
+    return (mean + g.uniform(-spread, spread, size=(nt, np_))).astype(np.float32)
+
+
+def bubble_c1(resolution: int = 2048, seed: int = 1) -> tuple[np.ndarray, np.ndarray]:
+    """(h f32 [nt][np] metres, surfactant f32 [nt][np])."""
+    nt, np_ = resolution, 2 * resolution
+    h = smooth_modes(nt, np_, seed=seed).astype(np.float32)
+    c = surfactant_noise(nt, np_, seed=seed + 1)
+    return h, c
+
+
+def icosphere(subdivisions: int = 5) -> np.ndarray:
+    """Unit vertices of an icosphere, [10 * 4^s + 2, 3] f64, deterministic order."""
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+             (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    verts = [np.array(v, dtype=np.float64) / np.linalg.norm(v) for v in verts]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+             (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(subdivisions):
+        cache: dict[tuple[int, int], int] = {}
+
+        def mid(a: int, b: int) -> int:
+            key = (a, b) if a < b else (b, a)
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    return np.array(verts, dtype=np.float64)

@@ -1,0 +1,272 @@
+"""Pins the drainage oracle: the reference's own drainage.rs unit tests (drainage.rs:616-720),
+independent numpy restatements and analytic checks. CPU only."""
+import math
+
+import numpy as np
+import pytest
+
+EPS = np.finfo(np.float64).eps
+
+
+# --- drainage.rs:621-633 (ThicknessField) -----------------------------------------------------
+def test_thickness_field_creation():
+    from soap_bubble_simulation_gb300 import ThicknessField
+
+    f = ThicknessField(64, 128, 500e-9)
+    assert f.num_theta() == 64
+    assert f.num_phi() == 128
+    assert abs(f.get(0, 0) - 500e-9) < EPS
+
+
+def test_thickness_field_get_set():
+    from soap_bubble_simulation_gb300 import ThicknessField
+
+    f = ThicknessField(64, 128, 500e-9)
+    f.set(10, 20, 400e-9)
+    assert abs(f.get(10, 20) - 400e-9) < EPS
+    assert abs(f.delta_theta() - math.pi / 63) < 1e-15
+    assert abs(f.phi_at(64) - math.pi) < 1e-15
+
+
+# --- drainage.rs:636-719 (DrainageSimulator), on the oracle in both precisions ----------------
+@pytest.mark.parametrize("precision", ["f64", "f32k", "f32x2"])
+def test_drainage_simulator_creation(orc, precision):
+    s = orc.CpuSim(precision=precision)
+    assert abs(s.current_time()) < EPS
+    assert not s.has_critical_region()
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32k"])
+def test_drainage_step_advances_time(orc, precision):
+    s = orc.CpuSim(precision=precision)
+    s.step(0.001)
+    assert abs(s.current_time() - 0.001) < EPS
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32k"])
+def test_get_thickness_interpolation(orc, precision):
+    s = orc.CpuSim(precision=precision)
+    assert abs(s.get_thickness(0.5, 1.0) - s.get_thickness(1.5, 3.0)) < 1e-15
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32x2"])
+def test_drainage_causes_thinning_at_top(orc, precision):
+    s = orc.CpuSim(precision=precision)
+    before = s.get_thickness(0.1, 0.0)
+    for _ in range(100):
+        s.step(0.001)
+    after = s.get_thickness(0.1, 0.0)
+    assert after < before, (before, after)
+
+
+def test_plain_f32_loses_the_gravity_increment(orc):
+    """Why the compensated storage exists: at 500 nm the per-step gravity increment is ~1/1000
+    of an f32 ulp, so a plain-f32 uniform field does not thin at all, while f32x2 thins by the
+    same amount as f64."""
+    d = {}
+    for p in ("f64", "f32k", "f32x2"):
+        s = orc.CpuSim(precision=p)
+        b = s.get_thickness(0.1, 0.0)
+        s.step_n(0.001, 100)
+        d[p] = b - s.get_thickness(0.1, 0.0)
+    assert d["f32k"] == 0.0
+    assert d["f32x2"] == pytest.approx(d["f64"], rel=1e-6)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32k"])
+def test_phi_periodicity(orc, precision):
+    s = orc.CpuSim(precision=precision)
+    s.set_field(np.random.default_rng(3).uniform(400e-9, 600e-9, size=(128, 256)))
+    assert abs(s.get_thickness(1.0, 0.0) - s.get_thickness(1.0, 2 * math.pi)) < 1e-12
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32k", "f32x2"])
+def test_reset(orc, precision):
+    s = orc.CpuSim(precision=precision)
+    for _ in range(10):
+        s.step(0.001)
+    s.reset(600e-9)
+    assert abs(s.current_time()) < EPS
+    # 1e-15 as in the reference; plain f32 storage can only hold 600 nm to half an f32 ulp
+    tol = 1e-15 if precision != "f32k" else 600e-9 * 2.0**-24
+    assert abs(s.get_thickness(0.5, 0.5) - 600e-9) < tol
+
+
+# --- independent numpy restatement of one step (drainage.rs:298-392) ---------------------------
+def numpy_step(h, dt, R=0.025, rho=1000.0, g=9.81, eta=1e-3, D=1e-9, hc=10e-9):
+    nt, np_ = h.shape
+    dth, dph = math.pi / (nt - 1), 2 * math.pi / np_
+    out = h.copy()
+    coef = rho * g / (3.0 * eta)
+    for i in range(1, nt - 1):
+        th = i * dth
+        s, c = math.sin(th), math.cos(th)
+        ss = math.copysign(1e-10, s) if abs(s) < 1e-10 else s
+        hcur = h[i]
+        d2t = (h[i + 1] - 2.0 * hcur + h[i - 1]) / (dth * dth)
+        d1t = (h[i + 1] - h[i - 1]) / (2.0 * dth)
+        hp, hm = np.roll(hcur, -1), np.roll(hcur, 1)
+        d2p = (hp - 2.0 * hcur + hm) / (dph * dph)
+        lap = (d2t + c / ss * d1t + d2p / (ss * ss)) / (R * R)
+        new = np.maximum(hcur + dt * (-coef * hcur ** 3 * s + D * lap), 0.0)
+        out[i] = np.where(hcur < hc, hcur, new)
+    out[0] = out[1].sum() / np_
+    out[-1] = out[-2].sum() / np_
+    return out
+
+
+def test_step_matches_numpy_restatement(orc):
+    h0 = np.random.default_rng(5).uniform(300e-9, 700e-9, size=(24, 48))
+    h0[5, 7] = 5e-9  # below critical: frozen
+    s = orc.CpuSim(resolution=24)
+    s.set_marginal_regeneration(False)
+    s.set_field(h0)
+    want = h0
+    for _ in range(5):
+        s.step(0.001)
+        want = numpy_step(want, 0.001)
+    got = s.field()
+    assert np.max(np.abs(got - want)) / np.max(np.abs(want)) < 1e-14
+    assert got[5, 7] == 5e-9
+
+
+def test_uniform_field_gravity_only_ode(orc):
+    """D = 0, TFE off: every interior cell follows h' = h - dt C h^3 sin(theta) exactly."""
+    s = orc.CpuSim(resolution=32, surfactant_diffusion=0.0)
+    s.set_marginal_regeneration(False)
+    s.step(0.5)
+    got = s.field()
+    C = 1000.0 * 9.81 / 3e-3
+    th = np.arange(32) * (math.pi / 31)
+    want = 500e-9 - 0.5 * C * (500e-9) ** 3 * np.sin(th)
+    np.testing.assert_allclose(got[1:-1, 0], want[1:-1], rtol=1e-15)
+    assert got[0, 0] == pytest.approx(want[1], rel=1e-15)
+
+
+# --- marginal regeneration schedule (drainage.rs:395-477) -------------------------------------
+def tfe_schedule(n_steps, dt):
+    """Python restatement of the spawn/advance/retain bookkeeping; returns fronts after each step."""
+    t, nxt, fronts, hist = 0.0, 0.5, [], []
+    for _ in range(n_steps):
+        nxt -= dt
+        if nxt <= 0.0:
+            phi = abs(math.sin(t * 7.89 + 1.23)) * 2.0 * math.pi
+            width = 0.3 + abs(math.sin(t * 3.21)) * 0.4
+            vel = 0.05 + abs(math.cos(t * 5.67)) * 0.05
+            fronts.append([phi, 0.0, width, vel])
+            if len(fronts) > 8:
+                fronts.pop(0)
+            nxt = 2.0 * (0.5 + abs(math.sin(t * 12.345)))
+        for f in fronts:
+            f[1] = min(f[1] + f[3] * dt, math.pi / 2)
+        fronts = [f for f in fronts if f[1] < math.pi / 2 * 0.95]
+        hist.append([list(f) for f in fronts])
+        t += dt
+    return hist
+
+
+def test_tfe_schedule_matches_restatement(orc):
+    s = orc.CpuSim(resolution=16)
+    hist = tfe_schedule(3000, 0.001)
+    for k in range(3000):
+        s.step(0.001)
+        if k % 250 == 0 or k in (498, 499, 500, 501):
+            got = s.fronts()
+            want = np.array(hist[k]).reshape(-1, 4)
+            assert got.shape == want.shape, k
+            np.testing.assert_array_equal(got, want)
+    assert s.active_tfe_count() >= 1
+
+
+def test_tfe_thins_only_inside_fronts(orc):
+    """With D = 0 and gravity off, only TFE changes h: cells inside a front shrink by exactly
+    (1 - 0.075 dt) per step (ratio 0.85)."""
+    s = orc.CpuSim(resolution=64, surfactant_diffusion=0.0, gravity=0.0)
+    s.step_n(0.01, 150)  # first front spawns at t = 0.5 s, reaches the rows next to the equator later
+    f = s.field()
+    assert s.active_tfe_count() >= 1
+    ratio = f / 500e-9
+    assert np.all(ratio <= 1.0 + 1e-15)
+    thinned = ratio < 1.0 - 1e-12
+    assert thinned.any()
+    # the thinned set is a band around the equator
+    rows = np.where(thinned.any(axis=1))[0]
+    assert abs((rows.min() + rows.max()) / 2 - 31.5) <= 1.0
+
+
+def test_tfe_ratio_clamp(orc):
+    s = orc.CpuSim()
+    s.set_tfe_thickness_ratio(0.1)
+    assert s.tfe_thickness_ratio() == 0.5
+    s.set_tfe_thickness_ratio(2.0)
+    assert s.tfe_thickness_ratio() == 0.95
+
+
+# --- precision of the CUDA kernel's f32 arithmetic, checked on the CPU --------------------------
+def rel_linf(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+@pytest.mark.parametrize("precision", ["f32k", "f32x2"])
+def test_f32_kernel_order_per_step_tolerance(orc, precision):
+    from soap_bubble_simulation_gb300 import synthetic
+
+    h0 = synthetic.bubble_c0(128, seed=0).astype(np.float32).astype(np.float64)
+    a = orc.CpuSim(precision="f64")
+    b = orc.CpuSim(precision=precision)
+    for k in range(20):
+        a.set_field(h0 if k == 0 else b.field())
+        if k == 0:
+            b.set_field(h0)
+        a.step(0.001)
+        b.step(0.001)
+        assert rel_linf(b.field(), a.field()) <= 1e-5
+
+
+@pytest.mark.parametrize("precision,tol", [("f32k", 1e-4), ("f32x2", 1e-8)])
+def test_f32_kernel_order_1000_steps_c0(orc, precision, tol):
+    """Config 0 at the reference dt, 1000 steps, TFE on: relative L-inf vs f64 within 1e-4
+    (plain f32; measured 5.4e-5) and 1e-8 (compensated; measured 1.5e-9)."""
+    from soap_bubble_simulation_gb300 import synthetic
+
+    h0 = synthetic.bubble_c0(128, seed=0).astype(np.float32).astype(np.float64)
+    a = orc.CpuSim(precision="f64", threads=0)
+    b = orc.CpuSim(precision=precision, threads=0)
+    a.set_field(h0)
+    b.set_field(h0)
+    a.step_n(0.001, 1000)
+    b.step_n(0.001, 1000)
+    err = rel_linf(b.field(), a.field())
+    assert err <= tol, err
+    assert a.active_tfe_count() == b.active_tfe_count() >= 1
+
+
+def test_volume_of_uniform_field(orc):
+    """Sum h R^2 sin dth dphi over a uniform field approaches 4 pi R^2 h."""
+    R, h = 0.025, 500e-9
+    f = np.full((512, 1024), h)
+    v = orc.film_volume(f, R)
+    assert v == pytest.approx(4 * math.pi * R * R * h, rel=1e-4)
+    assert orc.film_volume(f.astype(np.float32), R) == pytest.approx(v, rel=1e-7)
+
+
+# --- WGSL semantics: faithful operation order vs the CUDA kernel's order -----------------------
+def test_wgsl_kernel_order_close_to_wgsl_order(orc):
+    from soap_bubble_simulation_gb300 import synthetic
+
+    h = synthetic.smooth_modes(64, 128).astype(np.float32)
+    c = synthetic.surfactant_noise(64, 128)
+    for mar in (0, 1):
+        p = orc.wgsl_params(marangoni_enabled=mar)
+        h1, c1 = orc.wgsl_run(p, h, c, 1, "wgsl")
+        h2, c2 = orc.wgsl_run(p, h, c, 1, "kernel")
+        assert rel_linf(h2, h1) <= 1e-5
+        assert np.max(np.abs(c2 - c1)) <= 1e-5
+        hN, cN = orc.wgsl_run(p, h, c, 1000, "wgsl")
+        hK, cK = orc.wgsl_run(p, h, c, 1000, "kernel")
+        assert rel_linf(hK, hN) <= 1e-4
+        assert np.max(np.abs(cK - cN)) <= 1e-4
+        # poles copied (drainage.wgsl:85-89)
+        np.testing.assert_array_equal(hN[0], h[0])
+        np.testing.assert_array_equal(hN[-1], h[-1])
+        np.testing.assert_array_equal(cK[-1], c[-1])
