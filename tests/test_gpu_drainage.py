@@ -219,8 +219,12 @@ def test_errors_are_reported(sbs):
     with pytest.raises(sbs.SbsError):
         make_sim(sbs, 2)
     sim = make_sim(sbs, 16)
-    with pytest.raises(sbs.SbsError):
+    with pytest.raises(ValueError):
         sim.set_thickness_array(np.zeros((15, 32), np.float32))
+    short = np.zeros(15 * 32, np.float32)
+    with pytest.raises(sbs.SbsError, match="expected 16 x 32"):
+        sbs._native.call("sbs_drainage_set_thickness", sim.handle, sbs._native.ptr(short), short.size,
+                         sbs._native.MEM_HOST)
     with pytest.raises(sbs.SbsError):
         sim.step(float("nan"))
     with pytest.raises(sbs.SbsError, match="WGSL"):
