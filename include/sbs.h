@@ -250,6 +250,27 @@ int sbs_gpu_drainage_set_steps_per_frame(sbs_drainage *h, uint32_t steps);
 int sbs_film_volume_device(const float *h, uint32_t num_theta, uint32_t num_phi, size_t pitch, double radius,
                            double *out, void *stream);
 
+/* The same film volume as sbs_film_volume_device, computed without allocating
+ * any memory. It has no counterpart in the reference. It is meant for callers
+ * that must not allocate GPU memory while they run: for example an engine that
+ * has given the GPU's memory to its own pool and budgets it per frame, or a
+ * real-time loop that cannot afford the stall an allocation may cause. Instead
+ * of asking CUDA for scratch space, the call works in one fixed array of
+ * 155,680 bytes that libsbs places in device memory when it is loaded; every GPU
+ * that loads the library keeps that array until the process exits.
+ * Rules:
+ *  - num_theta <= 16384 (the rows whose weights fit in the array); larger
+ *    grids are rejected with SBS_E_INVALID.
+ *  - The first call on each device looks up the array's device address; make
+ *    that first call before any stream capture on that device.
+ *  - Every call uses the same array, which keeps the previous call's contents
+ *    (the call clears its own counter). Calls whose work overlaps on the GPU,
+ *    from different streams or threads, race and can return wrong sums:
+ *    serialise them.
+ *  - Synchronous: returns after the result has been copied to *out. */
+int sbs_film_volume_device_noalloc(const float *h, uint32_t num_theta, uint32_t num_phi, size_t pitch,
+                                   double radius, double *out, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* Interference (interference.rs:127-512)                              */
 /* ------------------------------------------------------------------ */

@@ -159,6 +159,7 @@ SIGNATURES: dict[str, list] = {
     "sbs_gpu_drainage_set_time_scale": [_P, _F],
     "sbs_gpu_drainage_set_steps_per_frame": [_P, _U32],
     "sbs_film_volume_device": [_P, _U32, _U32, _SZ, _D, _DP, _P],
+    "sbs_film_volume_device_noalloc": [_P, _U32, _U32, _SZ, _D, _DP, _P],
     "sbs_interference_color_batch": [_D, _DP, _P, _P, _SZ, _I, _I, _P, _I, _P],
     "sbs_interference_terms_batch": [_D, _D, _P, _P, _SZ, _P, _I, _P],
     "sbs_optical_path_batch": [_D, _P, _P, _P, _SZ, _P, _I, _P],
