@@ -235,6 +235,13 @@ int sbs_gpu_drainage_set_bubble_radius(sbs_drainage *h, float radius);
 int sbs_gpu_drainage_set_marangoni_enabled(sbs_drainage *h, int enabled);
 int sbs_gpu_drainage_set_marangoni_params(sbs_drainage *h, float gamma_air, float gamma_reduction,
                                           float surfactant_diffusion, float marangoni_coeff);
+/* Steps advanced per kernel launch (no reference counterpart). 2..4 use the
+ * temporally blocked kernel (one read and one write of the fields per K steps;
+ * grid_width must be a multiple of 4), 0 or 1 launch one step at a time. The
+ * results are bit-identical either way. Default 4 where supported. */
+int sbs_gpu_drainage_set_time_blocking(sbs_drainage *h, int steps_per_launch);
+int sbs_gpu_drainage_time_blocking(const sbs_drainage *h, int *out);
+
 /* Public fields of GPUDrainageSimulator (gpu_drainage.rs:100-107). */
 int sbs_gpu_drainage_set_enabled(sbs_drainage *h, int enabled);
 int sbs_gpu_drainage_set_time_scale(sbs_drainage *h, float time_scale);

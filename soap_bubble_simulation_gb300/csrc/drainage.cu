@@ -228,14 +228,25 @@ int allocate(sbs_drainage *h) {
             SBS_CUDA_TRY(cudaMemset(h->hl[i], 0, bytes));
         }
     }
-    h->geom = step_geometry(h->nt, h->np);
+    h->geom = step_geometry(h->nt, h->np, h->sem, h->x2);
+    if (h->sem == SBS_WGSL_SEMANTICS && wtb_supported(h->nt, h->np)) {
+        h->wtb_k = 4;
+        h->wgeom = wtb_geometry(h->nt, h->np, h->wtb_k);
+    }
     for (int i = 0; i < 2; ++i) {
         SBS_CUDA_TRY(cudaMalloc(&h->part[i], sizeof(double) * 4 * h->geom.nbx));
         SBS_CUDA_TRY(cudaMemset(h->part[i], 0, sizeof(double) * 4 * h->geom.nbx));
     }
     SBS_CUDA_TRY(cudaMalloc(&h->rows, sizeof(float4) * h->nt));
     SBS_CUDA_TRY(cudaMalloc(&h->vol_w, sizeof(double) * h->nt));
-    SBS_CUDA_TRY(cudaMalloc(&h->vol_partials, sizeof(double) * (size_t)h->geom.nbx * h->geom.nby));
+    // one volume partial per block of whichever step kernel runs the check
+    size_t vol_blocks = (size_t)h->geom.nbx * h->geom.nby;
+    if (h->sem == SBS_WGSL_SEMANTICS && wtb_supported(h->nt, h->np))
+        for (int k = 2; k <= 4; ++k) {
+            const StepGeom g = wtb_geometry(h->nt, h->np, k);
+            vol_blocks = std::max(vol_blocks, (size_t)g.nbx * g.nby);
+        }
+    SBS_CUDA_TRY(cudaMalloc(&h->vol_partials, sizeof(double) * vol_blocks));
     SBS_CUDA_TRY(cudaMalloc(&h->vol_counter, sizeof(unsigned) * 2));
     SBS_CUDA_TRY(cudaMemset(h->vol_counter, 0, sizeof(unsigned) * 2));
     h->vol_index = h->vol_counter + 1;
@@ -279,12 +290,28 @@ void release(sbs_drainage *h) {
 }
 
 // Enqueues `count` steps starting from buffer `start`; returns the buffer holding the result.
-// Step i reads pole rows from memory when i == 0 (the chunk starts from a materialised field) and
-// from the ring partials of step i-1 otherwise; the chunk ends by materialising the pole rows.
-int enqueue_steps(sbs_drainage *h, int start, int count, float dt, bool vol_last, bool use_sched, int *end) {
+// CPU semantics: step i reads pole rows from memory when i == 0 (the chunk starts from a
+// materialised field) and from the ring partials of step i-1 otherwise; the chunk ends by
+// materialising the pole rows. WGSL semantics: runs of wtb_k steps go through the temporally
+// blocked kernel; with last_single the final step is a single-step launch, so the other buffer
+// ends one pass behind the newest (what the reference's current_buffer() returns).
+int enqueue_steps(sbs_drainage *h, int start, int count, float dt, bool vol_last, bool use_sched, bool last_single,
+                  int *end) {
     const Consts &k = consts_of(h);
+    std::vector<int> plan;  // steps per launch
+    if (h->sem == SBS_WGSL_SEMANTICS && h->wtb_k > 1) {
+        int rem = count - (last_single && count > 0 ? 1 : 0);
+        while (rem >= h->wtb_k) {
+            plan.push_back(h->wtb_k);
+            rem -= h->wtb_k;
+        }
+        for (; rem > 0; --rem) plan.push_back(1);
+        if (last_single && count > 0) plan.push_back(1);
+    } else {
+        plan.assign(count, 1);
+    }
     int cur = start;
-    for (int i = 0; i < count; ++i) {
+    for (size_t i = 0; i < plan.size(); ++i) {
         StepArgs a{};
         a.hin = h->h[cur];
         a.hout = h->h[cur ^ 1];
@@ -296,7 +323,7 @@ int enqueue_steps(sbs_drainage *h, int start, int count, float dt, bool vol_last
         a.pin = h->part[(i + 1) & 1];
         a.pout = h->part[i & 1];
         a.tfe = use_sched ? h->sched_dev + i : nullptr;
-        const bool vol = vol_last && i == count - 1;
+        const bool vol = vol_last && i + 1 == plan.size();
         a.vol_w = vol ? h->vol_w : nullptr;
         a.vol_partials = h->vol_partials;
         a.vol_counter = h->vol_counter;
@@ -305,7 +332,7 @@ int enqueue_steps(sbs_drainage *h, int start, int count, float dt, bool vol_last
         a.nt = h->nt;
         a.np = h->np;
         a.pitch = (int)h->pitch;
-        a.rb = h->geom.rb;
+        a.rb = plan[i] > 1 ? h->wgeom.rb : h->geom.rb;
         a.poles_virtual = i > 0 ? 1 : 0;
         a.marangoni = h->params.marangoni_enabled ? 1 : 0;
         a.crit = k.crit;
@@ -315,7 +342,10 @@ int enqueue_steps(sbs_drainage *h, int start, int count, float dt, bool vol_last
         a.Gt = k.Gt;
         a.M = k.M;
         a.dt = dt;
-        SBS_CUDA_TRY(launch_step(h->sem, h->x2, a, h->geom, h->stream));
+        if (plan[i] > 1)
+            SBS_CUDA_TRY(launch_wtb(plan[i], a, h->wgeom, h->stream));
+        else
+            SBS_CUDA_TRY(launch_step(h->sem, h->x2, a, h->geom, h->stream));
         cur ^= 1;
     }
     if (h->sem == SBS_CPU_SEMANTICS && count > 0)
@@ -325,8 +355,16 @@ int enqueue_steps(sbs_drainage *h, int start, int count, float dt, bool vol_last
     return SBS_OK;
 }
 
+// Number of launches enqueue_steps uses for `count` steps (each flips the ping-pong buffers).
+int launches_in(const sbs_drainage *h, int count, bool last_single) {
+    if (!(h->sem == SBS_WGSL_SEMANTICS && h->wtb_k > 1)) return count;
+    const int tail = last_single && count > 0 ? 1 : 0;
+    const int body = count - tail;
+    return body / h->wtb_k + body % h->wtb_k + tail;
+}
+
 // Runs one chunk (count <= kMaxChunk) through a cached CUDA graph (or directly when short).
-int run_chunk(sbs_drainage *h, int count, double dt, bool vol_last) {
+int run_chunk(sbs_drainage *h, int count, double dt, bool vol_last, bool last_single) {
     const bool cpu = h->sem == SBS_CPU_SEMANTICS;
     const bool use_sched = cpu && h->tfe.enabled;
     float dtf;
@@ -353,19 +391,20 @@ int run_chunk(sbs_drainage *h, int count, double dt, bool vol_last) {
     }
     int end = h->cur;
     if (count < kGraphMin) {
-        int rc = enqueue_steps(h, h->cur, count, dtf, vol_last, use_sched, &end);
+        int rc = enqueue_steps(h, h->cur, count, dtf, vol_last, use_sched, last_single, &end);
         if (rc) return rc;
     } else {
         uint32_t bits;
         std::memcpy(&bits, &dtf, 4);
         std::string key = std::to_string(h->cur) + ":" + std::to_string(count) + ":" + std::to_string(vol_last) +
-                          ":" + std::to_string(use_sched) + ":" + std::to_string(bits);
+                          ":" + std::to_string(use_sched) + ":" + std::to_string(bits) + ":" +
+                          std::to_string(last_single) + ":" + std::to_string(h->wtb_k);
         auto it = h->graphs.find(key);
         cudaGraphExec_t exec = nullptr;
         if (it == h->graphs.end()) {
             cudaGraph_t graph = nullptr;
             SBS_CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-            int rc = enqueue_steps(h, h->cur, count, dtf, vol_last, use_sched, &end);
+            int rc = enqueue_steps(h, h->cur, count, dtf, vol_last, use_sched, last_single, &end);
             cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
             if (rc) {
                 if (graph) cudaGraphDestroy(graph);
@@ -379,7 +418,7 @@ int run_chunk(sbs_drainage *h, int count, double dt, bool vol_last) {
         } else {
             exec = it->second;
         }
-        end = h->cur ^ (count & 1);
+        end = h->cur ^ (launches_in(h, count, last_single) & 1);
         SBS_CUDA_TRY(cudaGraphLaunch(exec, h->stream));
     }
     h->cur = end;
@@ -401,7 +440,7 @@ int run_steps(sbs_drainage *h, double dt, uint64_t n, uint32_t check_every) {
                 vol = true;
             }
         }
-        int rc = run_chunk(h, (int)g, dt, vol);
+        int rc = run_chunk(h, (int)g, dt, vol, done + g == n);
         if (rc) return rc;
         done += g;
     }
@@ -938,6 +977,25 @@ int sbs_gpu_drainage_set_marangoni_params(sbs_drainage *h, float gamma_air, floa
     h->params.surfactant_diffusion = surfactant_diffusion;
     h->params.marangoni_coeff = marangoni_coeff;
     return refresh(h, &consts_of(h));
+}
+
+int sbs_gpu_drainage_set_time_blocking(sbs_drainage *h, int steps_per_launch) {
+    CHECK_HANDLE(h);
+    REQUIRE_SEM(h, SBS_WGSL_SEMANTICS);
+    SBS_CHECK_ARG(steps_per_launch >= 0 && steps_per_launch <= 4, "steps_per_launch must be 0..4");
+    if (steps_per_launch > 1 && !wtb_supported(h->nt, h->np))
+        return set_error(SBS_E_INVALID, "time blocking needs grid_width a multiple of 4 (got %d)", h->np);
+    destroy_graphs(h);
+    h->wtb_k = steps_per_launch > 1 ? steps_per_launch : 0;
+    if (h->wtb_k) h->wgeom = wtb_geometry(h->nt, h->np, h->wtb_k);
+    return SBS_OK;
+}
+
+int sbs_gpu_drainage_time_blocking(const sbs_drainage *h, int *out) {
+    CHECK_HANDLE(h);
+    SBS_CHECK_ARG(out != nullptr, "out is null");
+    *out = h->wtb_k > 1 ? h->wtb_k : 1;
+    return SBS_OK;
 }
 
 int sbs_gpu_drainage_set_enabled(sbs_drainage *h, int enabled) {

@@ -24,6 +24,7 @@
 // error-free TwoSum, giving ~48 significant bits with f32 arithmetic at 16 B per cell-step.
 #include <cuda_runtime.h>
 
+#include "cell.cuh"
 #include "sbs_internal.h"
 
 namespace sbs {
@@ -137,7 +138,7 @@ __device__ __forceinline__ void phi_neighbors(const float *rowp, const float4 &v
     pp.w = (c + 4 < np) ? rh : w0;
 }
 
-template <int SEM, int X2, bool VOL>
+template <int SEM, int X2, bool VOL, bool MAR = false>
 __global__ void __launch_bounds__(kBlockThreadsMax) drain_step_kernel(const StepArgs a) {
     __shared__ double s_red[64];
     __shared__ TfeStep s_tfe;
@@ -235,16 +236,22 @@ __global__ void __launch_bounds__(kBlockThreadsMax) drain_step_kernel(const Step
 
         float4 outh, outl = splat4(0.f), outc = splat4(0.f);
         double ring_s = 0.0, ring_c = 0.0;
+        float4 wh4, wc4;
+        if (WGSL)
+            wgsl_cell4<MAR>(hc, hp, hn, hpm, hpp, cc, cp, cn, cpm, cpp, co, b, DR2, a.DsR2, a.Gt, a.M, dt, crit, wh4,
+                            wc4);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const float h = getk(hc, k);
             const float tm = getk(hp, k), tp = getk(hn, k), pm = getk(hpm, k), pp = getk(hpp, k);
             const bool valid = active && (c + k < np);
             float vh, vl = 0.f, vc = 0.f;
-            if (h < crit) {
+            if (WGSL) {
+                vh = getk(wh4, k);
+                vc = getk(wc4, k);
+            } else if (h < crit) {
                 vh = h;
                 if (X2) vl = getk(lc4, k);
-                if (WGSL) vc = getk(cc, k);
             } else {
                 float lt = (tp - h) + (tm - h);
                 float d1 = tp - tm;
@@ -259,26 +266,7 @@ __global__ void __launch_bounds__(kBlockThreadsMax) drain_step_kernel(const Step
                 }
                 const float L = fmaf(co.z, lp, fmaf(co.y, d1, b * lt));
                 const float h3 = (h * h) * h;
-                float inc = fmaf(DR2, L, co.x * h3);
-                if (WGSL) {
-                    const float cv = getk(cc, k);
-                    const float ctm = getk(cp, k), ctp = getk(cn, k), cpmk = getk(cpm, k), cppk = getk(cpp, k);
-                    if (a.marangoni) {
-                        const float gt = a.Gt * (ctp - ctm);
-                        const float gp = co.w * (cppk - cpmk);
-                        const float mag = sqrtf(fmaf(gt, gt, gp * gp));
-                        inc = inc + (a.M * mag) * (h * h);
-                    }
-                    const float lc = (ctp - cv) + (ctm - cv);
-                    const float d1c = ctp - ctm;
-                    const float lpc = (cppk - cv) + (cpmk - cv);
-                    const float Lc = fmaf(co.z, lpc, fmaf(co.y, d1c, b * lc));
-                    float dc = a.DsR2 * Lc;
-                    if (a.marangoni) dc = fmaf(0.001f * L, cv, dc);
-                    float y = fmaf(dt, dc, cv);
-                    y = y > 0.f ? y : 0.f;
-                    vc = y < 1.f ? y : 1.f;
-                }
+                const float inc = fmaf(DR2, L, co.x * h3);
                 if (X2) {
                     const float t = fmaf(dt, inc, l);
                     const float s = h + t;
@@ -604,12 +592,26 @@ cudaError_t launch_join_f64(const float *hi, const float *lo, double *dst, int n
     return cudaGetLastError();
 }
 
-StepGeom step_geometry(int nt, int np) {
+StepGeom step_geometry(int nt, int np, int semantics, int x2) {
     StepGeom g{};
     const int chunks = (np + 127) / 128;
     g.wx = chunks < 4 ? chunks : 4;
     g.nbx = (chunks + g.wx - 1) / g.wx;
-    g.rb = 16;
+    // strips sized so the grid is about one wave of resident blocks
+    int dev = 0, sms = 148, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const void *fn = semantics == SBS_CPU_SEMANTICS
+                         ? (x2 ? (const void *)drain_step_kernel<SBS_CPU_SEMANTICS, 1, false>
+                               : (const void *)drain_step_kernel<SBS_CPU_SEMANTICS, 0, false>)
+                         : (const void *)drain_step_kernel<SBS_WGSL_SEMANTICS, 0, false>;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * g.wx, 0);
+    if (per_sm < 1) per_sm = 1;
+    int strips = per_sm * sms / g.nbx;
+    if (strips < 1) strips = 1;
+    int rb = (nt - 2 + strips - 1) / strips;
+    if (rb < 4) rb = 4;
+    g.rb = rb;
     g.nby = (nt - 2 + g.rb - 1) / g.rb;
     return g;
 }
@@ -629,11 +631,16 @@ cudaError_t launch_step(int semantics, int x2, const StepArgs &a, const StepGeom
             else
                 drain_step_kernel<SBS_CPU_SEMANTICS, 0, false><<<grid, block, 0, s>>>(a);
         }
+    } else if (a.marangoni) {
+        if (vol)
+            drain_step_kernel<SBS_WGSL_SEMANTICS, 0, true, true><<<grid, block, 0, s>>>(a);
+        else
+            drain_step_kernel<SBS_WGSL_SEMANTICS, 0, false, true><<<grid, block, 0, s>>>(a);
     } else {
         if (vol)
-            drain_step_kernel<SBS_WGSL_SEMANTICS, 0, true><<<grid, block, 0, s>>>(a);
+            drain_step_kernel<SBS_WGSL_SEMANTICS, 0, true, false><<<grid, block, 0, s>>>(a);
         else
-            drain_step_kernel<SBS_WGSL_SEMANTICS, 0, false><<<grid, block, 0, s>>>(a);
+            drain_step_kernel<SBS_WGSL_SEMANTICS, 0, false, false><<<grid, block, 0, s>>>(a);
     }
     return cudaGetLastError();
 }

@@ -1,0 +1,259 @@
+// Temporally blocked drainage step for the GPUDrainageSimulator semantics (drainage.wgsl).
+//
+// One launch advances the field by K steps with one read and one write of h and Gamma, instead of
+// K reads and writes. The pole rows never change in these semantics, so K steps of the 5-point
+// stencil only depend on a cone K cells wide around each output cell, which one warp can hold:
+//
+//  * phi: a warp loads 128 consecutive cells (32 lanes x float4) but keeps only the middle 120.
+//    Each level spoils one more cell at each warp edge (the neighbour beyond the warp is not
+//    available), so for K <= 4 only lanes 0 and 31 go bad; warps therefore start 120 cells apart
+//    and the loads wrap around the row end (row length a multiple of 4).
+//  * theta: a thread sweeps its strip top to bottom as a time-skewed pipeline. After loading row t
+//    (level 0) it computes level l of row t - l from a three-row window of level l - 1, for
+//    l = 1..K, and stores level K. Each level's windows rotate through three register slots whose
+//    index is fixed at compile time (the row loop is unrolled by three), so nothing is copied.
+//
+// The per-cell arithmetic is wgsl_cell(), the same function the single-step kernel uses, so K
+// launches of one and one launch of this give bit-identical fields.
+#include <cuda_runtime.h>
+
+#include "cell.cuh"
+#include "sbs_internal.h"
+
+namespace sbs {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kWarpsPerBlock = 4;
+constexpr int kSegStride = 120;  // output cells per warp
+
+__device__ __forceinline__ double wtb_block_sum(double v, double *smem) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    if (lane == 0) smem[warp] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < nw; ++i) t += smem[i];
+    __syncthreads();
+    return t;
+}
+
+#ifndef SBS_WTB_PREFETCH
+#define SBS_WTB_PREFETCH 1  // request level-0 row t+1 while computing row t (0: load it at row t)
+#endif
+
+struct Wtb {
+    const float *hin, *cin;  // column-offset input pointers of this lane
+    float *hout, *cout;      // column-offset output pointers
+    const float4 *sco;       // this strip's per-row coefficients in shared memory, from row sco_base
+    int sco_base;
+    int nt, pitch, r0, r1;
+    bool store;
+    float b, DR2, DsR2, Gt, M, dt, crit;
+    const double *vol_w;
+};
+
+// One pipeline iteration: load level-0 row t, then compute level l of row t - l for l = 1..K.
+// Slot P holds the row most recently written to each level's window.
+// With SBS_WTB_PREFETCH the level-0 row t arrives in (ph, pc), loaded one iteration earlier, and
+// row t + 1 is requested here; otherwise row t is loaded here.
+template <int K, int P, bool VOL, bool MAR>
+__device__ __forceinline__ void wtb_iter(const Wtb &w, int t, float4 (&wh)[K][3], float4 (&wc)[K][3], float4 &ph,
+                                         float4 &pc, double &vacc) {
+    constexpr int CUR = (P + 2) % 3, UP = (P + 1) % 3;
+    const int tl = SBS_WTB_PREFETCH ? t + 1 : t;
+    float4 nh = make_float4(0.f, 0.f, 0.f, 0.f), nc = nh;
+    if (tl >= 0 && tl < w.nt) {
+        nh = __ldg(reinterpret_cast<const float4 *>(w.hin + (size_t)tl * w.pitch));
+        nc = __ldg(reinterpret_cast<const float4 *>(w.cin + (size_t)tl * w.pitch));
+    }
+    if (SBS_WTB_PREFETCH) {
+        wh[0][P] = ph;
+        wc[0][P] = pc;
+        ph = nh;
+        pc = nc;
+    } else {
+        wh[0][P] = nh;
+        wc[0][P] = nc;
+    }
+#pragma unroll
+    for (int l = 1; l <= K; ++l) {
+        const int i = t - l;
+        const bool need = i >= w.r0 - (K - l) && i < w.r1 + (K - l) && i >= 0 && i < w.nt;  // warp-uniform
+        float4 oh = make_float4(0.f, 0.f, 0.f, 0.f), oc = oh;
+        if (need) {
+            const float4 hc = wh[l - 1][CUR], cc = wc[l - 1][CUR];
+            if (i == 0 || i == w.nt - 1) {  // pole rows are frozen (drainage.wgsl:85-89)
+                oh = hc;
+                oc = cc;
+            } else {
+                const float4 hu = wh[l - 1][UP], hd = wh[l - 1][P];
+                const float4 cu = wc[l - 1][UP], cd = wc[l - 1][P];
+                const float4 co = w.sco[i - w.sco_base];
+                const float hl = __shfl_up_sync(kFull, hc.w, 1), hr = __shfl_down_sync(kFull, hc.x, 1);
+                const float cl = __shfl_up_sync(kFull, cc.w, 1), cr = __shfl_down_sync(kFull, cc.x, 1);
+                const float4 hpm = make_float4(hl, hc.x, hc.y, hc.z), hpp = make_float4(hc.y, hc.z, hc.w, hr);
+                const float4 cpm = make_float4(cl, cc.x, cc.y, cc.z), cpp = make_float4(cc.y, cc.z, cc.w, cr);
+wgsl_cell4<MAR>(hc, hu, hd, hpm, hpp, cc, cu, cd, cpm, cpp, co, w.b, w.DR2, w.DsR2, w.Gt, w.M, w.dt, w.crit, oh,
+                                oc);
+            }
+        }
+        if (l < K) {
+            wh[l][P] = oh;
+            wc[l][P] = oc;
+        } else if (need && i >= w.r0 && i < w.r1 && w.store) {
+            *reinterpret_cast<float4 *>(w.hout + (size_t)i * w.pitch) = oh;
+            *reinterpret_cast<float4 *>(w.cout + (size_t)i * w.pitch) = oc;
+            if (VOL) vacc += ((double)oh.x + (double)oh.y + (double)oh.z + (double)oh.w) * __ldg(w.vol_w + i);
+        }
+    }
+}
+
+template <int K, bool VOL, bool MAR>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) wtb_wgsl_kernel(const StepArgs a) {
+    __shared__ double s_red[32];
+    __shared__ int s_last;
+    extern __shared__ float4 s_co[];  // coefficient rows [r0 - K, r1 + K) of this strip
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int np = a.np;
+    const int seg = blockIdx.x * kWarpsPerBlock + warp;
+    const int out0 = seg * kSegStride;
+    const int c_unwrapped = out0 - 4 + 4 * lane;
+    const int col = ((c_unwrapped % np) + np) % np;
+
+    Wtb w;
+    w.hin = a.hin + col;
+    w.cin = a.cin + col;
+    w.hout = a.hout + col;
+    w.cout = a.cout + col;
+    w.nt = a.nt;
+    w.pitch = a.pitch;
+    w.r0 = 1 + blockIdx.y * a.rb;
+    w.r1 = min(w.r0 + a.rb, a.nt - 1);
+    w.store = lane >= 1 && lane <= 30 && c_unwrapped < np;
+    w.b = a.b;
+    w.DR2 = a.DR2;
+    w.DsR2 = a.DsR2;
+    w.Gt = a.Gt;
+    w.M = a.M;
+    w.dt = a.dt;
+    w.crit = a.crit;
+    w.vol_w = a.vol_w;
+    w.sco_base = w.r0 - K;
+    w.sco = s_co;
+    for (int i = threadIdx.x; i < a.rb + 2 * K; i += blockDim.x) {
+        const int r = w.sco_base + i;
+        s_co[i] = (r >= 0 && r < a.nt) ? __ldg(a.rows + r) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+
+    float4 wh[K][3], wc[K][3];
+#pragma unroll
+    for (int l = 0; l < K; ++l)
+#pragma unroll
+        for (int s = 0; s < 3; ++s) {
+            wh[l][s] = make_float4(0.f, 0.f, 0.f, 0.f);
+            wc[l][s] = wh[l][s];
+        }
+
+    double vacc = 0.0;
+    const int t0 = w.r0 - K, t1 = w.r1 + K;  // level-0 rows [t0, t1)
+    float4 ph = make_float4(0.f, 0.f, 0.f, 0.f), pc = ph;
+    if (SBS_WTB_PREFETCH && t0 >= 0) {
+        ph = __ldg(reinterpret_cast<const float4 *>(w.hin + (size_t)t0 * w.pitch));
+        pc = __ldg(reinterpret_cast<const float4 *>(w.cin + (size_t)t0 * w.pitch));
+    }
+    for (int t = t0; t < t1; t += 3) {
+        wtb_iter<K, 0, VOL, MAR>(w, t, wh, wc, ph, pc, vacc);
+        if (t + 1 < t1) wtb_iter<K, 1, VOL, MAR>(w, t + 1, wh, wc, ph, pc, vacc);
+        if (t + 2 < t1) wtb_iter<K, 2, VOL, MAR>(w, t + 2, wh, wc, ph, pc, vacc);
+    }
+
+    if (VOL) {
+        const double s = wtb_block_sum(vacc, s_red);
+        const unsigned nblocks = gridDim.x * gridDim.y;
+        const unsigned bid = blockIdx.y * gridDim.x + blockIdx.x;
+        if (threadIdx.x == 0) {
+            a.vol_partials[bid] = s;
+            __threadfence();
+            const unsigned tk = atomicAdd(a.vol_counter, 1u);
+            s_last = (tk == nblocks - 1);
+        }
+        __syncthreads();
+        if (s_last) {
+            __threadfence();
+            double tot = 0.0;
+            for (unsigned i = threadIdx.x; i < nblocks; i += blockDim.x) tot += __ldcg(a.vol_partials + i);
+            double pole = 0.0;  // the frozen pole rows of the input
+            for (int j = threadIdx.x; j < np; j += blockDim.x) {
+                pole += (double)__ldg(a.hin + j) * __ldg(a.vol_w);
+                pole += (double)__ldg(a.hin + (size_t)(a.nt - 1) * a.pitch + j) * __ldg(a.vol_w + a.nt - 1);
+            }
+            tot = wtb_block_sum(tot, s_red);
+            pole = wtb_block_sum(pole, s_red);
+            if (threadIdx.x == 0) {
+                const unsigned idx = *a.vol_index;
+                a.vol_out[idx] = tot + pole;
+                *a.vol_index = idx + 1;
+                *a.vol_counter = 0u;
+                __threadfence();
+            }
+        }
+    }
+}
+
+template <int K>
+const void *wtb_fn(bool vol, bool mar) {
+    if (vol) return mar ? (const void *)wtb_wgsl_kernel<K, true, true> : (const void *)wtb_wgsl_kernel<K, true, false>;
+    return mar ? (const void *)wtb_wgsl_kernel<K, false, true> : (const void *)wtb_wgsl_kernel<K, false, false>;
+}
+
+const void *wtb_kernel(int K, bool vol, bool mar) {
+    switch (K) {
+        case 2:
+            return wtb_fn<2>(vol, mar);
+        case 3:
+            return wtb_fn<3>(vol, mar);
+        case 4:
+            return wtb_fn<4>(vol, mar);
+        default:
+            return nullptr;
+    }
+}
+
+}  // namespace
+
+bool wtb_supported(int nt, int np) { return np % 4 == 0 && np >= 8 && nt >= 3; }
+
+StepGeom wtb_geometry(int nt, int np, int K) {
+    StepGeom g{};
+    const int segs = (np + kSegStride - 1) / kSegStride;
+    g.wx = kWarpsPerBlock;
+    g.nbx = (segs + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    int dev = 0, sms = 148, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wtb_kernel(K, false, false), kWarpsPerBlock * 32,
+                                                  sizeof(float4) * 64);
+    if (per_sm < 1) per_sm = 1;
+    const int resident = per_sm * sms;
+    int strips = resident / g.nbx;
+    if (strips < 1) strips = 1;
+    int rb = (nt - 2 + strips - 1) / strips;
+    if (rb < 4 * K) rb = 4 * K;
+    g.rb = rb;
+    g.nby = (nt - 2 + rb - 1) / rb;
+    return g;
+}
+
+cudaError_t launch_wtb(int K, const StepArgs &a, const StepGeom &g, cudaStream_t s) {
+    const void *fn = wtb_kernel(K, a.vol_w != nullptr, a.marangoni != 0);
+    if (fn == nullptr) return cudaErrorInvalidValue;
+    dim3 grid(g.nbx, g.nby), block(kWarpsPerBlock * 32);
+    void *args[] = {(void *)&a};
+    return cudaLaunchKernel(fn, grid, block, args, sizeof(float4) * (g.rb + 2 * K), s);
+}
+
+}  // namespace sbs

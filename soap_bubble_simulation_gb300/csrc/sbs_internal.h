@@ -83,7 +83,11 @@ struct StepGeom {
     int rb;
 };
 
-StepGeom step_geometry(int nt, int np);
+StepGeom step_geometry(int nt, int np, int semantics, int x2);
+// Temporally blocked WGSL step (K = 2..4 steps per launch), drainage_wtb.cu.
+bool wtb_supported(int nt, int np);
+StepGeom wtb_geometry(int nt, int np, int K);
+cudaError_t launch_wtb(int K, const StepArgs &a, const StepGeom &g, cudaStream_t s);
 // x2: compensated f32x2 thickness (hi + lo words); CPU semantics only.
 cudaError_t launch_step(int semantics, int x2, const StepArgs &a, const StepGeom &g, cudaStream_t s);
 // Writes the pole rows of `h` (and `hl`, if not null) from the ring partials of the last step.
@@ -181,6 +185,8 @@ struct sbs_drainage {
     double *qbuf = nullptr;
     size_t qcap = 0;
     sbs::StepGeom geom{};
+    int wtb_k = 0;  // steps per temporally blocked launch (WGSL semantics; 0 = single steps only)
+    sbs::StepGeom wgeom{};
 
     // CPU semantics parameters (from sbs_config)
     sbs_config cfg{};

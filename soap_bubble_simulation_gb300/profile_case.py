@@ -23,10 +23,13 @@ def main(argv=None) -> None:
     p.add_argument("--case", default="wgsl", choices=["wgsl", "cpu", "cpu32"])
     p.add_argument("--res", type=int, default=2048)
     p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--blocking", type=int, default=-1, help="WGSL steps per launch (default: library choice)")
     a = p.parse_args(argv)
     h, c = synthetic.bubble_c1(a.res)
     if a.case == "wgsl":
         sim = GPUDrainageSimulator(None, 550e-9, 2 * a.res, a.res)
+        if a.blocking >= 0:
+            N.call("sbs_gpu_drainage_set_time_blocking", sim.handle, a.blocking)
         sim.set_thickness_array(h)
         sim.set_concentration_array(c)
         sim.run(a.steps)

@@ -368,3 +368,62 @@ def test_wgsl_volume_checks(sbs, orc):
     for k in range(4):
         cur_h, cur_c = orc.wgsl_run(p, cur_h, cur_c, 50, "kernel")
         assert vols[k] == pytest.approx(orc.film_volume(cur_h, 0.025), rel=1e-12)
+
+
+# --------------------------------------------------------------------------------------------
+# Temporal blocking (several WGSL steps per launch) must not change a single bit
+# --------------------------------------------------------------------------------------------
+def set_blocking(sbs, sim, k):
+    sbs._native.call("sbs_gpu_drainage_set_time_blocking", sim.handle, k)
+
+
+@pytest.mark.parametrize("W,H", [(4096, 300), (512, 200), (8, 5), (132, 40), (248, 9)])
+@pytest.mark.parametrize("marangoni", [0, 1])
+def test_time_blocking_bit_identical(sbs, orc, W, H, marangoni):
+    from soap_bubble_simulation_gb300 import synthetic
+
+    h = synthetic.smooth_modes(H, W, seed=W * 7 + H).astype(np.float32)
+    h[H // 3, : W // 5] = 25e-9  # a patch below the critical thickness
+    c = synthetic.surfactant_noise(H, W, seed=H)
+    results = []
+    for k in (1, 2, 3, 4):
+        sim = sbs.GPUDrainageSimulator(None, 500e-9, W, H)
+        set_blocking(sbs, sim, k)
+        sim.set_thickness_array(h)
+        sim.set_concentration_array(c)
+        sim.set_marangoni_enabled(bool(marangoni))
+        sim.run(23)
+        sim.run(18)
+        results.append((sim.thickness_array(), sim.concentration_array()))
+    for hk, ck in results[1:]:
+        np.testing.assert_array_equal(hk, results[0][0])
+        np.testing.assert_array_equal(ck, results[0][1])
+    if W * H <= 512 * 200:
+        p = orc.wgsl_params(grid_width=W, grid_height=H, marangoni_enabled=marangoni)
+        ho, co = orc.wgsl_run(p, h, c, 41, "kernel")
+        np.testing.assert_array_equal(results[0][0], ho)
+        np.testing.assert_array_equal(results[0][1], co)
+
+
+def test_time_blocking_keeps_previous_buffer_one_pass_behind(sbs, orc):
+    from soap_bubble_simulation_gb300 import synthetic
+
+    h = synthetic.smooth_modes(64, 128).astype(np.float32)
+    sim = sbs.GPUDrainageSimulator(None, 500e-9, 128, 64)
+    out = ctypes.c_int()
+    sbs._native.call("sbs_gpu_drainage_time_blocking", sim.handle, ctypes.byref(out))
+    assert out.value == 4
+    sim.set_thickness_array(h)
+    sim.run(9)  # two 4-step launches and one single step
+    prev = orc.wgsl_run(orc.wgsl_params(), h, np.full_like(h, 0.5), 8, "kernel")[0]
+    stale = sim.current_buffer()
+    v = sbs.film_volume_device(stale.ptr, 64, 128, stale.pitch, 0.025)
+    assert v == pytest.approx(orc.film_volume(prev, 0.025), rel=1e-12)
+
+
+def test_time_blocking_needs_width_multiple_of_4(sbs):
+    sim = sbs.GPUDrainageSimulator(None, 500e-9, 130, 20)
+    with pytest.raises(sbs.SbsError, match="multiple of 4"):
+        set_blocking(sbs, sim, 4)
+    set_blocking(sbs, sim, 1)
+    sim.run(5)
