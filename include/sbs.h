@@ -344,6 +344,23 @@ int sbs_lut2d_lookup_batch(const double *lut, uint32_t T, uint32_t A, double tmi
 int sbs_drainage_vertex_colors(sbs_drainage *h, const double *xyz, size_t nv, const double *lut, uint32_t T,
                                uint32_t A, double tmin, double tmax, double *rgb, int mem);
 
+/* ------------------------------------------------------------------ */
+/* Spectral interference contracted against colour-matching functions */
+/* ------------------------------------------------------------------ */
+#define SBS_SPECTRAL_TC_BF16 0 /* BF16 spectra x BF16 CMF on the tensor cores (tcgen05), FP32 accumulation */
+#define SBS_SPECTRAL_FP32 1    /* FP32 spectra and FP32 FMA contraction (precision reference) */
+
+/* For n points (thickness t_nm, cos_i, film index n_film; f32), the Airy
+ * reflectance F s^2/(1 + F s^2) with s = sin(pi opd/lambda + pi/2), opd =
+ * 2 n t cos_t, full unpolarised Fresnel R and F = 4R/(1-R)^2 (the formulation
+ * of generate_interference_lut, interference_lut.rs:45-133, with arbitrary
+ * wavelengths) at nl <= 128 wavelengths wl_nm, contracted with the nl x 3
+ * matrix cmf: rgb[3k+c] = sum_l R_l(k) cmf[3l+c]. The generalisation of the
+ * reference's 7-sample CIE sum to a dense spectral contraction. Synchronous
+ * in both memory modes (it reads back a device status flag). */
+int sbs_spectral_rgb(const float *t_nm, const float *cos_i, const float *n_film, size_t n, const float *wl_nm,
+                     uint32_t nl, const float *cmf, int mode, float *rgb, int mem, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

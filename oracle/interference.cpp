@@ -287,7 +287,8 @@ void orc_vertex_colors(const double *field, uint32_t nt, uint32_t np, const doub
 // ------------------------------------------------------------------
 void orc_spectral_rgb(const float *t_nm, const float *cos_i, const float *n_film, size_t n, const double *wl,
                       uint32_t nl, const double *cmf, double *rgb) {
-    for (size_t k = 0; k < n; ++k) {
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < (int64_t)n; ++k) {
         double ci = (double)cos_i[k], nf = (double)n_film[k], t = (double)t_nm[k];
         double sin_i = std::sqrt(std::max(1.0 - ci * ci, 0.0));
         double sin_t = sin_i / nf;

@@ -12,7 +12,7 @@ from .drainage import (DeviceField, DrainageParams, DrainageSimulator, GPUDraina
 from .interference import (LUT_ANGLE_SAMPLES, LUT_MAX_THICKNESS_NM, LUT_THICKNESS_SAMPLES,
                            FresnelCoefficients, InterferenceCalculator, RgbColor, constants,
                            generate_interference_lut, generate_interference_lut_array, lookup_2d,
-                           sample_interference_lut, schlick_interference_rgb, wavelengths)
+                           sample_interference_lut, schlick_interference_rgb, spectral_rgb, wavelengths)
 from ._native import SbsError
 
 __all__ = [
@@ -20,6 +20,6 @@ __all__ = [
     "DeviceField", "DrainageParams", "DrainageSimulator", "GPUDrainageSimulator", "ThicknessField",
     "film_volume_device", "LUT_ANGLE_SAMPLES", "LUT_MAX_THICKNESS_NM", "LUT_THICKNESS_SAMPLES",
     "FresnelCoefficients", "InterferenceCalculator", "RgbColor", "constants", "generate_interference_lut",
-    "generate_interference_lut_array", "lookup_2d", "sample_interference_lut", "schlick_interference_rgb",
+    "generate_interference_lut_array", "lookup_2d", "sample_interference_lut", "schlick_interference_rgb", "spectral_rgb",
     "wavelengths", "SbsError",
 ]

@@ -28,6 +28,8 @@ PREC_F64 = 0
 PREC_F32 = 1
 DRAIN_F32 = 0
 DRAIN_F32X2 = 1
+SPECTRAL_TC_BF16 = 0
+SPECTRAL_FP32 = 1
 LOOKUP_GRID = 0
 LOOKUP_TEXEL = 1
 
@@ -172,6 +174,7 @@ SIGNATURES: dict[str, list] = {
     "sbs_schlick_rgb_batch": [_F, _FP, _P, _P, _SZ, _P, _I, _P],
     "sbs_lut_rgba8_lookup_batch": [_P, _U32, _U32, _F, _F, _I, _P, _P, _SZ, _P, _I, _P],
     "sbs_lut2d_lookup_batch": [_P, _U32, _U32, _D, _D, _P, _P, _SZ, _P, _I, _P],
+    "sbs_spectral_rgb": [_P, _P, _P, _SZ, _P, _U32, _P, _I, _P, _I, _P],
     "sbs_drainage_vertex_colors": [_P, _P, _SZ, _P, _U32, _U32, _D, _D, _P, _I],
 }
 _RESTYPES = {"sbs_last_error": C.c_char_p, "sbs_version": C.c_char_p}

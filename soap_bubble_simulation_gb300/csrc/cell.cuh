@@ -83,3 +83,58 @@ __device__ __forceinline__ void wgsl_cell4(const float4 &h, const float4 &tm, co
 }
 
 }  // namespace sbs
+
+namespace sbs {
+
+// DrainageSimulator semantics (drainage.rs:326-379) for two cells, plain f32 (X2 = false) or
+// compensated hi + lo words (X2 = true: differences include the lo words and h + dt*inc is an
+// error-free TwoSum). Cells below the critical thickness keep their words (drainage.rs:331).
+template <bool X2>
+__device__ __forceinline__ void cpu_cell2(float2 h, float2 tm, float2 tp, float2 pm, float2 pp, float2 l, float2 tml,
+                                          float2 tpl, float2 pml, float2 ppl, const float4 &co, float b, float DR2,
+                                          float dt, float crit, float2 &vh, float2 &vl) {
+    float2 lt = add2(sub2(tp, h), sub2(tm, h));
+    float2 d1 = sub2(tp, tm);
+    float2 lp = add2(sub2(pp, h), sub2(pm, h));
+    if (X2) {
+        lt = add2(lt, add2(sub2(tpl, l), sub2(tml, l)));
+        d1 = add2(d1, sub2(tpl, tml));
+        lp = add2(lp, add2(sub2(ppl, l), sub2(pml, l)));
+    }
+    const float2 L = fma2(f2(co.z), lp, fma2(f2(co.y), d1, mul2(f2(b), lt)));
+    const float2 h3 = mul2(mul2(h, h), h);
+    const float2 inc = fma2(f2(DR2), L, mul2(f2(co.x), h3));
+    if (X2) {
+        const float2 t = fma2(f2(dt), inc, l);
+        const float2 s = add2(h, t);
+        const float2 bb = sub2(s, h);
+        const float2 e = add2(sub2(h, sub2(s, bb)), sub2(t, bb));
+        vh.x = h.x < crit ? h.x : (s.x < 0.f ? 0.f : s.x);
+        vh.y = h.y < crit ? h.y : (s.y < 0.f ? 0.f : s.y);
+        vl.x = h.x < crit ? l.x : (s.x < 0.f ? 0.f : e.x);
+        vl.y = h.y < crit ? l.y : (s.y < 0.f ? 0.f : e.y);
+    } else {
+        const float2 x = fma2(f2(dt), inc, h);
+        vh.x = h.x < crit ? h.x : (x.x > 0.f ? x.x : 0.f);
+        vh.y = h.y < crit ? h.y : (x.y > 0.f ? x.y : 0.f);
+        vl = make_float2(0.f, 0.f);
+    }
+}
+
+template <bool X2>
+__device__ __forceinline__ void cpu_cell4(const float4 &h, const float4 &tm, const float4 &tp, const float4 &pm,
+                                          const float4 &pp, const float4 &l, const float4 &tml, const float4 &tpl,
+                                          const float4 &pml, const float4 &ppl, const float4 &co, float b, float DR2,
+                                          float dt, float crit, float4 &vh, float4 &vl) {
+    float2 a, c, e, g;
+    cpu_cell2<X2>(make_float2(h.x, h.y), make_float2(tm.x, tm.y), make_float2(tp.x, tp.y), make_float2(pm.x, pm.y),
+                  make_float2(pp.x, pp.y), make_float2(l.x, l.y), make_float2(tml.x, tml.y), make_float2(tpl.x, tpl.y),
+                  make_float2(pml.x, pml.y), make_float2(ppl.x, ppl.y), co, b, DR2, dt, crit, a, c);
+    cpu_cell2<X2>(make_float2(h.z, h.w), make_float2(tm.z, tm.w), make_float2(tp.z, tp.w), make_float2(pm.z, pm.w),
+                  make_float2(pp.z, pp.w), make_float2(l.z, l.w), make_float2(tml.z, tml.w), make_float2(tpl.z, tpl.w),
+                  make_float2(pml.z, pml.w), make_float2(ppl.z, ppl.w), co, b, DR2, dt, crit, e, g);
+    vh = make_float4(a.x, a.y, e.x, e.y);
+    vl = make_float4(c.x, c.y, g.x, g.y);
+}
+
+}  // namespace sbs

@@ -240,47 +240,17 @@ __global__ void __launch_bounds__(kBlockThreadsMax) drain_step_kernel(const Step
         if (WGSL)
             wgsl_cell4<MAR>(hc, hp, hn, hpm, hpp, cc, cp, cn, cpm, cpp, co, b, DR2, a.DsR2, a.Gt, a.M, dt, crit, wh4,
                             wc4);
+        else
+            cpu_cell4<X2 != 0>(hc, hp, hn, hpm, hpp, lc4, lp4, ln4, lpm, lpp, co, b, DR2, dt, crit, wh4, wc4);
+        const bool ring_row = CPU && (r == 1 || r == nt - 2);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const float h = getk(hc, k);
-            const float tm = getk(hp, k), tp = getk(hn, k), pm = getk(hpm, k), pp = getk(hpp, k);
             const bool valid = active && (c + k < np);
-            float vh, vl = 0.f, vc = 0.f;
-            if (WGSL) {
-                vh = getk(wh4, k);
-                vc = getk(wc4, k);
-            } else if (h < crit) {
-                vh = h;
-                if (X2) vl = getk(lc4, k);
-            } else {
-                float lt = (tp - h) + (tm - h);
-                float d1 = tp - tm;
-                float lp = (pp - h) + (pm - h);
-                float l = 0.f;
-                if (X2) {
-                    l = getk(lc4, k);
-                    const float tpl = getk(ln4, k), tml = getk(lp4, k), ppl = getk(lpp, k), pml = getk(lpm, k);
-                    lt = lt + ((tpl - l) + (tml - l));
-                    d1 = d1 + (tpl - tml);
-                    lp = lp + ((ppl - l) + (pml - l));
-                }
-                const float L = fmaf(co.z, lp, fmaf(co.y, d1, b * lt));
-                const float h3 = (h * h) * h;
-                const float inc = fmaf(DR2, L, co.x * h3);
-                if (X2) {
-                    const float t = fmaf(dt, inc, l);
-                    const float s = h + t;
-                    const float bb = s - h;
-                    const float e = (h - (s - bb)) + (t - bb);
-                    vh = s < 0.f ? 0.f : s;
-                    vl = s < 0.f ? 0.f : e;
-                } else {
-                    const float x = fmaf(dt, inc, h);
-                    vh = x > 0.f ? x : 0.f;
-                }
-            }
+            float vh = getk(wh4, k), vl = 0.f, vc = 0.f;
+            if (WGSL) vc = getk(wc4, k);
+            if (X2) vl = getk(wc4, k);
             if (CPU) {
-                if (valid && (r == 1 || r == nt - 2)) comp_add(ring_s, ring_c, (double)vh + (double)vl);
+                if (ring_row && valid) comp_add(ring_s, ring_c, (double)vh + (double)vl);
                 if (fmask) {
                     const int col = c + k;
                     for (int f = 0; f < nf; ++f) {

@@ -280,3 +280,21 @@ def lookup_2d(lut: np.ndarray, tmin: float, tmax: float, film_thickness_nm, cos_
     N.call("sbs_lut2d_lookup_batch", N.ptr(L), L.shape[0], L.shape[1], float(tmin), float(tmax), N.ptr(t), N.ptr(ci),
            t.size, N.ptr(out), N.MEM_HOST, None)
     return out
+
+
+def spectral_rgb(film_thickness_nm, cos_theta, refractive_index, wavelengths_nm, cmf, mode: str = "tc") -> np.ndarray:
+    """Per point: Airy reflectance at each wavelength contracted with the [nl, 3] colour-matching
+    matrix. mode 'tc' = BF16 tensor-core contraction (tcgen05, FP32 accumulation), 'fp32' = FP32
+    throughout. Returns [n, 3] f32."""
+    t = _arr(film_thickness_nm, np.float32)
+    ci = _arr(cos_theta, np.float32)
+    nf = _arr(refractive_index, np.float32)
+    wl = _arr(wavelengths_nm, np.float32)
+    m = np.ascontiguousarray(np.asarray(cmf, dtype=np.float32).reshape(-1, 3))
+    if m.shape[0] != wl.size:
+        raise ValueError("cmf must have one row per wavelength")
+    out = np.empty((t.size, 3), dtype=np.float32)
+    md = N.SPECTRAL_TC_BF16 if mode == "tc" else N.SPECTRAL_FP32
+    N.call("sbs_spectral_rgb", N.ptr(t), N.ptr(ci), N.ptr(nf), t.size, N.ptr(wl), wl.size, N.ptr(m), md, N.ptr(out),
+           N.MEM_HOST, None)
+    return out

@@ -3,7 +3,8 @@
     python -m soap_bubble_simulation_gb300.profile_case --case wgsl --res 2048 --steps 20
 
 Cases: `wgsl` (GPUDrainageSimulator semantics, h + surfactant), `cpu` (DrainageSimulator
-semantics, compensated f32x2), `cpu32` (plain f32). The field is the seeded smooth-mode field of
+semantics, compensated f32x2), `cpu32` (plain f32), `spectral-tc` / `spectral-fp32` (81-wavelength
+spectral colour of --points seeded points, tensor-core or FP32 contraction). The field is the seeded smooth-mode field of
 the 2048-resolution workload, built at the requested resolution. Steps launch one kernel each
 (graph replay for runs of 8 or more).
 """
@@ -20,11 +21,22 @@ from .drainage import DrainageSimulator, GPUDrainageSimulator, _Handle
 
 def main(argv=None) -> None:
     p = argparse.ArgumentParser()
-    p.add_argument("--case", default="wgsl", choices=["wgsl", "cpu", "cpu32"])
+    p.add_argument("--case", default="wgsl", choices=["wgsl", "cpu", "cpu32", "spectral-tc", "spectral-fp32"])
+    p.add_argument("--points", type=int, default=1 << 20, help="spectral cases: number of points")
     p.add_argument("--res", type=int, default=2048)
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--blocking", type=int, default=-1, help="WGSL steps per launch (default: library choice)")
     a = p.parse_args(argv)
+    if a.case.startswith("spectral"):
+        from .interference import spectral_rgb
+
+        t, ci, nf = synthetic.spectral_points(a.points)
+        wl = synthetic.WAVELENGTHS_81
+        cmf = synthetic.spectral_cmf(wl)
+        for _ in range(a.steps):
+            spectral_rgb(t, ci, nf, wl, cmf, mode="tc" if a.case == "spectral-tc" else "fp32")
+        print(f"ran {a.steps} spectral evaluations of {a.points} points ({a.case})")
+        return
     h, c = synthetic.bubble_c1(a.res)
     if a.case == "wgsl":
         sim = GPUDrainageSimulator(None, 550e-9, 2 * a.res, a.res)

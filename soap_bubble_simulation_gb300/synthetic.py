@@ -83,3 +83,46 @@ def icosphere(subdivisions: int = 5) -> np.ndarray:
             nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
         faces = nf
     return np.array(verts, dtype=np.float64)
+
+
+# --- spectral interference workload ---------------------------------------------------------
+WAVELENGTHS_81 = np.arange(380.0, 781.0, 5.0)  # 380..780 nm, 5 nm step
+
+
+def spectral_points(n: int = 8_388_608, seed: int = 3):
+    """Surface points: thickness U[10, 1500] nm, cos(theta) U[0, 1], film index U[1.30, 1.40] (f32)."""
+    g = rng(seed)
+    t = g.uniform(10.0, 1500.0, n).astype(np.float32)
+    c = g.uniform(0.0, 1.0, n).astype(np.float32)
+    nf = g.uniform(1.30, 1.40, n).astype(np.float32)
+    return t, c, nf
+
+
+def spectral_cmf(wl: np.ndarray = WAVELENGTHS_81, seed: int = 4) -> np.ndarray:
+    """[len(wl), 3] colour-matching matrix: per channel a sum of 2 or 3 Gaussian lobes with
+    seeded amplitude U[0.2, 1.2], centre in the channel's band and width U[15, 60] nm."""
+    g = rng(seed)
+    bands = [(550.0, 700.0), (480.0, 600.0), (400.0, 500.0)]  # R, G, B
+    out = np.zeros((wl.size, 3))
+    for ch, (lo, hi) in enumerate(bands):
+        for _ in range(int(g.integers(2, 4))):
+            a, mu, s = g.uniform(0.2, 1.2), g.uniform(lo, hi), g.uniform(15.0, 60.0)
+            out[:, ch] += a * np.exp(-0.5 * ((wl - mu) / s) ** 2)
+    return out
+
+
+def delta_e76(rgb_a: np.ndarray, rgb_b: np.ndarray, white: np.ndarray) -> np.ndarray:
+    """CIE76 colour difference of two linear-RGB arrays [n, 3]: each channel is divided by the
+    white response (the CMF column sums: a perfect reflector maps to 1), then linear sRGB -> XYZ
+    (D65) -> CIELAB."""
+    M = np.array([[0.4124564, 0.3575761, 0.1804375], [0.2126729, 0.7151522, 0.0721750],
+                  [0.0193339, 0.1191920, 0.9503041]])
+    wn = np.array([0.95047, 1.0, 1.08883])
+
+    def lab(rgb):
+        xyz = (np.asarray(rgb, np.float64) / white) @ M.T / wn
+        d = 6.0 / 29.0
+        f = np.where(xyz > d ** 3, np.cbrt(np.maximum(xyz, 0)), xyz / (3 * d * d) + 4.0 / 29.0)
+        return np.stack([116 * f[:, 1] - 16, 500 * (f[:, 0] - f[:, 1]), 200 * (f[:, 1] - f[:, 2])], axis=1)
+
+    return np.linalg.norm(lab(rgb_a) - lab(rgb_b), axis=1)
