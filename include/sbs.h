@@ -345,6 +345,37 @@ int sbs_drainage_vertex_colors(sbs_drainage *h, const double *xyz, size_t nv, co
                                uint32_t A, double tmin, double tmax, double *rgb, int mem);
 
 /* ------------------------------------------------------------------ */
+/* Batched foam drainage                                               */
+/* ------------------------------------------------------------------ */
+/* Many bubbles, each with its own GPUDrainageSimulator-semantics grid
+ * (resolution x 2 resolution cells, own radius), advanced together. No
+ * reference counterpart: the reference's foam bubbles carry one scalar film
+ * thickness each (foam.rs:44). The physics of each bubble is drainage.wgsl's,
+ * with the shared DrainageParams (bubble_radius overridden per bubble; grid
+ * fields ignored); a bubble advanced here matches a single GPUDrainageSimulator
+ * bit for bit. Fields start at 500 nm and surfactant 0.5. */
+typedef struct sbs_foam sbs_foam;
+int sbs_foam_create(uint32_t nbubbles, const uint32_t *resolution, const float *radius_m,
+                    const sbs_drainage_params *params, sbs_foam **out);
+int sbs_foam_destroy(sbs_foam *f);
+int sbs_foam_total_cells(const sbs_foam *f, uint64_t *out);
+/* Per-bubble fields, [resolution][2 resolution] f32, mem = SBS_MEM_HOST or SBS_MEM_DEVICE. */
+int sbs_foam_set_thickness(sbs_foam *f, uint32_t bubble, const float *src, size_t n, int mem);
+int sbs_foam_get_thickness(sbs_foam *f, uint32_t bubble, float *dst, size_t n, int mem);
+int sbs_foam_set_concentration(sbs_foam *f, uint32_t bubble, const float *src, size_t n, int mem);
+int sbs_foam_get_concentration(sbs_foam *f, uint32_t bubble, float *dst, size_t n, int mem);
+/* Advances every bubble `steps` passes: one persistent kernel (cooperative,
+ * grid barriers between phases of steps_per_phase steps; a second launch for a
+ * remainder), replayed from a CUDA graph. SBS_E_TIMEOUT if a barrier wait ran out. */
+int sbs_foam_run(sbs_foam *f, uint32_t steps);
+/* Tile shape: steps per phase (1, 2 or 4) and theta rows per work item (4..256). */
+int sbs_foam_set_tiles(sbs_foam *f, uint32_t steps_per_phase, uint32_t strip_rows);
+/* Times every candidate tile shape for trial_steps steps on the bubbles (fields
+ * are saved and restored), keeps the fastest and reports it. */
+int sbs_foam_autotune(sbs_foam *f, uint32_t trial_steps, uint32_t *steps_per_phase, uint32_t *strip_rows);
+int sbs_foam_stream(const sbs_foam *f, void **out);
+
+/* ------------------------------------------------------------------ */
 /* Spectral interference contracted against colour-matching functions */
 /* ------------------------------------------------------------------ */
 #define SBS_SPECTRAL_TC_BF16 0 /* BF16 spectra x BF16 CMF on the tensor cores (tcgen05), FP32 accumulation */

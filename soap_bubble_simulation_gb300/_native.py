@@ -174,6 +174,17 @@ SIGNATURES: dict[str, list] = {
     "sbs_schlick_rgb_batch": [_F, _FP, _P, _P, _SZ, _P, _I, _P],
     "sbs_lut_rgba8_lookup_batch": [_P, _U32, _U32, _F, _F, _I, _P, _P, _SZ, _P, _I, _P],
     "sbs_lut2d_lookup_batch": [_P, _U32, _U32, _D, _D, _P, _P, _SZ, _P, _I, _P],
+    "sbs_foam_create": [_U32, _P, _P, C.POINTER(SbsDrainageParams), C.POINTER(_P)],
+    "sbs_foam_destroy": [_P],
+    "sbs_foam_total_cells": [_P, C.POINTER(C.c_uint64)],
+    "sbs_foam_set_thickness": [_P, _U32, _P, _SZ, _I],
+    "sbs_foam_get_thickness": [_P, _U32, _P, _SZ, _I],
+    "sbs_foam_set_concentration": [_P, _U32, _P, _SZ, _I],
+    "sbs_foam_get_concentration": [_P, _U32, _P, _SZ, _I],
+    "sbs_foam_run": [_P, _U32],
+    "sbs_foam_set_tiles": [_P, _U32, _U32],
+    "sbs_foam_autotune": [_P, _U32, _U32P, _U32P],
+    "sbs_foam_stream": [_P, C.POINTER(_P)],
     "sbs_spectral_rgb": [_P, _P, _P, _SZ, _P, _U32, _P, _I, _P, _I, _P],
     "sbs_drainage_vertex_colors": [_P, _P, _SZ, _P, _U32, _U32, _D, _D, _P, _I],
 }

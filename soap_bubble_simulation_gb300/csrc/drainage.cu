@@ -118,6 +118,32 @@ void TfeClock::advance(double t, double dt, int nt, int np, TfeStep *out) {
     out->nf = n;
 }
 
+// Per-row coefficients of the WGSL semantics (f32 angle grid, sin floor 1e-4 with sign,
+// drainage.wgsl:92-101) and the kernel constants, from the DrainageParams; f64 volume weights.
+void wgsl_tables(int H, int W, const sbs_drainage_params &p, std::vector<float4> *rows, std::vector<double> *w,
+                 float *b, float *DR2, float *DsR2, float *Gt, float *M) {
+    const float PI32 = 3.14159265358979323846f;
+    const float dth32 = PI32 / (float)(H - 1), dph32 = 2.0f * PI32 / (float)W;
+    const double dth = (double)dth32, dph = (double)dph32, R = (double)p.bubble_radius;
+    const double coef = (double)p.density * (double)p.gravity / (3.0 * (double)p.viscosity);
+    rows->resize(H);
+    if (w) w->resize(H);
+    const double vdth = kPi / (double)(H - 1), vdph = 2.0 * kPi / (double)W;
+    for (int i = 0; i < H; ++i) {
+        const float th32 = (float)i * dth32;
+        const double sn = std::sin((double)th32), cs = std::cos((double)th32);
+        const double ss = std::fabs(sn) < 1e-4 ? (sn > 0 ? 1e-4 : (sn < 0 ? -1e-4 : 0.0)) : sn;
+        (*rows)[i] = make_float4((float)(-coef * sn), (float)((cs / ss) / (2.0 * dth)),
+                                 (float)((1.0 / (ss * ss)) / (dph * dph)), (float)(1.0 / (2.0 * dph * R * ss)));
+        if (w) (*w)[i] = R * R * std::sin((double)i * vdth) * vdth * vdph;
+    }
+    *b = (float)(1.0 / (dth * dth));
+    *DR2 = (float)((double)p.diffusion_coeff / (R * R));
+    *DsR2 = (float)((double)p.surfactant_diffusion / (R * R));
+    *Gt = (float)(1.0 / (2.0 * dth * R));
+    *M = (float)((double)p.marangoni_coeff * (double)p.gamma_reduction);
+}
+
 }  // namespace sbs
 
 using namespace sbs;
@@ -157,28 +183,7 @@ struct WgslConsts {
 };
 
 void rows_wgsl(sbs_drainage *h, std::vector<float4> &rows, std::vector<double> &w, WgslConsts *k) {
-    const int H = h->nt, W = h->np;
-    const sbs_drainage_params &p = h->params;
-    const float PI32 = 3.14159265358979323846f;
-    const float dth32 = PI32 / (float)(H - 1), dph32 = 2.0f * PI32 / (float)W;
-    const double dth = (double)dth32, dph = (double)dph32, R = (double)p.bubble_radius;
-    const double coef = (double)p.density * (double)p.gravity / (3.0 * (double)p.viscosity);
-    rows.resize(H);
-    w.resize(H);
-    const double vdth = kPi / (double)(H - 1), vdph = 2.0 * kPi / (double)W;
-    for (int i = 0; i < H; ++i) {
-        const float th32 = (float)i * dth32;
-        const double sn = std::sin((double)th32), cs = std::cos((double)th32);
-        const double ss = std::fabs(sn) < 1e-4 ? (sn > 0 ? 1e-4 : (sn < 0 ? -1e-4 : 0.0)) : sn;
-        rows[i] = make_float4((float)(-coef * sn), (float)((cs / ss) / (2.0 * dth)),
-                              (float)((1.0 / (ss * ss)) / (dph * dph)), (float)(1.0 / (2.0 * dph * R * ss)));
-        w[i] = R * R * std::sin((double)i * vdth) * vdth * vdph;
-    }
-    k->b = (float)(1.0 / (dth * dth));
-    k->DR2 = (float)((double)p.diffusion_coeff / (R * R));
-    k->DsR2 = (float)((double)p.surfactant_diffusion / (R * R));
-    k->Gt = (float)(1.0 / (2.0 * dth * R));
-    k->M = (float)((double)p.marangoni_coeff * (double)p.gamma_reduction);
+    wgsl_tables(h->nt, h->np, h->params, &rows, &w, &k->b, &k->DR2, &k->DsR2, &k->Gt, &k->M);
 }
 
 using Consts = KernelConsts;

@@ -149,6 +149,10 @@ struct KernelConsts {
 
 cudaError_t launch_fill(float *p, size_t pitch, int nt, int np, float v, cudaStream_t s);
 
+// Per-row coefficients and kernel constants of the WGSL semantics for an H x W grid.
+void wgsl_tables(int H, int W, const sbs_drainage_params &p, std::vector<float4> *rows, std::vector<double> *w,
+                 float *b, float *DR2, float *DsR2, float *Gt, float *M);
+
 }  // namespace sbs
 
 // ---------------------------------------------------------------------------

@@ -1,0 +1,86 @@
+// One row of the time-skewed register pipeline that advances a warp's 128-column window of the
+// WGSL-semantics fields by K steps (used by the single-bubble and the batched foam kernels, so
+// both round identically). See drainage_wtb.cu for the scheme.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "cell.cuh"
+
+namespace sbs {
+
+#ifndef SBS_WTB_PREFETCH
+#define SBS_WTB_PREFETCH 1  // request level-0 row t+1 while computing row t (0: load it at row t)
+#endif
+
+struct Wtb {
+    const float *hin, *cin;  // column-offset input pointers of this lane
+    float *hout, *cout;      // column-offset output pointers
+    const float4 *sco;       // this strip's per-row coefficients in shared memory, from row sco_base
+    int sco_base;
+    int nt, pitch, r0, r1;
+    bool store;
+    float b, DR2, DsR2, Gt, M, dt, crit;
+    const double *vol_w;
+};
+
+// One pipeline iteration: load level-0 row t, then compute level l of row t - l for l = 1..K.
+// Slot P holds the row most recently written to each level's window.
+// With SBS_WTB_PREFETCH the level-0 row t arrives in (ph, pc), loaded one iteration earlier, and
+// row t + 1 is requested here; otherwise row t is loaded here.
+template <int K, int P, bool VOL, bool MAR, bool CG = false>
+__device__ __forceinline__ void wtb_iter(const Wtb &w, int t, float4 (&wh)[K][3], float4 (&wc)[K][3], float4 &ph,
+                                         float4 &pc, double &vacc) {
+    constexpr int CUR = (P + 2) % 3, UP = (P + 1) % 3;
+    const int tl = SBS_WTB_PREFETCH ? t + 1 : t;
+    float4 nh = make_float4(0.f, 0.f, 0.f, 0.f), nc = nh;
+    if (tl >= 0 && tl < w.nt) {
+        const float4 *ph4 = reinterpret_cast<const float4 *>(w.hin + (size_t)tl * w.pitch);
+        const float4 *pc4 = reinterpret_cast<const float4 *>(w.cin + (size_t)tl * w.pitch);
+        nh = CG ? __ldcg(ph4) : __ldg(ph4);
+        nc = CG ? __ldcg(pc4) : __ldg(pc4);
+    }
+    if (SBS_WTB_PREFETCH) {
+        wh[0][P] = ph;
+        wc[0][P] = pc;
+        ph = nh;
+        pc = nc;
+    } else {
+        wh[0][P] = nh;
+        wc[0][P] = nc;
+    }
+#pragma unroll
+    for (int l = 1; l <= K; ++l) {
+        const int i = t - l;
+        const bool need = i >= w.r0 - (K - l) && i < w.r1 + (K - l) && i >= 0 && i < w.nt;  // warp-uniform
+        float4 oh = make_float4(0.f, 0.f, 0.f, 0.f), oc = oh;
+        if (need) {
+            const float4 hc = wh[l - 1][CUR], cc = wc[l - 1][CUR];
+            if (i == 0 || i == w.nt - 1) {  // pole rows are frozen (drainage.wgsl:85-89)
+                oh = hc;
+                oc = cc;
+            } else {
+                const float4 hu = wh[l - 1][UP], hd = wh[l - 1][P];
+                const float4 cu = wc[l - 1][UP], cd = wc[l - 1][P];
+                const float4 co = w.sco[i - w.sco_base];
+                const float hl = __shfl_up_sync(0xffffffffu, hc.w, 1), hr = __shfl_down_sync(0xffffffffu, hc.x, 1);
+                const float cl = __shfl_up_sync(0xffffffffu, cc.w, 1), cr = __shfl_down_sync(0xffffffffu, cc.x, 1);
+                const float4 hpm = make_float4(hl, hc.x, hc.y, hc.z), hpp = make_float4(hc.y, hc.z, hc.w, hr);
+                const float4 cpm = make_float4(cl, cc.x, cc.y, cc.z), cpp = make_float4(cc.y, cc.z, cc.w, cr);
+                wgsl_cell4<MAR>(hc, hu, hd, hpm, hpp, cc, cu, cd, cpm, cpp, co, w.b, w.DR2, w.DsR2, w.Gt, w.M, w.dt,
+                                w.crit, oh, oc);
+            }
+        }
+        if (l < K) {
+            wh[l][P] = oh;
+            wc[l][P] = oc;
+        } else if (need && i >= w.r0 && i < w.r1 && w.store) {
+            *reinterpret_cast<float4 *>(w.hout + (size_t)i * w.pitch) = oh;
+            *reinterpret_cast<float4 *>(w.cout + (size_t)i * w.pitch) = oc;
+            if (VOL) vacc += ((double)oh.x + (double)oh.y + (double)oh.z + (double)oh.w) * __ldg(w.vol_w + i);
+        }
+    }
+}
+
+
+}  // namespace sbs

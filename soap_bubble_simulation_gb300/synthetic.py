@@ -126,3 +126,23 @@ def delta_e76(rgb_a: np.ndarray, rgb_b: np.ndarray, white: np.ndarray) -> np.nda
         return np.stack([116 * f[:, 1] - 16, 500 * (f[:, 0] - f[:, 1]), 200 * (f[:, 1] - f[:, 2])], axis=1)
 
     return np.linalg.norm(lab(rgb_a) - lab(rgb_b), axis=1)
+
+
+# --- batched foam workload ------------------------------------------------------------------
+def foam_bubbles(n: int = 4096, seed: int = 6):
+    """Diameters log-uniform in 2-80 mm; resolution = 32 * round(512 d / 80 mm / 32) clamped to
+    [32, 512] (theta rows; phi = 2 x rows). Returns (resolution uint32 [n], radius metres f32 [n])."""
+    g = rng(seed)
+    d_mm = np.exp(g.uniform(np.log(2.0), np.log(80.0), n))
+    res = np.clip(32 * np.round(512.0 * d_mm / 80.0 / 32.0), 32, 512).astype(np.uint32)
+    return res, (d_mm * 1e-3 / 2.0).astype(np.float32)
+
+
+def foam_fields(res: np.ndarray, seed: int = 7):
+    """Per bubble: h = U[300, 800] nm x (1 + 0.05 U[-1, 1]) (f32, [res][2 res]); surfactant 0.5."""
+    g = rng(seed)
+    hs = []
+    for r in res:
+        base = g.uniform(300e-9, 800e-9)
+        hs.append((base * (1.0 + 0.05 * g.uniform(-1.0, 1.0, size=(int(r), 2 * int(r))))).astype(np.float32))
+    return hs
