@@ -31,6 +31,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include "sbs_nn.h"
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -391,6 +393,86 @@ int sbs_foam_stream(const sbs_foam *f, void **out);
  * in both memory modes (it reads back a device status flag). */
 int sbs_spectral_rgb(const float *t_nm, const float *cos_i, const float *n_film, size_t n, const float *wl_nm,
                      uint32_t nl, const float *cmf, int mode, float *rgb, int mem, void *stream);
+
+
+/* ------------------------------------------------------------------ */
+/* Drainage surrogate: conv neural operator over SBS_NN_STEPS passes   */
+/* ------------------------------------------------------------------ */
+/* The network, its features, parameter layout and GELU are defined in
+ * sbs_nn.h. The surrogate approximates SBS_NN_STEPS WGSL-semantics passes
+ * (drainage.wgsl:72-202 with marangoni_enabled = 0, where the surfactant does
+ * not feed back into the thickness) and is trained here, on this GPU, on
+ * trajectories that the plain solver generates. */
+typedef struct sbs_surrogate sbs_surrogate;
+
+#define SBS_NN_LAYERED 0 /* one kernel per layer (mma.sync tensor cores), activations through HBM */
+#define SBS_NN_FUSED 1   /* all four layers in one persistent tcgen05 kernel, activations on chip */
+
+/* New surrogate with He-initialised weights (normal, splitmix64 seed). */
+int sbs_surrogate_create(uint64_t seed, sbs_surrogate **out);
+int sbs_surrogate_destroy(sbs_surrogate *s);
+/* FP32 parameter vector, n = SBS_NN_PARAMS, host memory. */
+int sbs_surrogate_set_params(sbs_surrogate *s, const float *params, size_t n);
+int sbs_surrogate_get_params(sbs_surrogate *s, float *params, size_t n);
+/* Features of nf <= 16 fields: h, c [nf][nt][np] (nt = p[k].grid_height, np =
+ * p[k].grid_width, the same for every field), x out [nf][nt][np][8] (BF16
+ * values as f32). mem applies to h, c and x. */
+int sbs_surrogate_features(sbs_surrogate *s, uint32_t nf, const float *h, const float *c,
+                           const sbs_drainage_params *p, float *x, int mem);
+/* Network output y [nf][nt][np] (mode SBS_NN_LAYERED or SBS_NN_FUSED). */
+int sbs_surrogate_forward(sbs_surrogate *s, uint32_t nf, const float *h, const float *c,
+                          const sbs_drainage_params *p, float *y, int mode, int mem);
+/* Masked mean-square loss of the network output against target [nf][nt][np]
+ * (rows with sin(theta) >= SBS_NN_MASK_SIN) and its gradient (SBS_NN_PARAMS
+ * floats). Host memory. */
+int sbs_surrogate_loss_grad(sbs_surrogate *s, uint32_t nf, const float *h, const float *c,
+                            const sbs_drainage_params *p, const float *target, double *loss, float *grad);
+/* Training data: runs the plain WGSL-semantics solver (the sbs_gpu_drainage
+ * kernels) from (h0, c0, host) with parameters p for pairs * SBS_NN_STEPS
+ * passes and keeps the pairs + 1 snapshots on the device. Every trajectory of
+ * one surrogate has the grid of the first. */
+int sbs_surrogate_add_trajectory(sbs_surrogate *s, const float *h0, const float *c0, const sbs_drainage_params *p,
+                                 uint32_t pairs);
+int sbs_surrogate_num_trajectories(const sbs_surrogate *s, uint32_t *out);
+int sbs_surrogate_clear_data(sbs_surrogate *s);
+/* Adam (0.9, 0.999, 1e-8) with a cosine learning-rate decay from lr to lr/20
+ * over iters steps; each step a batch of `batch` (<= 16) snapshot pairs drawn
+ * (splitmix64 seed) from trajectories [0, n_train). losses (host, iters) gets
+ * each step's loss; may be null. */
+int sbs_surrogate_train(sbs_surrogate *s, uint32_t n_train, uint32_t iters, uint32_t batch, float lr, uint64_t seed,
+                        float *losses);
+typedef struct sbs_surrogate_eval {
+    double loss;              /* masked MSE of the network output against (h' - h) / kout */
+    double loss_identity;     /* the same for y = 0 (h' = h) */
+    double rel_linf;          /* max over pairs of the masked relative L-inf error of the predicted h' */
+    double rel_linf_identity; /* the same for h' = h */
+} sbs_surrogate_eval;
+/* Evaluates every pair of trajectories [first, first + count). */
+int sbs_surrogate_evaluate(sbs_surrogate *s, uint32_t first, uint32_t count, int mode, sbs_surrogate_eval *out);
+/* One surrogate rollout of a WGSL-semantics handle: h <- h + kout y, the
+ * concentration held, the clock advanced by SBS_NN_STEPS * dt. */
+int sbs_surrogate_advance(sbs_surrogate *s, sbs_drainage *h, int mode);
+typedef struct sbs_surrogate_stats {
+    uint32_t rollouts;         /* SBS_NN_STEPS-pass intervals advanced */
+    uint32_t surrogate;        /* of which by the surrogate alone */
+    uint32_t plain;            /* by the plain solver (checks and fallback) */
+    uint32_t checks;
+    uint32_t failed_checks;
+    uint32_t pad;
+    double max_check_error;    /* largest masked relative L-inf error seen in a check */
+    double last_check_error;
+} sbs_surrogate_stats;
+/* Surrogate-accelerated run of `passes` WGSL passes (a multiple of
+ * SBS_NN_STEPS) on handle h. Every check_every-th interval (0 = never) both
+ * the surrogate and the plain solver advance from the same state; the plain
+ * result is kept, and if the masked relative L-inf difference exceeds tol the
+ * plain solver also runs the next check_every - 1 intervals. */
+int sbs_surrogate_rollout(sbs_surrogate *s, sbs_drainage *h, uint32_t passes, uint32_t check_every, double tol,
+                          int mode, sbs_surrogate_stats *stats);
+/* Masked relative L-inf difference max|a - b| / max|b| over rows with
+ * sin(theta) >= SBS_NN_MASK_SIN of two nt x np fields (device or host). */
+int sbs_surrogate_masked_error(const float *a, const float *b, uint32_t nt, uint32_t np, int mem, double *out);
+int sbs_surrogate_stream(const sbs_surrogate *s, void **out);
 
 #ifdef __cplusplus
 }

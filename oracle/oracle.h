@@ -151,6 +151,32 @@ void orc_vertex_colors(const double *field, uint32_t n_theta, uint32_t n_phi, co
 void orc_spectral_rgb(const float *t_nm, const float *cos_i, const float *n_film, size_t n,
                       const double *wl, uint32_t nl, const double *cmf /*nl*3*/, double *rgb);
 
+
+/* ------------------------------------------------------------------ */
+/* Drainage surrogate (conv neural operator, include/sbs_nn.h)          */
+/* ------------------------------------------------------------------ */
+/* Restates the network definition of include/sbs_nn.h in double arithmetic on BF16-rounded
+ * operands (x, weights, activations, and in the backward pass the per-layer output gradients),
+ * rounding the layer pre-activations to float where the CUDA path holds them in FP32.
+ * Tensors are channel-last: [nb][nt][np][ch]. */
+/* features of one field (nt = grid_height, np = grid_width of p); x: nt*np*8 BF16-valued floats */
+void orc_nn_features(const float *h, const float *c, const orc_wgsl_params *p, float *x);
+/* kout of one field (include/sbs_nn.h) */
+float orc_nn_kout(const orc_wgsl_params *p);
+/* forward: y (nb*nt*np) from x (nb*nt*np*8) with the FP32 parameter vector (BF16-rounded inside) */
+void orc_nn_forward(const float *params, uint32_t nb, uint32_t nt, uint32_t np, const float *x, float *y);
+/* masked mean-square loss of y against target over rows with sin(theta) >= SBS_NN_MASK_SIN and its
+ * gradient (SBS_NN_PARAMS floats). Returns the loss. */
+double orc_nn_loss_grad(const float *params, uint32_t nb, uint32_t nt, uint32_t np, const float *x,
+                        const float *target, float *grad);
+/* h_out = surrogate update of h given the network output y (include/sbs_nn.h "Map") */
+void orc_nn_apply(const float *h, const float *y, uint32_t nt, uint32_t np, float kout, float *h_out);
+/* 1: drop every BF16 / float rounding (all-double network), for finite-difference checks */
+void orc_nn_set_exact(int exact);
+/* gelu and its derivative in the FP32 form of include/sbs_nn.h */
+float orc_nn_gelu(float x);
+float orc_nn_gelu_grad(float x);
+
 #ifdef __cplusplus
 }
 #endif

@@ -102,6 +102,14 @@ _SIGS = {
     "orc_lut2d_lookup": ([_P, _U32, _U32, _D, _D, _D, _D, _P], None),
     "orc_vertex_colors": ([_P, _U32, _U32, _P, _SZ, _P, _U32, _U32, _D, _D, _P], None),
     "orc_spectral_rgb": ([_P, _P, _P, _SZ, _P, _U32, _P, _P], None),
+    "orc_nn_features": ([_P, _P, C.POINTER(OrcWgslParams), _P], None),
+    "orc_nn_kout": ([C.POINTER(OrcWgslParams)], _F),
+    "orc_nn_forward": ([_P, _U32, _U32, _U32, _P, _P], None),
+    "orc_nn_loss_grad": ([_P, _U32, _U32, _U32, _P, _P, _P], _D),
+    "orc_nn_apply": ([_P, _P, _U32, _U32, _F, _P], None),
+    "orc_nn_gelu": ([_F], _F),
+    "orc_nn_set_exact": ([_I], None),
+    "orc_nn_gelu_grad": ([_F], _F),
 }
 
 
@@ -337,3 +345,60 @@ def spectral_rgb(t, ci, n, wl, cmf):
     out = np.zeros((t.size, 3))
     lib().orc_spectral_rgb(_p(t), _p(ci), _p(n), t.size, _p(wl), wl.size, _p(cmf), _p(out))
     return out
+
+
+# ---------------------------------------------------------------- drainage surrogate (include/sbs_nn.h)
+NN_PARAMS = 21121
+
+
+def nn_features(h, c, params: OrcWgslParams) -> np.ndarray:
+    """Features [nt][np][8] (BF16 values held in float32) of one field."""
+    h = np.ascontiguousarray(h, dtype=np.float32)
+    c = np.ascontiguousarray(c, dtype=np.float32)
+    x = np.empty(h.shape + (8,), dtype=np.float32)
+    lib().orc_nn_features(_p(h), _p(c), C.byref(params), _p(x))
+    return x
+
+
+def nn_kout(params: OrcWgslParams) -> float:
+    return float(lib().orc_nn_kout(C.byref(params)))
+
+
+def nn_forward(theta, x) -> np.ndarray:
+    """Network output y [nb][nt][np] for features x [nb][nt][np][8]."""
+    theta = np.ascontiguousarray(theta, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    nb, nt, np_ = x.shape[:3]
+    y = np.empty((nb, nt, np_), dtype=np.float32)
+    lib().orc_nn_forward(_p(theta), nb, nt, np_, _p(x), _p(y))
+    return y
+
+
+def nn_loss_grad(theta, x, target):
+    theta = np.ascontiguousarray(theta, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    target = np.ascontiguousarray(target, dtype=np.float32)
+    nb, nt, np_ = x.shape[:3]
+    g = np.empty(NN_PARAMS, dtype=np.float32)
+    loss = lib().orc_nn_loss_grad(_p(theta), nb, nt, np_, _p(x), _p(target), _p(g))
+    return float(loss), g
+
+
+def nn_apply(h, y, kout: float) -> np.ndarray:
+    h = np.ascontiguousarray(h, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    out = np.empty_like(h)
+    lib().orc_nn_apply(_p(h), _p(y), h.shape[0], h.shape[1], float(kout), _p(out))
+    return out
+
+
+def nn_set_exact(exact: bool) -> None:
+    lib().orc_nn_set_exact(1 if exact else 0)
+
+
+def nn_gelu(x: float) -> float:
+    return float(lib().orc_nn_gelu(float(x)))
+
+
+def nn_gelu_grad(x: float) -> float:
+    return float(lib().orc_nn_gelu_grad(float(x)))

@@ -15,6 +15,7 @@ from .interference import (LUT_ANGLE_SAMPLES, LUT_MAX_THICKNESS_NM, LUT_THICKNES
                            sample_interference_lut, schlick_interference_rgb, spectral_rgb, wavelengths)
 from ._native import SbsError
 from .foam import FoamDrainage
+from .surrogate import SURROGATE_STEPS, DrainageSurrogate, field_params, masked_error
 
 __all__ = [
     "BubbleParameters", "ConfigError", "EnvironmentParameters", "FluidParameters", "SimulationConfig",
@@ -22,5 +23,6 @@ __all__ = [
     "film_volume_device", "LUT_ANGLE_SAMPLES", "LUT_MAX_THICKNESS_NM", "LUT_THICKNESS_SAMPLES",
     "FresnelCoefficients", "InterferenceCalculator", "RgbColor", "constants", "generate_interference_lut",
     "generate_interference_lut_array", "lookup_2d", "sample_interference_lut", "schlick_interference_rgb", "spectral_rgb",
-    "wavelengths", "SbsError", "FoamDrainage",
+    "wavelengths", "SbsError", "FoamDrainage", "SURROGATE_STEPS", "DrainageSurrogate", "field_params",
+    "masked_error",
 ]

@@ -32,6 +32,10 @@ SPECTRAL_TC_BF16 = 0
 SPECTRAL_FP32 = 1
 LOOKUP_GRID = 0
 LOOKUP_TEXEL = 1
+NN_LAYERED = 0
+NN_FUSED = 1
+NN_PARAMS = 21121
+NN_STEPS = 64
 
 _ERR_NAMES = {
     SBS_E_INVALID: "SBS_E_INVALID",
@@ -187,6 +191,22 @@ SIGNATURES: dict[str, list] = {
     "sbs_foam_stream": [_P, C.POINTER(_P)],
     "sbs_spectral_rgb": [_P, _P, _P, _SZ, _P, _U32, _P, _I, _P, _I, _P],
     "sbs_drainage_vertex_colors": [_P, _P, _SZ, _P, _U32, _U32, _D, _D, _P, _I],
+    "sbs_surrogate_create": [C.c_uint64, C.POINTER(_P)],
+    "sbs_surrogate_destroy": [_P],
+    "sbs_surrogate_set_params": [_P, _P, _SZ],
+    "sbs_surrogate_get_params": [_P, _P, _SZ],
+    "sbs_surrogate_features": [_P, _U32, _P, _P, _P, _P, _I],
+    "sbs_surrogate_forward": [_P, _U32, _P, _P, _P, _P, _I, _I],
+    "sbs_surrogate_loss_grad": [_P, _U32, _P, _P, _P, _P, _DP, _P],
+    "sbs_surrogate_add_trajectory": [_P, _P, _P, C.POINTER(SbsDrainageParams), _U32],
+    "sbs_surrogate_num_trajectories": [_P, _U32P],
+    "sbs_surrogate_clear_data": [_P],
+    "sbs_surrogate_train": [_P, _U32, _U32, _U32, _F, C.c_uint64, _P],
+    "sbs_surrogate_evaluate": [_P, _U32, _U32, _I, _P],
+    "sbs_surrogate_advance": [_P, _P, _I],
+    "sbs_surrogate_rollout": [_P, _P, _U32, _U32, _D, _I, _P],
+    "sbs_surrogate_masked_error": [_P, _P, _U32, _U32, _I, _DP],
+    "sbs_surrogate_stream": [_P, C.POINTER(_P)],
 }
 _RESTYPES = {"sbs_last_error": C.c_char_p, "sbs_version": C.c_char_p}
 

@@ -518,6 +518,10 @@ int create_common(sbs_drainage *h) {
 
 }  // namespace
 
+namespace sbs {
+int drainage_run_async(sbs_drainage *h, uint32_t passes) { return run_steps(h, 0.0, passes, 0); }
+}  // namespace sbs
+
 extern "C" {
 
 int sbs_drainage_create(const sbs_config *cfg, sbs_drainage **out) {

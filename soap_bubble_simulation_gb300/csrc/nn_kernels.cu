@@ -1,0 +1,808 @@
+// Training-side kernels of the drainage surrogate (include/sbs_nn.h) and its layered forward
+// pass: features, 3x3 convolutions as implicit GEMMs on the tensor cores (mma.sync BF16 x BF16 ->
+// FP32), the one-channel output layer and its gradients on the FP32 pipe, loss, deterministic
+// gradient reduction, Adam, and weight packing.
+//
+// Layouts (channel-last, cells = fields x nt x np):
+//   features x        BF16 [cells][8]
+//   pre-activations y FP32 [cells][32]       activations a BF16 [cells][32]
+//   output y4 / gradient g4 FP32 [cells]     layer gradients g BF16 [cells][32]
+// A convolution tile is one row segment of kTileCols = 128 cells of one field: the block stages
+// the three input rows it reads (reflected in theta, periodic in phi) and the packed weights in
+// shared memory, and its four warps each compute 32 cells x 32 channels with m16n8k16 MMAs whose
+// A fragments are gathered by ldmatrix from the shifted rows (no im2col buffer).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "nn.cuh"
+#include "nn_kernels.h"
+#include "sbs_internal.h"
+
+namespace sbs {
+namespace nn {
+namespace {
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void ldsm_x4(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(addr));
+}
+
+__device__ __forceinline__ void ldsm_x4_t(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(addr));
+}
+
+__device__ __forceinline__ void mma16816(float *d, const uint32_t *a, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+        "{%0, %1, %2, %3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ int refl_row(int i, int nt) { return i < 0 ? 1 : (i >= nt ? nt - 2 : i); }
+
+// Byte offset of 16-byte channel chunk `ch` of staged cell `q` in a row buffer of cells with CIN
+// channels. 32-channel cells (64 B) are XOR-swizzled so that the 8 rows of an ldmatrix phase
+// fall into distinct bank groups.
+template <int CIN>
+__device__ __forceinline__ uint32_t cell_off(int q, int ch) {
+    if constexpr (CIN == 8) {
+        return (uint32_t)q * 16u;
+    } else {
+        return (uint32_t)q * 64u + ((uint32_t)(ch ^ ((q >> 1) & 3)) << 4);
+    }
+}
+
+constexpr int kRowCells = kTileCols + 2;  // staged columns j0-1 .. j0+128
+
+// ----------------------------------------------------------------------------------- features
+__global__ void features_kernel(Fields fs, GridTab g, uint4 *x) {
+    const int b = blockIdx.z, i = blockIdx.y;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= g.np) return;
+    const Field &f = fs.f[b];
+    const int nt = g.nt, np = g.np;
+    const float *rc = f.h + (size_t)i * f.pitch;
+    const float *rn = f.h + (size_t)refl_row(i - 1, nt) * f.pitch;
+    const float *rs = f.h + (size_t)refl_row(i + 1, nt) * f.pitch;
+    const float4 row = g.rows[i];
+    const float hc = rc[j], hn = rn[j], hs = rs[j];
+    const float hw = rc[j == 0 ? np - 1 : j - 1], he = rc[j + 1 == np ? 0 : j + 1];
+    const float cc = f.c[(size_t)i * f.pitch + j];
+    const float h2 = __fadd_rn(hc, hc);
+    float v[8];
+    v[0] = __fmul_rn(__fsub_rn(hc, SBS_NN_H0), SBS_NN_INV_HS);
+    v[1] = __fmul_rn(__fsub_rn(__fadd_rn(hn, hs), h2), g.ct);
+    v[2] = __fmul_rn(__fsub_rn(__fadd_rn(hw, he), h2), row.x);
+    v[3] = __fmul_rn(__fsub_rn(hs, hn), row.y);
+    v[4] = __fmul_rn(__fsub_rn(cc, 0.5f), 10.f);
+    v[5] = f.f5;
+    v[6] = f.f6;
+    v[7] = __fmul_rn(__fmul_rn(__fmul_rn(hc, hc), hc), __fmul_rn(f.gk, row.z));
+    uint4 o;
+    o.x = pack2(clampf(v[0]), clampf(v[1]));
+    o.y = pack2(clampf(v[2]), clampf(v[3]));
+    o.z = pack2(clampf(v[4]), clampf(v[5]));
+    o.w = pack2(clampf(v[6]), clampf(v[7]));
+    x[((size_t)b * nt + i) * np + j] = o;
+}
+
+// ------------------------------------------------------------------ 3x3 convolution (mma.sync)
+// BWD = false: y = conv(x, W) + b, a = bf16(gelu(y))     (x: CIN channels, packed W [oc][tap*CIN+ic])
+// BWD = true : dX = conv^T(g, W), g_prev = bf16(dX * gelu'(y_prev))  (g: 32 channels, packed W
+//              [ic][tap*32+oc]); the transpose reads g at (i - dy, j - dx) with zero rows outside
+//              the grid, plus the reflected sources: row 1 also receives output row 0's dy = -1
+//              taps, row nt-2 output row nt-1's dy = +1 taps.
+struct ConvArgs {
+    const bf16 *in;
+    const bf16 *w;
+    const float *bias;
+    const float *yprev;
+    float *yout;
+    bf16 *aout;
+    int nt, np, tiles_x;
+};
+
+template <int CIN, bool BWD>
+__global__ void __launch_bounds__(128) conv_kernel(ConvArgs a) {
+    constexpr int KC = 9 * CIN / 8 + (CIN == 8 ? 1 : 0);  // 16-byte K chunks (padded to even)
+    constexpr int KS = KC / 2;                             // k16 steps
+    constexpr int KP = KC * 8;                             // packed K
+    constexpr int WS = KP + 8;                             // smem weight row stride (elements)
+    constexpr int CPC = CIN / 8;                           // chunks per cell
+    constexpr int CB = CIN * 2;                            // bytes per staged cell
+    constexpr int ROWB = kRowCells * CB;
+    extern __shared__ __align__(16) uint8_t smem[];
+    uint8_t *sIn = smem;                    // 4 row buffers
+    bf16 *sW = (bf16 *)(smem + 4 * ROWB);   // [32][WS]
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tile = blockIdx.x;
+    const int tx = tile % a.tiles_x;
+    const int row_id = tile / a.tiles_x;  // field * nt + i
+    const int i = row_id % a.nt, b = row_id / a.nt;
+    const int nt = a.nt, np = a.np, j0 = tx * kTileCols;
+
+    // weights
+    for (int e = tid; e < 32 * KP / 8; e += 128) {
+        const int n = e / (KP / 8), k8 = e % (KP / 8);
+        *(uint4 *)(sW + n * WS + k8 * 8) = *(const uint4 *)(a.w + (size_t)n * KP + k8 * 8);
+    }
+    // source rows: buffer dy+1 holds the row read by taps with row offset dy; buffer 3 the extra
+    int src[4];
+    int extra_t0 = -1;
+    if (!BWD) {
+        src[0] = refl_row(i - 1, nt);
+        src[1] = i;
+        src[2] = refl_row(i + 1, nt);
+        src[3] = -1;
+    } else {
+        src[0] = i + 1 < nt ? i + 1 : -1;  // dy = -1 reads g at i + 1
+        src[1] = i;
+        src[2] = i - 1 >= 0 ? i - 1 : -1;  // dy = +1 reads g at i - 1
+        src[3] = -1;
+        if (i == 1) {
+            src[3] = 0;
+            extra_t0 = 0;  // taps (dy = -1, dx = -1..1)
+        } else if (i == nt - 2) {
+            src[3] = nt - 1;
+            extra_t0 = 6;  // taps (dy = +1, dx = -1..1)
+        }
+    }
+    const bf16 *base = a.in + (size_t)b * nt * np * CIN;
+    for (int e = tid; e < 4 * kRowCells * CPC; e += 128) {
+        const int rb = e / (kRowCells * CPC), r = e % (kRowCells * CPC);
+        const int q = r / CPC, ch = r % CPC;
+        int col = (j0 - 1 + q) % np;
+        col = col < 0 ? col + np : col;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (src[rb] >= 0) v = *(const uint4 *)(base + ((size_t)src[rb] * np + col) * CIN + ch * 8);
+        *(uint4 *)(sIn + rb * ROWB + cell_off<CIN>(q, ch)) = v;
+    }
+    __syncthreads();
+
+    float acc[2][4][4];
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int n = 0; n < 4; ++n)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) acc[m][n][r] = 0.f;
+
+    const uint32_t sIn_u = smem_addr(sIn), sW_u = smem_addr(sW);
+    const int q8 = lane >> 3, r8 = lane & 7;
+
+    auto kstep = [&](int c0, int buf_override) {
+        // A: two m-tiles
+        uint32_t af[2][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+            const int rr = (q8 & 1) * 8 + r8;
+            int c = c0 + (q8 >> 1);
+            if (c >= 9 * CPC) c = 0;  // K padding chunk: finite data against zero weights
+            const int t = c / CPC, ch = c % CPC;
+            const int dy = t / 3 - 1, dx = t % 3 - 1;
+            const int buf = buf_override >= 0 ? buf_override : dy + 1;
+            const int q = 32 * warp + 16 * mt + rr + (BWD ? -dx : dx) + 1;
+            ldsm_x4(sIn_u + buf * ROWB + cell_off<CIN>(q, ch), af[mt][0], af[mt][1], af[mt][2], af[mt][3]);
+        }
+        // B: four n-tiles, two ldmatrix.x4
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            const int n = (2 * p + (q8 >> 1)) * 8 + r8;
+            const int k = c0 * 8 + (q8 & 1) * 8;
+            uint32_t b0, b1, b2, b3;
+            ldsm_x4(sW_u + (n * WS + k) * 2, b0, b1, b2, b3);
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) {
+                mma16816(acc[mt][2 * p], af[mt], b0, b1);
+                mma16816(acc[mt][2 * p + 1], af[mt], b2, b3);
+            }
+        }
+    };
+
+#pragma unroll 2
+    for (int s = 0; s < KS; ++s) kstep(2 * s, -1);
+    if (BWD && extra_t0 >= 0) {
+        for (int s = 0; s < 3 * CPC / 2; ++s) kstep(extra_t0 * CPC + 2 * s, 3);
+    }
+
+    // epilogue
+    const int g = lane >> 2, q4 = lane & 3;
+    const size_t cell0 = ((size_t)b * nt + i) * np;
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) {
+#pragma unroll
+        for (int hr = 0; hr < 2; ++hr) {
+            const int m = 32 * warp + 16 * mt + g + 8 * hr;
+            const int j = j0 + m;
+            if (j >= np) continue;
+            const size_t cell = cell0 + j;
+#pragma unroll
+            for (int nn = 0; nn < 4; ++nn) {
+                const int n = nn * 8 + 2 * q4;
+                const float v0 = acc[mt][nn][2 * hr], v1 = acc[mt][nn][2 * hr + 1];
+                if (!BWD) {
+                    const float y0 = __fadd_rn(v0, a.bias[n]), y1 = __fadd_rn(v1, a.bias[n + 1]);
+                    *(float2 *)(a.yout + cell * 32 + n) = make_float2(y0, y1);
+                    *(uint32_t *)(a.aout + cell * 32 + n) = pack2(gelu(y0), gelu(y1));
+                } else {
+                    const float2 yp = *(const float2 *)(a.yprev + cell * 32 + n);
+                    *(uint32_t *)(a.aout + cell * 32 + n) =
+                        pack2(__fmul_rn(v0, gelu_grad(yp.x)), __fmul_rn(v1, gelu_grad(yp.y)));
+                }
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------- weight gradient of a 3x3 convolution
+// D[oc][tap*CIN + ic] = sum_cells g[cell][oc] * x[src(cell, tap)][ic], db[oc] = sum_cells g.
+// Each block accumulates its strided share of tiles in registers and writes one partial row.
+struct WgradArgs {
+    const bf16 *g;
+    const bf16 *x;
+    float *partial;  // [gridDim.x][32 * 9 * CIN + 32]
+    int nt, np, tiles_x, ntiles;
+};
+
+template <int CIN>
+__global__ void __launch_bounds__(128) wgrad_kernel(WgradArgs a) {
+    constexpr int CPC = CIN / 8;
+    constexpr int CB = CIN * 2;
+    constexpr int ROWB = kRowCells * CB;
+    constexpr int NT = 9 * CIN / 8;         // n8 tiles
+    constexpr int NTW = (NT + 3) / 4;       // per warp
+    extern __shared__ __align__(16) uint8_t smem[];
+    uint8_t *sX = smem;             // 3 rows
+    uint8_t *sG = smem + 3 * ROWB;  // 128 cells
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nt = a.nt, np = a.np;
+    const int q8 = lane >> 3, r8 = lane & 7;
+    const uint32_t sX_u = smem_addr(sX), sG_u = smem_addr(sG);
+    const int nbeg = warp * NTW, nend = min(NT, nbeg + NTW);
+
+    float acc[2][NTW][4];
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int n = 0; n < NTW; ++n)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) acc[m][n][r] = 0.f;
+    float dbias = 0.f;
+
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const int tx = tile % a.tiles_x, row_id = tile / a.tiles_x;
+        const int i = row_id % nt, b = row_id / nt, j0 = tx * kTileCols;
+        const int src[3] = {refl_row(i - 1, nt), i, refl_row(i + 1, nt)};
+        const bf16 *xb = a.x + (size_t)b * nt * np * CIN;
+        __syncthreads();  // previous tile's reads done
+        for (int e = tid; e < 3 * kRowCells * CPC; e += 128) {
+            const int rb = e / (kRowCells * CPC), r = e % (kRowCells * CPC);
+            const int q = r / CPC, ch = r % CPC;
+            int col = (j0 - 1 + q) % np;
+            col = col < 0 ? col + np : col;
+            *(uint4 *)(sX + rb * ROWB + cell_off<CIN>(q, ch)) =
+                *(const uint4 *)(xb + ((size_t)src[rb] * np + col) * CIN + ch * 8);
+        }
+        const bf16 *gb = a.g + ((size_t)b * nt + i) * np * 32;
+        for (int e = tid; e < kTileCols * 4; e += 128) {
+            const int m = e >> 2, ch = e & 3;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (j0 + m < np) v = *(const uint4 *)(gb + (size_t)(j0 + m) * 32 + ch * 8);
+            *(uint4 *)(sG + cell_off<32>(m, ch)) = v;
+        }
+        __syncthreads();
+        if (tid < 32) {
+            float s = 0.f;
+            for (int m = 0; m < kTileCols; ++m) {
+                const bf16 *p = (const bf16 *)(sG + cell_off<32>(m, tid >> 3)) + (tid & 7);
+                s += __bfloat162float(*p);
+            }
+            dbias += s;
+        }
+        if (nbeg < nend) {
+#pragma unroll 1
+            for (int s = 0; s < kTileCols / 16; ++s) {
+                uint32_t af[2][4];
+#pragma unroll
+                for (int mt = 0; mt < 2; ++mt) {
+                    const int ch = 2 * mt + (q8 & 1);
+                    const int m = 16 * s + 8 * (q8 >> 1) + r8;
+                    ldsm_x4_t(sG_u + cell_off<32>(m, ch), af[mt][0], af[mt][1], af[mt][2], af[mt][3]);
+                }
+#pragma unroll
+                for (int jn = 0; jn < NTW; jn += 2) {
+                    // n-tiles nbeg + jn and nbeg + jn + 1 (the second clamped to the first when absent)
+                    int nb = nbeg + jn + (q8 >> 1);
+                    if (nb >= nend) nb = nbeg + jn;
+                    const int t = (nb * 8) / CIN, ch = ((nb * 8) % CIN) / 8;
+                    const int dy = t / 3 - 1, dx = t % 3 - 1;
+                    const int m = 16 * s + 8 * (q8 & 1) + r8;
+                    uint32_t b0, b1, b2, b3;
+                    ldsm_x4_t(sX_u + (dy + 1) * ROWB + cell_off<CIN>(m + dx + 1, ch), b0, b1, b2, b3);
+#pragma unroll
+                    for (int mt = 0; mt < 2; ++mt) {
+                        if (nbeg + jn < nend) mma16816(acc[mt][jn], af[mt], b0, b1);
+                        if (jn + 1 < NTW && nbeg + jn + 1 < nend) mma16816(acc[mt][jn + 1], af[mt], b2, b3);
+                    }
+                }
+            }
+        }
+    }
+    float *out = a.partial + (size_t)blockIdx.x * (32 * 9 * CIN + 32);
+    const int g = lane >> 2, q4 = lane & 3;
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int jn = 0; jn < NTW; ++jn) {
+            if (nbeg + jn >= nend) continue;
+            const int n = (nbeg + jn) * 8 + 2 * q4;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int oc = 16 * mt + g + 8 * (r >> 1);
+                out[oc * 9 * CIN + n + (r & 1)] = acc[mt][jn][r];
+            }
+        }
+    if (tid < 32) out[32 * 9 * CIN + tid] = dbias;
+}
+
+// ------------------------------------------------------------ output layer (one channel, FP32)
+// y4 = b4 + sum_{tap, ic} W4[tap][ic] a3[src][ic]; with a target, also the masked loss gradient
+// g4 = 2 (y4 - target) / n_mask and per-block partial sums of (y4 - target)^2.
+struct OutArgs {
+    const bf16 *a3;
+    const float *w4;  // [9][32], BF16-rounded values
+    const float *b4;
+    float *y4;
+    const float *target;  // null: forward only
+    float *g4;
+    double *loss_part;
+    float inv_nmask2;  // 2 / n_mask
+    GridTab g;
+    int nf;
+};
+
+__global__ void out_kernel(OutArgs a) {
+    __shared__ float sw[9 * 32];
+    __shared__ double sred[8];
+    for (int e = threadIdx.x; e < 9 * 32; e += blockDim.x) sw[e] = a.w4[e];
+    __syncthreads();
+    const int nt = a.g.nt, np = a.g.np;
+    const size_t cells = (size_t)a.nf * nt * np;
+    const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double l = 0.0;
+    if (c < cells) {
+        const int j = (int)(c % np), i = (int)((c / np) % nt);
+        const size_t fb = (c / ((size_t)np * nt)) * nt * np;
+        float y = *a.b4;
+        for (int t = 0; t < 9; ++t) {
+            const int dy = t / 3 - 1, dx = t % 3 - 1;
+            const int r = refl_row(i + dy, nt);
+            int q = j + dx;
+            q = q < 0 ? q + np : (q >= np ? q - np : q);
+            const uint4 *p = (const uint4 *)(a.a3 + (fb + (size_t)r * np + q) * 32);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint4 v = p[k];
+                const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const __nv_bfloat162 h2 = *reinterpret_cast<const __nv_bfloat162 *>(&w[e]);
+                    const float2 f = __bfloat1622float2(h2);
+                    y = __fmaf_rn(sw[t * 32 + k * 8 + 2 * e], f.x, y);
+                    y = __fmaf_rn(sw[t * 32 + k * 8 + 2 * e + 1], f.y, y);
+                }
+            }
+        }
+        a.y4[c] = y;
+        if (a.target) {
+            const float m = a.g.rows[i].w;
+            float gr = 0.f;
+            if (m != 0.f) {
+                const float d = __fsub_rn(y, a.target[c]);
+                l = (double)d * (double)d;
+                gr = __fmul_rn(d, a.inv_nmask2);
+            }
+            a.g4[c] = gr;
+        }
+    }
+    if (a.target) {
+        for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+        if ((threadIdx.x & 31) == 0) sred[threadIdx.x >> 5] = l;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0;
+            for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sred[k];
+            a.loss_part[blockIdx.x] = s;
+        }
+    }
+}
+
+// dW4[tap][ic] = sum g4[cell] a3[src(cell,tap)][ic], db4 = sum g4: 289 threads per block, each
+// block a contiguous chunk of cells; partial rows [block][289].
+struct Wgrad4Args {
+    const float *g4;
+    const bf16 *a3;
+    float *partial;
+    GridTab g;
+    size_t cells, chunk;
+};
+
+__global__ void wgrad4_kernel(Wgrad4Args a) {
+    __shared__ float sg[256];
+    const int tid = threadIdx.x;
+    const int t = tid / 32, ic = tid % 32;
+    const int nt = a.g.nt, np = a.g.np;
+    const int dy = t / 3 - 1, dx = t % 3 - 1;
+    const size_t c0 = (size_t)blockIdx.x * a.chunk;
+    const size_t c1 = min(a.cells, c0 + a.chunk);
+    float acc = 0.f;
+    for (size_t cb = c0; cb < c1; cb += 256) {
+        __syncthreads();
+        if (tid < 256) sg[tid] = cb + tid < c1 ? a.g4[cb + tid] : 0.f;
+        __syncthreads();
+        const int n = (int)min((size_t)256, c1 - cb);
+        if (tid < 288) {
+            for (int k = 0; k < n; ++k) {
+                const float gv = sg[k];
+                if (gv == 0.f) continue;
+                const size_t c = cb + k;
+                const int j = (int)(c % np), i = (int)((c / np) % nt);
+                const size_t fb = (c / ((size_t)np * nt)) * nt * np;
+                const int r = refl_row(i + dy, nt);
+                int q = j + dx;
+                q = q < 0 ? q + np : (q >= np ? q - np : q);
+                acc = __fmaf_rn(gv, __bfloat162float(a.a3[(fb + (size_t)r * np + q) * 32 + ic]), acc);
+            }
+        } else if (tid == 288) {
+            for (int k = 0; k < n; ++k) acc = __fadd_rn(acc, sg[k]);
+        }
+    }
+    if (tid < 289) a.partial[(size_t)blockIdx.x * 289 + tid] = acc;
+}
+
+// g3[cell][ic] = bf16( (sum over the taps that read `cell` of g4[out] W4[tap][ic]) * gelu'(y3) ),
+// one warp per cell, lane = ic.
+struct Dgrad4Args {
+    const float *g4;
+    const float *w4;
+    const float *y3;
+    bf16 *g3;
+    GridTab g;
+    size_t cells;
+};
+
+__global__ void dgrad4_kernel(Dgrad4Args a) {
+    const size_t c = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int ic = threadIdx.x & 31;
+    if (c >= a.cells) return;
+    const int nt = a.g.nt, np = a.g.np;
+    const int j = (int)(c % np), i = (int)((c / np) % nt);
+    const size_t fb = (c / ((size_t)np * nt)) * nt * np;
+    float s = 0.f;
+    for (int t = 0; t < 9; ++t) {
+        const int dy = t / 3 - 1, dx = t % 3 - 1;
+        const int r = i - dy;
+        int q = j - dx;
+        q = q < 0 ? q + np : (q >= np ? q - np : q);
+        if (r >= 0 && r < nt) s = __fmaf_rn(a.g4[fb + (size_t)r * np + q], a.w4[t * 32 + ic], s);
+        if (i == 1 && dy == -1) s = __fmaf_rn(a.g4[fb + q], a.w4[t * 32 + ic], s);
+        if (i == nt - 2 && dy == 1) s = __fmaf_rn(a.g4[fb + (size_t)(nt - 1) * np + q], a.w4[t * 32 + ic], s);
+    }
+    a.g3[c * 32 + ic] = __float2bfloat16_rn(__fmul_rn(s, gelu_grad(a.y3[c * 32 + ic])));
+}
+
+// sum of partial rows (fixed order) scattered into the canonical parameter layout
+// W[tap][oc][ic] (partial column oc * 9 * CIN + tap * CIN + ic) and b[oc].
+__global__ void reduce_partials_kernel(const float *partial, int nblocks, int ci, int co, float *grad_w,
+                                       float *grad_b) {
+    const int ncol = co * 9 * ci + co;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ncol) return;
+    float s = 0.f;
+    for (int k = 0; k < nblocks; ++k) s = __fadd_rn(s, partial[(size_t)k * ncol + e]);
+    if (e < co * 9 * ci) {
+        const int oc = e / (9 * ci), r = e % (9 * ci), t = r / ci, ic = r % ci;
+        grad_w[((size_t)t * co + oc) * ci + ic] = s;
+    } else {
+        grad_b[e - co * 9 * ci] = s;
+    }
+}
+
+// layer-4 partial rows are [block][tap*32 + ic] then db4
+__global__ void reduce4_kernel(const float *partial, int nblocks, float *grad_w4, float *grad_b4) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= 289) return;
+    float s = 0.f;
+    for (int k = 0; k < nblocks; ++k) s = __fadd_rn(s, partial[(size_t)k * 289 + e]);
+    if (e < 288)
+        grad_w4[e] = s;
+    else
+        *grad_b4 = s;
+}
+
+__global__ void adam_kernel(float *theta, float *m, float *v, const float *grad, int n, float lr, float b1,
+                            float b2, float eps, float c1, float c2) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const float g = grad[e];
+    const float mm = b1 * m[e] + (1.f - b1) * g;
+    const float vv = b2 * v[e] + (1.f - b2) * g * g;
+    m[e] = mm;
+    v[e] = vv;
+    theta[e] -= lr * (mm * c1) / (sqrtf(vv * c2) + eps);
+}
+
+// BF16 weight layouts for the layered kernels from the FP32 parameter vector.
+__global__ void pack_kernel(const float *theta, Packed p) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    // forward layouts [oc][tap*CIN+ic], K padded (layer 1: 72 -> 80)
+    if (e < 32 * 80) {
+        const int oc = e / 80, k = e % 80;
+        float v = 0.f;
+        if (k < 72) v = theta[SBS_NN_W1 + ((k / 8) * 32 + oc) * 8 + (k % 8)];
+        p.wf1[e] = __float2bfloat16_rn(v);
+    }
+    if (e < 32 * 288) {
+        const int n = e / 288, k = e % 288, t = k / 32, r = k % 32;
+        // forward: n = oc, r = ic;  transpose: n = ic, r = oc
+        p.wf2[e] = __float2bfloat16_rn(theta[SBS_NN_W2 + (t * 32 + n) * 32 + r]);
+        p.wf3[e] = __float2bfloat16_rn(theta[SBS_NN_W3 + (t * 32 + n) * 32 + r]);
+        p.wb2[e] = __float2bfloat16_rn(theta[SBS_NN_W2 + (t * 32 + r) * 32 + n]);
+        p.wb3[e] = __float2bfloat16_rn(theta[SBS_NN_W3 + (t * 32 + r) * 32 + n]);
+    }
+    if (e < 288) p.w4[e] = __bfloat162float(__float2bfloat16_rn(theta[SBS_NN_W4 + e]));
+    if (e < 32) {
+        p.b[e] = theta[SBS_NN_B1 + e];
+        p.b[32 + e] = theta[SBS_NN_B2 + e];
+        p.b[64 + e] = theta[SBS_NN_B3 + e];
+    }
+    if (e == 0) p.b[96] = theta[SBS_NN_B4];
+}
+
+// h' = max(h + kout y, 0) on rows 1..nt-2, rows 0 and nt-1 copied (one field).
+__global__ void apply_kernel(const float *h, size_t pitch_in, const float *y, float kout, int nt, int np, float *out,
+                             size_t pitch_out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+    if (j >= np) return;
+    const float hc = h[(size_t)i * pitch_in + j];
+    float r = hc;
+    if (i > 0 && i + 1 < nt) r = fmaxf(__fadd_rn(hc, __fmul_rn(kout, y[(size_t)i * np + j])), 0.f);
+    out[(size_t)i * pitch_out + j] = r;
+}
+
+// target[b][cell] = (h_next - h) / kout for a batch of snapshot pairs
+struct TargetArgs {
+    const float *h0[kMaxFields];
+    const float *h1[kMaxFields];
+    float kout[kMaxFields];
+};
+
+__global__ void target_kernel(TargetArgs t, int nt, int np, float *target) {
+    const int b = blockIdx.z, i = blockIdx.y;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= np) return;
+    const size_t k = (size_t)i * np + j;
+    target[((size_t)b * nt) * np + k] = __fdiv_rn(__fsub_rn(t.h1[b][k], t.h0[b][k]), t.kout[b]);
+}
+
+// max |a - b| and max |b| over the masked rows (rows[i].w != 0) as float bit patterns (both are
+// non-negative, so unsigned order is float order); a NaN difference counts as +inf.
+__global__ void masked_err_kernel(const float *a, size_t pa, const float *b, size_t pb, const float4 *rows, int nt,
+                                  int np, unsigned *out) {
+    const int i = blockIdx.y;
+    float d = 0.f, m = 0.f;
+    if (rows[i].w != 0.f) {
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < np; j += gridDim.x * blockDim.x) {
+            const float va = a[(size_t)i * pa + j], vb = b[(size_t)i * pb + j];
+            float e = fabsf(__fsub_rn(va, vb));
+            if (e != e) e = __int_as_float(0x7f800000);
+            d = fmaxf(d, e);
+            m = fmaxf(m, fabsf(vb));
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        d = fmaxf(d, __shfl_xor_sync(0xffffffffu, d, o));
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(out, __float_as_uint(d));
+        atomicMax(out + 1, __float_as_uint(m));
+    }
+}
+
+template <int CIN, bool BWD>
+size_t conv_smem() {
+    constexpr int KC = 9 * CIN / 8 + (CIN == 8 ? 1 : 0);
+    return (size_t)4 * kRowCells * CIN * 2 + (size_t)32 * (KC * 8 + 8) * 2;
+}
+
+template <int CIN>
+size_t wgrad_smem() {
+    return (size_t)3 * kRowCells * CIN * 2 + (size_t)kTileCols * 64;
+}
+
+template <int CIN, bool BWD>
+cudaError_t launch_conv(const ConvArgs &a, int nf, cudaStream_t st) {
+    const size_t sm = conv_smem<CIN, BWD>();
+    cudaError_t e = cudaFuncSetAttribute(conv_kernel<CIN, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    const unsigned tiles = (unsigned)(a.tiles_x * a.nt * nf);
+    conv_kernel<CIN, BWD><<<tiles, 128, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------ host wrappers
+cudaError_t features(const Fields &fs, int nf, const GridTab &g, bf16 *x, cudaStream_t st) {
+    dim3 grid((g.np + 127) / 128, g.nt, nf);
+    features_kernel<<<grid, 128, 0, st>>>(fs, g, (uint4 *)x);
+    return cudaGetLastError();
+}
+
+cudaError_t conv_forward(int layer, const bf16 *in, const Packed &p, float *y, bf16 *a, int nf, int nt, int np,
+                         cudaStream_t st) {
+    ConvArgs c{};
+    c.in = in;
+    c.yout = y;
+    c.aout = a;
+    c.nt = nt;
+    c.np = np;
+    c.tiles_x = (np + kTileCols - 1) / kTileCols;
+    if (layer == 1) {
+        c.w = p.wf1;
+        c.bias = p.b;
+        return launch_conv<8, false>(c, nf, st);
+    }
+    c.w = layer == 2 ? p.wf2 : p.wf3;
+    c.bias = p.b + 32 * (layer - 1);
+    return launch_conv<32, false>(c, nf, st);
+}
+
+cudaError_t conv_backward_data(int layer, const bf16 *g, const Packed &p, const float *yprev, bf16 *gprev, int nf,
+                               int nt, int np, cudaStream_t st) {
+    ConvArgs c{};
+    c.in = g;
+    c.w = layer == 2 ? p.wb2 : p.wb3;
+    c.yprev = yprev;
+    c.aout = gprev;
+    c.nt = nt;
+    c.np = np;
+    c.tiles_x = (np + kTileCols - 1) / kTileCols;
+    return launch_conv<32, true>(c, nf, st);
+}
+
+cudaError_t conv_backward_weight(int layer, const bf16 *g, const bf16 *x, float *partial, int nblocks, float *grad,
+                                 int nf, int nt, int np, cudaStream_t st) {
+    WgradArgs w{};
+    w.g = g;
+    w.x = x;
+    w.partial = partial;
+    w.nt = nt;
+    w.np = np;
+    w.tiles_x = (np + kTileCols - 1) / kTileCols;
+    w.ntiles = w.tiles_x * nt * nf;
+    const int ci = layer == 1 ? 8 : 32;
+    const int ow = layer == 1 ? SBS_NN_W1 : (layer == 2 ? SBS_NN_W2 : SBS_NN_W3);
+    const int ob = layer == 1 ? SBS_NN_B1 : (layer == 2 ? SBS_NN_B2 : SBS_NN_B3);
+    cudaError_t e;
+    if (ci == 8) {
+        const size_t sm = wgrad_smem<8>();
+        e = cudaFuncSetAttribute(wgrad_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        wgrad_kernel<8><<<nblocks, 128, sm, st>>>(w);
+    } else {
+        const size_t sm = wgrad_smem<32>();
+        e = cudaFuncSetAttribute(wgrad_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        wgrad_kernel<32><<<nblocks, 128, sm, st>>>(w);
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const int ncol = 32 * 9 * ci + 32;
+    reduce_partials_kernel<<<(ncol + 255) / 256, 256, 0, st>>>(partial, nblocks, ci, 32, grad + ow, grad + ob);
+    return cudaGetLastError();
+}
+
+cudaError_t output_layer(const bf16 *a3, const Packed &p, float *y4, const float *target, float *g4,
+                         double *loss_part, float inv_nmask2, const GridTab &g, int nf, cudaStream_t st,
+                         int *nblocks_out) {
+    OutArgs o{};
+    o.a3 = a3;
+    o.w4 = p.w4;
+    o.y4 = y4;
+    o.target = target;
+    o.g4 = g4;
+    o.loss_part = loss_part;
+    o.inv_nmask2 = inv_nmask2;
+    o.g = g;
+    o.nf = nf;
+    o.b4 = p.b + 96;
+    const size_t cells = (size_t)nf * g.nt * g.np;
+    const int nb = (int)((cells + 255) / 256);
+    out_kernel<<<nb, 256, 0, st>>>(o);
+    if (nblocks_out) *nblocks_out = nb;
+    return cudaGetLastError();
+}
+
+cudaError_t output_backward(const float *g4, const bf16 *a3, const float *y3, const Packed &p, bf16 *g3,
+                            float *partial, int nblocks, float *grad, const GridTab &g, int nf, cudaStream_t st) {
+    const size_t cells = (size_t)nf * g.nt * g.np;
+    Wgrad4Args w{};
+    w.g4 = g4;
+    w.a3 = a3;
+    w.partial = partial;
+    w.g = g;
+    w.cells = cells;
+    w.chunk = (cells + nblocks - 1) / nblocks;
+    wgrad4_kernel<<<nblocks, 320, 0, st>>>(w);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    reduce4_kernel<<<2, 256, 0, st>>>(partial, nblocks, grad + SBS_NN_W4, grad + SBS_NN_B4);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    Dgrad4Args d{};
+    d.g4 = g4;
+    d.w4 = p.w4;
+    d.y3 = y3;
+    d.g3 = g3;
+    d.g = g;
+    d.cells = cells;
+    dgrad4_kernel<<<(unsigned)((cells + 7) / 8), 256, 0, st>>>(d);
+    return cudaGetLastError();
+}
+
+cudaError_t adam(float *theta, float *m, float *v, const float *grad, float lr, float b1, float b2, float eps,
+                 int step, cudaStream_t st) {
+    const float c1 = (float)(1.0 / (1.0 - std::pow((double)b1, step)));
+    const float c2 = (float)(1.0 / (1.0 - std::pow((double)b2, step)));
+    adam_kernel<<<(SBS_NN_PARAMS + 255) / 256, 256, 0, st>>>(theta, m, v, grad, SBS_NN_PARAMS, lr, b1, b2, eps, c1,
+                                                             c2);
+    return cudaGetLastError();
+}
+
+cudaError_t pack(const float *theta, const Packed &p, cudaStream_t st) {
+    pack_kernel<<<(32 * 288 + 255) / 256, 256, 0, st>>>(theta, p);
+    return cudaGetLastError();
+}
+
+cudaError_t apply(const float *h, size_t pitch_in, const float *y, float kout, int nt, int np, float *out,
+                  size_t pitch_out, cudaStream_t st) {
+    dim3 grid((np + 127) / 128, nt);
+    apply_kernel<<<grid, 128, 0, st>>>(h, pitch_in, y, kout, nt, np, out, pitch_out);
+    return cudaGetLastError();
+}
+
+cudaError_t targets(const float *const *h0, const float *const *h1, const float *kout, int nf, int nt, int np,
+                    float *target, cudaStream_t st) {
+    TargetArgs t{};
+    for (int b = 0; b < nf; ++b) {
+        t.h0[b] = h0[b];
+        t.h1[b] = h1[b];
+        t.kout[b] = kout[b];
+    }
+    dim3 grid((np + 127) / 128, nt, nf);
+    target_kernel<<<grid, 128, 0, st>>>(t, nt, np, target);
+    return cudaGetLastError();
+}
+
+cudaError_t masked_error(const float *a, size_t pa, const float *b, size_t pb, const GridTab &g, unsigned *out2,
+                         cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(out2, 0, 2 * sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned)std::min(8, (g.np + 255) / 256), g.nt);
+    masked_err_kernel<<<grid, 256, 0, st>>>(a, pa, b, pb, g.rows, g.nt, g.np, out2);
+    return cudaGetLastError();
+}
+
+}  // namespace nn
+}  // namespace sbs

@@ -35,6 +35,10 @@ void clear_error();
 // Makes sure a CUDA device exists and the runtime is usable; fails with SBS_E_CUDA otherwise.
 int require_device();
 
+// WGSL-semantics passes (params.dt each) enqueued on the handle's stream without a final
+// synchronisation (sbs_gpu_drainage_run minus the wait).
+int drainage_run_async(sbs_drainage *h, uint32_t passes);
+
 // ---------------------------------------------------------------------------
 // Drainage kernels
 // ---------------------------------------------------------------------------

@@ -1,0 +1,132 @@
+"""Drainage surrogate on the GPU against the CPU oracle (include/sbs_nn.h restated in oracle/).
+
+Bars: features bit-identical (the same FP32 operations); the network output within 2e-3 of
+max |y| (FP32 tensor-core accumulation order vs double; rare BF16 rounding flips of activations);
+gradients within 3e-2 relative L-inf per layer (the per-layer BF16 gradients amplify those flips).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+LAYERS = [("W1", 0, 2304), ("b1", 2304, 2336), ("W2", 2336, 11552), ("b2", 11552, 11584), ("W3", 11584, 20800),
+          ("b3", 20800, 20832), ("W4", 20832, 21120), ("b4", 21120, 21121)]
+
+
+def fields(nf, nt, np_, seed):
+    from soap_bubble_simulation_gb300 import synthetic as S
+
+    hs, cs = [], []
+    for k in range(nf):
+        hs.append(S.smooth_modes(nt, np_, seed=seed + k))
+        cs.append(S.surfactant_noise(nt, np_, seed=seed + 100 + k))
+    return np.stack(hs).astype(np.float32), np.stack(cs).astype(np.float32)
+
+
+def params_list(sbs, nf, nt, np_, seed):
+    g = np.random.default_rng(seed)
+    return [sbs.field_params(nt, np_, viscosity=float(10 ** g.uniform(-4, -2)),
+                             bubble_radius=float(10 ** g.uniform(np.log10(0.0075), np.log10(0.04))))
+            for _ in range(nf)]
+
+
+def orc_params(orc, p):
+    return orc.wgsl_params(dt=p.dt, gravity=p.gravity, viscosity=p.viscosity, density=p.density,
+                           diffusion_coeff=p.diffusion_coeff, bubble_radius=p.bubble_radius,
+                           grid_width=p.grid_width, grid_height=p.grid_height)
+
+
+@pytest.fixture(scope="module")
+def net(sbs):
+    s = sbs.DrainageSurrogate(seed=11)
+    yield s
+    s.close()
+
+
+@pytest.mark.parametrize("nt,np_", [(32, 64), (20, 200), (64, 128)])
+def test_features_bit_identical(sbs, orc, net, nt, np_):
+    h, c = fields(2, nt, np_, seed=5)
+    ps = params_list(sbs, 2, nt, np_, seed=1)
+    h[0, 3, 7] = np.nan  # non-finite input: clamped on both sides
+    x = net.features(h, c, ps)
+    for b in range(2):
+        want = orc.nn_features(h[b], c[b], orc_params(orc, ps[b]))
+        np.testing.assert_array_equal(x[b], want)
+
+
+@pytest.mark.parametrize("nt,np_,nf", [(16, 32, 2), (24, 160, 1), (64, 256, 3)])
+def test_forward_matches_oracle(sbs, orc, net, nt, np_, nf):
+    h, c = fields(nf, nt, np_, seed=nt)
+    ps = params_list(sbs, nf, nt, np_, seed=nt + 1)
+    theta = net.params
+    y = net.forward(h, c, ps, mode="layered")
+    x = np.stack([orc.nn_features(h[b], c[b], orc_params(orc, ps[b])) for b in range(nf)])
+    want = orc.nn_forward(theta, x)
+    err = np.abs(y - want).max() / np.abs(want).max()
+    assert err <= 2e-3, err
+
+
+def test_gradients_match_oracle(sbs, orc, net):
+    nt, np_, nf = 16, 40, 2
+    h, c = fields(nf, nt, np_, seed=3)
+    ps = params_list(sbs, nf, nt, np_, seed=4)
+    target = np.random.default_rng(9).standard_normal((nf, nt, np_)).astype(np.float32)
+    loss, grad = net.loss_grad(h, c, ps, target)
+    x = np.stack([orc.nn_features(h[b], c[b], orc_params(orc, ps[b])) for b in range(nf)])
+    loss_o, grad_o = orc.nn_loss_grad(net.params, x, target)
+    assert abs(loss - loss_o) <= 1e-3 * loss_o
+    for name, a, b in LAYERS:
+        e = np.abs(grad[a:b] - grad_o[a:b]).max() / np.abs(grad_o[a:b]).max()
+        assert e <= 3e-2, (name, e)
+
+
+def trained_surrogate(sbs, ntraj=24, nt=48, np_=96, iters=300):
+    s = sbs.DrainageSurrogate(seed=3)
+    g = np.random.default_rng(0)
+    from soap_bubble_simulation_gb300 import synthetic as S
+
+    for k in range(ntraj):
+        p = sbs.field_params(nt, np_, viscosity=float(10 ** g.uniform(-4, -2)),
+                             bubble_radius=float(10 ** g.uniform(np.log10(0.0075), np.log10(0.04))))
+        s.add_trajectory(S.smooth_modes(nt, np_, seed=1000 + k), S.surfactant_noise(nt, np_, seed=2000 + k), p,
+                         pairs=3)
+    losses = s.train(ntraj - 4, iters, batch=4, lr=3e-3, seed=1)
+    return s, losses
+
+
+def test_training_beats_identity(sbs):
+    s, losses = trained_surrogate(sbs)
+    assert np.isfinite(losses).all()
+    assert losses[-20:].mean() < 0.2 * losses[:5].mean()
+    ev = s.evaluate(20, 4, mode="layered")
+    # the trained network predicts the 64-pass change: far below the error of doing nothing
+    assert ev["loss"] < 0.1 * ev["loss_identity"], ev
+    assert ev["rel_linf"] < 0.5 * ev["rel_linf_identity"], ev
+    s.close()
+
+
+def test_rollout_checks_and_fallback(sbs):
+    s, _ = trained_surrogate(sbs, ntraj=8, iters=100)
+    from soap_bubble_simulation_gb300 import synthetic as S
+
+    nt, np_ = 48, 96
+    p = sbs.field_params(nt, np_, bubble_radius=0.02)
+    sim = sbs.GPUDrainageSimulator(None, 500e-9, np_, nt)
+    sim.update_params(p)
+    h0, c0 = S.smooth_modes(nt, np_, seed=77), S.surfactant_noise(nt, np_, seed=78)
+    sim.set_thickness_array(h0)
+    sim.set_concentration_array(c0)
+    st = s.rollout(sim, 8 * 64, check_every=2, tol=1e-3, mode="layered")
+    assert st["rollouts"] == 8 and st["checks"] == 4 and st["plain"] == 4 and st["surrogate"] == 4
+    assert st["failed_checks"] == 0 and st["max_check_error"] < 1e-3
+    h_sur = sim.thickness_array()
+    ref = sbs.GPUDrainageSimulator(None, 500e-9, np_, nt)
+    ref.update_params(p)
+    ref.set_thickness_array(h0)
+    ref.set_concentration_array(c0)
+    ref.run(8 * 64)
+    assert sbs.masked_error(h_sur, ref.thickness_array()) < 1e-3
+    # an impossible tolerance: every check fails and the plain solver runs the fallback intervals
+    st = s.rollout(sim, 8 * 64, check_every=4, tol=1e-30, mode="layered")
+    assert st["checks"] == 2 and st["failed_checks"] == 2 and st["plain"] == 8 and st["surrogate"] == 0
+    s.close()
