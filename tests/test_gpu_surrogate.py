@@ -130,3 +130,34 @@ def test_rollout_checks_and_fallback(sbs):
     st = s.rollout(sim, 8 * 64, check_every=4, tol=1e-30, mode="layered")
     assert st["checks"] == 2 and st["failed_checks"] == 2 and st["plain"] == 8 and st["surrogate"] == 0
     s.close()
+
+
+@pytest.mark.parametrize("nt,np_,nf", [(16, 32, 2), (20, 200, 1), (21, 96, 1), (64, 256, 3), (256, 512, 1), (37, 130, 2)])
+def test_fused_forward_matches_oracle(sbs, orc, net, nt, np_, nf):
+    """The fused tcgen05 kernel: narrow grids whose strip wraps, partial strips, several row blocks."""
+    h, c = fields(nf, nt, np_, seed=nt + 7)
+    ps = params_list(sbs, nf, nt, np_, seed=nt + 8)
+    y = net.forward(h, c, ps, mode="fused")
+    x = np.stack([orc.nn_features(h[b], c[b], orc_params(orc, ps[b])) for b in range(nf)])
+    want = orc.nn_forward(net.params, x)
+    err = np.abs(y - want).max() / np.abs(want).max()
+    assert err <= 2e-3, err
+    yl = net.forward(h, c, ps, mode="layered")
+    assert np.abs(y - yl).max() / np.abs(yl).max() <= 2e-3
+
+
+def test_fused_advance_matches_layered(sbs, net):
+    from soap_bubble_simulation_gb300 import synthetic as S
+
+    nt, np_ = 96, 192
+    p = sbs.field_params(nt, np_, bubble_radius=0.02)
+    out = {}
+    for mode in ("layered", "fused"):
+        sim = sbs.GPUDrainageSimulator(None, 500e-9, np_, nt)
+        sim.update_params(p)
+        sim.set_thickness_array(S.smooth_modes(nt, np_, seed=5))
+        sim.set_concentration_array(S.surfactant_noise(nt, np_, seed=6))
+        net.advance(sim, mode=mode)
+        out[mode] = sim.thickness_array()
+    d = np.abs(out["fused"] - out["layered"]).max()
+    assert d <= 1e-12, d  # kout * |dy| ~ 1e-13 m per unit of y
