@@ -428,11 +428,16 @@ int sbs_surrogate_forward(sbs_surrogate *s, uint32_t nf, const float *h, const f
 int sbs_surrogate_loss_grad(sbs_surrogate *s, uint32_t nf, const float *h, const float *c,
                             const sbs_drainage_params *p, const float *target, double *loss, float *grad);
 /* Training data: runs the plain WGSL-semantics solver (the sbs_gpu_drainage
- * kernels) from (h0, c0, host) with parameters p for pairs * SBS_NN_STEPS
- * passes and keeps the pairs + 1 snapshots on the device. Every trajectory of
- * one surrogate has the grid of the first. */
+ * kernels) from (h0, c0, host) with parameters p over pairs intervals of
+ * SBS_NN_STEPS * p->dt and keeps the pairs + 1 snapshots on the device. Each
+ * interval is integrated as SBS_NN_STEPS * substeps passes of p->dt / substeps;
+ * substeps = 0 picks the smallest power of two that keeps every row of the
+ * explicit scheme stable (1 wherever p->dt itself is stable), so that small
+ * bubbles on a coarse grid - the same per-cell diffusion numbers as large
+ * bubbles on a fine grid - give clean targets up to the poles. Every trajectory
+ * of one surrogate has the grid of the first. */
 int sbs_surrogate_add_trajectory(sbs_surrogate *s, const float *h0, const float *c0, const sbs_drainage_params *p,
-                                 uint32_t pairs);
+                                 uint32_t pairs, uint32_t substeps);
 int sbs_surrogate_num_trajectories(const sbs_surrogate *s, uint32_t *out);
 int sbs_surrogate_clear_data(sbs_surrogate *s);
 /* Adam (0.9, 0.999, 1e-8) with a cosine learning-rate decay from lr to lr/20

@@ -9,8 +9,8 @@
  * Map.  h' = h + kout * y  on rows 1 .. nt-2 (then max(., 0)); rows 0 and nt-1
  * are copied (the WGSL kernel freezes the poles).  y is the network output:
  *
- *   x  = features(h, surfactant, viscosity, diameter)           [nt][np][8]
- *   a1 = gelu(conv3x3(x,  W1) + b1)    8 -> 32
+ *   x  = features(h, surfactant, viscosity, diameter)           [nt][np][16]
+ *   a1 = gelu(conv3x3(x,  W1) + b1)   16 -> 32
  *   a2 = gelu(conv3x3(a1, W2) + b2)   32 -> 32
  *   a3 = gelu(conv3x3(a2, W3) + b3)   32 -> 32
  *   y  =      conv3x3(a3, W4) + b4    32 -> 1
@@ -29,15 +29,24 @@
  *   f5 = log10(viscosity / 1e-3)                               log-viscosity
  *   f6 = 3 * log10(diameter / 0.035)                           log-diameter
  *   f7 = (h * h * h) * (gk * sin(theta_i))                     gravity drainage
+ *   f8 = lt                                                    log10 theta diffusion number / MU_REF
+ *   f9 = lp[i]                                                 log10 phi diffusion number / MU_REF
+ *   f10 = sin(theta_i);  f11 .. f15 = 0
  * with dth = pi/(nt-1), dph = 2 pi/np, se_i = max(sin(i dth), SBS_NN_SIN_FLOOR),
  *   ct = 1/(dth^2 S2), cp[i] = 1/(dph^2 se_i^2 S2), cg[i] = cos(i dth)/(se_i 2 dth S2),
  *   gk = -(density gravity / (3 viscosity)) / ((diffusion_coeff / R^2) S2),
- *   kout = SBS_NN_STEPS * dt * (diffusion_coeff / R^2) * S2,  R = bubble_radius,
- * all computed in double and rounded to float.  The geometry-weighted finite
+ *   mu = SBS_NN_STEPS * dt * diffusion_coeff / R^2,  lm = log10(mu / SBS_NN_MU_REF),
+ *   lt = lm + log10(1 / dth^2),  lp[i] = lm + log10(1 / (dph^2 se_i^2))  (each log
+ *   computed in double and rounded to float, the sums in float),
+ *   kout = mu * S2,  R = bubble_radius,
+ * the other constants computed in double and rounded to float.  The geometry-weighted finite
  * differences carry the latitude dependence of the surface Laplacian (a
  * translation-invariant convolution cannot see theta) and keep the curvature
  * of a smooth field, which is below BF16 resolution relative to h itself at
- * fine grids, exact in FP32 before the network sees it.
+ * fine grids, exact in FP32 before the network sees it.  The diffusion numbers
+ * of the SBS_NN_STEPS-pass interval (per cell, in each direction) tell the
+ * network how far the interval spreads a perturbation, which sets the response
+ * independently of the grid resolution.
  *
  * Parameters: one FP32 vector of SBS_NN_PARAMS values, per layer W[tap][oc][ic]
  * then b[oc], tap = (dy + 1) * 3 + (dx + 1) with dy the row (theta) offset and
@@ -55,19 +64,19 @@
  */
 #pragma once
 
-#define SBS_NN_NF 8
+#define SBS_NN_NF 16
 #define SBS_NN_C 32
 #define SBS_NN_STEPS 64
 
 #define SBS_NN_W1 0
-#define SBS_NN_B1 2304
-#define SBS_NN_W2 2336
-#define SBS_NN_B2 11552
-#define SBS_NN_W3 11584
-#define SBS_NN_B3 20800
-#define SBS_NN_W4 20832
-#define SBS_NN_B4 21120
-#define SBS_NN_PARAMS 21121
+#define SBS_NN_B1 4608
+#define SBS_NN_W2 4640
+#define SBS_NN_B2 13856
+#define SBS_NN_W3 13888
+#define SBS_NN_B3 23104
+#define SBS_NN_W4 23136
+#define SBS_NN_B4 23424
+#define SBS_NN_PARAMS 23425
 
 #define SBS_NN_H0 5.5e-7f
 #define SBS_NN_INV_HS 6666666.5f /* float(1 / 150 nm) */
@@ -78,6 +87,7 @@
  * surrogate-versus-plain checks (rows nearer the poles are excluded: at fine
  * grids the explicit scheme is unstable there). */
 #define SBS_NN_MASK_SIN 0.2
+#define SBS_NN_MU_REF 0.044
 
 #define SBS_NN_Q0 0.39817786f
 #define SBS_NN_Q1 (-0.064430825f)

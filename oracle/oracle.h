@@ -159,11 +159,11 @@ void orc_spectral_rgb(const float *t_nm, const float *cos_i, const float *n_film
  * operands (x, weights, activations, and in the backward pass the per-layer output gradients),
  * rounding the layer pre-activations to float where the CUDA path holds them in FP32.
  * Tensors are channel-last: [nb][nt][np][ch]. */
-/* features of one field (nt = grid_height, np = grid_width of p); x: nt*np*8 BF16-valued floats */
+/* features of one field (nt = grid_height, np = grid_width of p); x: nt*np*16 BF16-valued floats */
 void orc_nn_features(const float *h, const float *c, const orc_wgsl_params *p, float *x);
 /* kout of one field (include/sbs_nn.h) */
 float orc_nn_kout(const orc_wgsl_params *p);
-/* forward: y (nb*nt*np) from x (nb*nt*np*8) with the FP32 parameter vector (BF16-rounded inside) */
+/* forward: y (nb*nt*np) from x (nb*nt*np*16) with the FP32 parameter vector (BF16-rounded inside) */
 void orc_nn_forward(const float *params, uint32_t nb, uint32_t nt, uint32_t np, const float *x, float *y);
 /* masked mean-square loss of y against target over rows with sin(theta) >= SBS_NN_MASK_SIN and its
  * gradient (SBS_NN_PARAMS floats). Returns the loss. */

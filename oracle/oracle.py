@@ -348,14 +348,15 @@ def spectral_rgb(t, ci, n, wl, cmf):
 
 
 # ---------------------------------------------------------------- drainage surrogate (include/sbs_nn.h)
-NN_PARAMS = 21121
+NN_PARAMS = 23425
+NN_NF = 16
 
 
 def nn_features(h, c, params: OrcWgslParams) -> np.ndarray:
-    """Features [nt][np][8] (BF16 values held in float32) of one field."""
+    """Features [nt][np][16] (BF16 values held in float32) of one field."""
     h = np.ascontiguousarray(h, dtype=np.float32)
     c = np.ascontiguousarray(c, dtype=np.float32)
-    x = np.empty(h.shape + (8,), dtype=np.float32)
+    x = np.empty(h.shape + (NN_NF,), dtype=np.float32)
     lib().orc_nn_features(_p(h), _p(c), C.byref(params), _p(x))
     return x
 
@@ -365,7 +366,7 @@ def nn_kout(params: OrcWgslParams) -> float:
 
 
 def nn_forward(theta, x) -> np.ndarray:
-    """Network output y [nb][nt][np] for features x [nb][nt][np][8]."""
+    """Network output y [nb][nt][np] for features x [nb][nt][np][16]."""
     theta = np.ascontiguousarray(theta, dtype=np.float32)
     x = np.ascontiguousarray(x, dtype=np.float32)
     nb, nt, np_ = x.shape[:3]

@@ -58,17 +58,21 @@ double gelu_grad_d(double x) {
 
 struct Grid {
     std::vector<float> cp, cg, sg;
+    std::vector<float> lip;  // log10(1 / (dph^2 se^2))
     std::vector<char> mask;
     float ct = 0.f;
+    float lith = 0.f;  // log10(1 / dth^2)
 };
 
 Grid make_grid(uint32_t nt, uint32_t np) {
     Grid g;
     const double dth = M_PI / (double)(nt - 1), dph = 2.0 * M_PI / (double)np, S2 = SBS_NN_S2;
     g.ct = (float)(1.0 / (dth * dth * S2));
+    g.lith = (float)std::log10(1.0 / (dth * dth));
     g.cp.resize(nt);
     g.cg.resize(nt);
     g.sg.resize(nt);
+    g.lip.resize(nt);
     g.mask.resize(nt);
     for (uint32_t i = 0; i < nt; ++i) {
         const double sn = std::sin((double)i * dth), cs = std::cos((double)i * dth);
@@ -76,13 +80,14 @@ Grid make_grid(uint32_t nt, uint32_t np) {
         g.cp[i] = (float)(1.0 / (dph * dph * se * se * S2));
         g.cg[i] = (float)(cs / (se * 2.0 * dth * S2));
         g.sg[i] = (float)sn;
+        g.lip[i] = (float)std::log10(1.0 / (dph * dph * se * se));
         g.mask[i] = (i > 0 && i + 1 < nt && sn >= SBS_NN_MASK_SIN) ? 1 : 0;
     }
     return g;
 }
 
 struct FieldConsts {
-    float gk, f5, f6, kout;
+    float gk, f5, f6, kout, lm;
 };
 
 FieldConsts field_consts(const orc_wgsl_params *p) {
@@ -93,7 +98,9 @@ FieldConsts field_consts(const orc_wgsl_params *p) {
     f.gk = (float)(-coef / (dr2 * S2));
     f.f5 = (float)std::log10((double)p->viscosity / 1e-3);
     f.f6 = (float)(3.0 * std::log10(2.0 * R / 0.035));
-    f.kout = (float)((double)SBS_NN_STEPS * (double)p->dt * dr2 * S2);
+    const double mu = (double)SBS_NN_STEPS * (double)p->dt * dr2;
+    f.kout = (float)(mu * S2);
+    f.lm = (float)std::log10(mu / SBS_NN_MU_REF);
     return f;
 }
 
@@ -247,13 +254,15 @@ void orc_nn_features(const float *h, const float *c, const orc_wgsl_params *p, f
     const uint32_t nt = p->grid_height, np = p->grid_width;
     const Grid g = make_grid(nt, np);
     const FieldConsts f = field_consts(p);
+    const float lt = f.lm + g.lith;
     for (uint32_t i = 0; i < nt; ++i) {
         const float *rn = h + (size_t)refl((int64_t)i - 1, nt) * np, *rs = h + (size_t)refl((int64_t)i + 1, nt) * np;
         const float *rc = h + (size_t)i * np;
         const float grav = f.gk * g.sg[i];
+        const float lp = f.lm + g.lip[i];
         for (uint32_t j = 0; j < np; ++j) {
             const float hc = rc[j], hn = rn[j], hs = rs[j], hw = rc[(j + np - 1) % np], he = rc[(j + 1) % np];
-            float v[8];
+            float v[SBS_NN_NF] = {};
             v[0] = (hc - SBS_NN_H0) * SBS_NN_INV_HS;
             v[1] = ((hn + hs) - (hc + hc)) * g.ct;
             v[2] = ((hw + he) - (hc + hc)) * g.cp[i];
@@ -262,8 +271,11 @@ void orc_nn_features(const float *h, const float *c, const orc_wgsl_params *p, f
             v[5] = f.f5;
             v[6] = f.f6;
             v[7] = ((hc * hc) * hc) * grav;
-            float *o = x + ((size_t)i * np + j) * 8;
-            for (int k = 0; k < 8; ++k) o[k] = bf16r(clampf(v[k]));
+            v[8] = lt;
+            v[9] = lp;
+            v[10] = g.sg[i];
+            float *o = x + ((size_t)i * np + j) * SBS_NN_NF;
+            for (int k = 0; k < SBS_NN_NF; ++k) o[k] = bf16r(clampf(v[k]));
         }
     }
 }

@@ -34,7 +34,7 @@ LOOKUP_GRID = 0
 LOOKUP_TEXEL = 1
 NN_LAYERED = 0
 NN_FUSED = 1
-NN_PARAMS = 21121
+NN_PARAMS = 23425
 NN_STEPS = 64
 
 _ERR_NAMES = {
@@ -198,7 +198,7 @@ SIGNATURES: dict[str, list] = {
     "sbs_surrogate_features": [_P, _U32, _P, _P, _P, _P, _I],
     "sbs_surrogate_forward": [_P, _U32, _P, _P, _P, _P, _I, _I],
     "sbs_surrogate_loss_grad": [_P, _U32, _P, _P, _P, _P, _DP, _P],
-    "sbs_surrogate_add_trajectory": [_P, _P, _P, C.POINTER(SbsDrainageParams), _U32],
+    "sbs_surrogate_add_trajectory": [_P, _P, _P, C.POINTER(SbsDrainageParams), _U32, _U32],
     "sbs_surrogate_num_trajectories": [_P, _U32P],
     "sbs_surrogate_clear_data": [_P],
     "sbs_surrogate_train": [_P, _U32, _U32, _U32, _F, C.c_uint64, _P],

@@ -41,6 +41,19 @@ __device__ __forceinline__ float gelu_grad(float x) {
     return __fmaf_rn(x, dphi, phi);
 }
 
+// Two GELUs with packed FP32x2 arithmetic: the same IEEE round-to-nearest operations as gelu(),
+// so the results are bitwise those of two gelu() calls.
+__device__ __forceinline__ float2 gelu2(float2 x) {
+    const float2 t = make_float2(fminf(fmaxf(x.x, -3.f), 3.f), fminf(fmaxf(x.y, -3.f), 3.f));
+    const float2 u = __fmul2_rn(t, t);
+    float2 p = __ffma2_rn(make_float2(SBS_NN_Q4, SBS_NN_Q4), u, make_float2(SBS_NN_Q3, SBS_NN_Q3));
+    p = __ffma2_rn(p, u, make_float2(SBS_NN_Q2, SBS_NN_Q2));
+    p = __ffma2_rn(p, u, make_float2(SBS_NN_Q1, SBS_NN_Q1));
+    p = __ffma2_rn(p, u, make_float2(SBS_NN_Q0, SBS_NN_Q0));
+    const float2 phi = __ffma2_rn(t, p, make_float2(0.5f, 0.5f));
+    return __fmul2_rn(x, phi);
+}
+
 __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<uint32_t *>(&v);
@@ -56,19 +69,36 @@ struct Field {
     const float *h;
     const float *c;
     size_t pitch;
-    float gk, f5, f6, kout;
+    float gk, f5, f6, kout, lm;
 };
 
 struct Fields {
     Field f[kMaxFields];
 };
 
-// Per-grid row table: cp, cg, sin(theta), loss/check mask (1.0 / 0.0).
+// Per-grid tables: rows[i] = (cp, cg, sin(theta), loss/check mask 1.0 / 0.0), lip[i] =
+// log10(1 / (dph^2 se^2)), lith = log10(1 / dth^2).
 struct GridTab {
     const float4 *rows;
-    float ct;
+    const float *lip;
+    float ct, lith;
     int nt, np;
 };
+
+// Writes the 16 features of one cell (include/sbs_nn.h) as two 16-byte planes.
+__device__ __forceinline__ void cell_features(float hc, float hn, float hs, float hw, float he, float cc, float4 row,
+                                              float lip, const Field &f, const GridTab &g, uint4 &p0, uint4 &p1) {
+    const float h2 = __fadd_rn(hc, hc);
+    p0.x = pack2(clampf(__fmul_rn(__fsub_rn(hc, SBS_NN_H0), SBS_NN_INV_HS)),
+                 clampf(__fmul_rn(__fsub_rn(__fadd_rn(hn, hs), h2), g.ct)));
+    p0.y = pack2(clampf(__fmul_rn(__fsub_rn(__fadd_rn(hw, he), h2), row.x)), clampf(__fmul_rn(__fsub_rn(hs, hn), row.y)));
+    p0.z = pack2(clampf(__fmul_rn(__fsub_rn(cc, 0.5f), 10.f)), clampf(f.f5));
+    p0.w = pack2(clampf(f.f6), clampf(__fmul_rn(__fmul_rn(__fmul_rn(hc, hc), hc), __fmul_rn(f.gk, row.z))));
+    p1.x = pack2(clampf(__fadd_rn(f.lm, g.lith)), clampf(__fadd_rn(f.lm, lip)));
+    p1.y = pack2(clampf(row.z), 0.f);
+    p1.z = 0u;
+    p1.w = 0u;
+}
 
 }  // namespace nn
 }  // namespace sbs

@@ -4,6 +4,10 @@
 //
 // Tiling. A tile is a strip of 128 consecutive phi columns (lanes; the middle 120 are output, the
 // 4 on each side are the halo the four layers consume) times a block of theta rows of one field.
+// The block has four epilogue warpgroups and one MMA warp. Warpgroup l-1 runs layer l's epilogue
+// (all 32 channels of its 128 lanes: read the finished accumulator slot, bias, GELU, write the
+// activation row, zero the slot), warpgroup 3 also computes the features; the four epilogues of a
+// row time run concurrently and signal the MMA warp through named barriers.
 // The block streams its rows top to bottom through all four layers at once, layer l two rows
 // behind layer l-1 ("row time" tau: layer l consumes its input row tau - 2(l-1) and finishes its
 // output row tau - 2l).
@@ -46,20 +50,24 @@ int sms_of(sbs_surrogate *s);
 
 namespace {
 
-constexpr int kLanes = 128;
+constexpr int kLanes = 128;                    // TMEM lanes = cells of a strip
+constexpr int kGroups = 4;                     // warpgroups: each owns one 8-channel plane
+constexpr int kEpi = kLanes * kGroups;         // epilogue threads (16 warps)
+constexpr int kThreads = kEpi + 32;            // + one MMA-issuing warp
 constexpr int kOut = 120;                      // output columns per strip
 constexpr int kHalo = 4;                       // lanes on each side of the outputs
 constexpr int kCells = 136;                    // staged cells per plane (q = lane + 1)
 constexpr uint32_t kPlane = kCells * 16;       // 2176 B
 constexpr uint32_t kRowX = 4 * kPlane;         // one 32-channel row buffer
+constexpr uint32_t kRowX0 = 2 * kPlane;        // one 16-feature row buffer
 constexpr uint32_t kBRows = 160;               // stacked dy ring rows (5 x 32)
 constexpr uint32_t kBChunk = kBRows * 16;      // one 8-channel K chunk
 constexpr uint32_t kBStep = 2 * kBChunk;       // one K16 step
 constexpr uint32_t kB4Rows = 24, kB4Chunk = kB4Rows * 16, kB4Step = 2 * kB4Chunk;
 constexpr uint32_t kBxRows = 24, kBxChunk = kBxRows * 16, kBxStep = 2 * kBxChunk;  // weights at row 2
 // smem image of the packed weights (built once per parameter change by pack_fused_kernel)
-constexpr uint32_t kOffB1 = 0;                          // 2 steps
-constexpr uint32_t kOffB2 = kOffB1 + 2 * kBStep;        // 6 steps
+constexpr uint32_t kOffB1 = 0;                          // 3 steps (dx)
+constexpr uint32_t kOffB2 = kOffB1 + 3 * kBStep;        // 6 steps (dx x 16-channel half)
 constexpr uint32_t kOffB3 = kOffB2 + 6 * kBStep;        // 6 steps
 constexpr uint32_t kOffB4 = kOffB3 + 6 * kBStep;        // 6 steps, 24 rows
 constexpr uint32_t kOffB4t = kOffB4 + 6 * kB4Step;      // W4(dy=-1) alone (top pole extra)
@@ -68,7 +76,7 @@ constexpr uint32_t kOffBias = kOffB4b + 6 * kBxStep;    // 97 floats (padded to 
 constexpr uint32_t kImage = kOffBias + 128 * 4;
 // rest of shared memory
 constexpr uint32_t kOffX0 = (kImage + 1023) / 1024 * 1024;  // 2 feature rows
-constexpr uint32_t kOffX = kOffX0 + 2 * kPlane;             // 3 layers x 2 rows
+constexpr uint32_t kOffX = kOffX0 + 2 * kRowX0;             // 3 layers x 2 rows
 constexpr uint32_t kOffBar = kOffX + 6 * kRowX;
 constexpr uint32_t kSmem = kOffBar + 64;
 __host__ __device__ constexpr uint32_t acc_col(int l) { return 96u * (uint32_t)l; }  // layer l (0-based)
@@ -122,26 +130,6 @@ __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.a
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tld32(uint32_t taddr, uint32_t *v) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
-          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
-          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-        : "r"(taddr));
-}
-
-__device__ __forceinline__ void tzero32(uint32_t taddr) {
-    const uint32_t z = 0;
-    asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, "
-        "%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1};" ::"r"(taddr),
-        "r"(z)
-        : "memory");
-}
-
 __device__ __forceinline__ uint32_t tld1(uint32_t taddr) {
     uint32_t v;
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];" : "=r"(v) : "r"(taddr));
@@ -174,12 +162,125 @@ struct FusedArgs {
     unsigned *err;
 };
 
-__global__ void __launch_bounds__(kLanes, 1) fused_kernel(FusedArgs a) {
+// MMAs of layer l (1-based) for input row s into the layer's accumulator ring (or, for the pole
+// extras, into one slot): issued by one thread.
+// Descriptor of the no-swizzle K-major tile at smem byte address addr (< 256 KB): base | addr >> 4.
+__device__ __forceinline__ uint64_t desc_at(uint64_t base, uint32_t addr) { return base | (uint64_t)(addr >> 4); }
+
+__device__ __forceinline__ void issue_layer(int l, int s, int nt, const int *lo, const int *hi, uint32_t sbase,
+                                            uint32_t tmem) {
+    const int w = mod3(1 - mod3(s));
+    const uint32_t xin = l == 1 ? sbase + kOffX0 + (s & 1) * kRowX0 : sbase + kOffX + ((l - 2) * 2 + (s & 1)) * kRowX;
+    const uint32_t boff = sbase + (l == 1 ? kOffB1 : (l == 2 ? kOffB2 : (l == 3 ? kOffB3 : kOffB4)));
+    const int nsteps = l == 1 ? 3 : 6;
+    const uint32_t dacc = tmem + acc_col(l - 1);
+    const uint64_t da = make_desc(0, kPlane, 128);
+    const uint64_t db = make_desc(0, l < 4 ? kBChunk : kB4Chunk, 128);
+    const uint32_t bstep = l < 4 ? kBStep : kB4Step, woff = l < 4 ? (uint32_t)w * 512u : (uint32_t)w * 16u;
+    const uint32_t id = idesc(l < 4 ? 96 : 16);
+#pragma unroll 1
+    for (int st = 0; st < nsteps; ++st) {
+        const int dxi = l == 1 ? st : st >> 1, kk = l == 1 ? 0 : st & 1;
+        mma(dacc, desc_at(da, xin + 2 * kk * kPlane + 16 * dxi), desc_at(db, boff + st * bstep + woff), id);
+    }
+    // theta reflection: row -1 reads row 1, row nt reads row nt-2
+    const bool top = s == 1 && lo[l] == 0;
+    const bool bot = s == nt - 2 && hi[l] == nt;
+    for (int e = 0; e < 2; ++e) {
+        if (!(e == 0 ? top : bot)) continue;
+        const int orow = e == 0 ? 0 : nt - 1;
+        for (int st = 0; st < nsteps; ++st) {
+            const int dxi = l == 1 ? st : st >> 1, kk = l == 1 ? 0 : st & 1;
+            const uint64_t ad = desc_at(da, xin + 2 * kk * kPlane + 16 * dxi);
+            if (l < 4) {
+                const int blk = e == 0 ? 2 : 0;  // W-1 block / W+1 block of the ring
+                mma(dacc + 32 * mod3(orow), ad, desc_at(db, boff + st * kBStep + blk * 512), idesc(32));
+            } else {
+                // B tile row 2 holds the weights: window start 2 - slot puts them at D column 288 + slot
+                const uint32_t wo = (uint32_t)(2 - mod3(orow)) * 16u;
+                mma(dacc, ad,
+                    desc_at(make_desc(0, kBxChunk, 128), sbase + (e == 0 ? kOffB4t : kOffB4b) + st * kBxStep + wo),
+                    idesc(16));
+            }
+        }
+    }
+}
+
+// Named barrier `id` between one epilogue warpgroup (arrive) and the MMA warp (sync): the epilogue
+// never waits for the MMA warp, the MMA warp waits for the epilogue of its layer. Barrier l (1..4)
+// signals layer l's epilogue, barrier 5 the features.
+constexpr int kNbCount = kLanes + 32;  // one warpgroup + the MMA warp
+__device__ __forceinline__ void nb_arrive(int id) {
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(kNbCount) : "memory");
+}
+__device__ __forceinline__ void nb_sync(int id) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(kNbCount) : "memory"); }
+
+// Inputs of one row's features for one lane, loaded a row ahead of their use.
+struct FeatIn {
+    float hc, hn, hs, hw, he, cc, lip;
+    float4 row;
+};
+
+__device__ __forceinline__ void feat_load(FeatIn &p, int i, int nt, const Field &fd, const GridTab &g, int col, int cw,
+                                          int ce) {
+    const float *rc = fd.h + (size_t)i * fd.pitch;
+    p.row = g.rows[i];
+    p.lip = g.lip[i];
+    p.hc = rc[col];
+    p.hn = fd.h[(size_t)refl_row(i - 1, nt) * fd.pitch + col];
+    p.hs = fd.h[(size_t)refl_row(i + 1, nt) * fd.pitch + col];
+    p.hw = rc[cw];
+    p.he = rc[ce];
+    p.cc = fd.c[(size_t)i * fd.pitch + col];
+}
+
+// The lane's 16 features as two 16-byte planes (include/sbs_nn.h; the same FP32 operations as
+// cell_features).
+__device__ __forceinline__ void feat_store(const FeatIn &p, const Field &fd, const GridTab &g, uint8_t *x0, int lane) {
+    uint4 p0, p1;
+    cell_features(p.hc, p.hn, p.hs, p.hw, p.he, p.cc, p.row, p.lip, fd, g, p0, p1);
+    *reinterpret_cast<uint4 *>(x0 + (lane + 1) * 16) = p0;
+    *reinterpret_cast<uint4 *>(x0 + kPlane + (lane + 1) * 16) = p1;
+}
+
+__device__ __forceinline__ void tld32(uint32_t taddr, uint32_t *v) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+}
+
+__device__ __forceinline__ void tzero32(uint32_t taddr) {
+    const uint32_t z = 0;
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, "
+        "%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1};" ::"r"(taddr),
+        "r"(z)
+        : "memory");
+}
+
+// Bounded wait for the commit of `bar` this thread tracks next; flips its parity bit. Skipped once
+// the block has failed, so a failed block drains quickly.
+__device__ __forceinline__ void wait_commit(uint64_t *bar, int b, uint32_t &phase, volatile int *s_fail, unsigned *err) {
+    if (!*s_fail && !mbar_wait_bounded(smem_u32(bar + b), (phase >> b) & 1u)) {
+        atomicOr(err, 1u);
+        *s_fail = 1;
+    }
+    phase ^= 1u << b;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) fused_kernel(FusedArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kOffBar);  // 4 layer barriers
     uint32_t *s_tmem = reinterpret_cast<uint32_t *>(bar + 4);
     volatile int *s_fail = reinterpret_cast<volatile int *>(s_tmem + 1);
     const int tid = threadIdx.x, warp = tid >> 5;
+    const bool mma_warp = tid >= kEpi;
+    const int grp = tid >> 7, lane = tid & (kLanes - 1);
     const int nt = a.g.nt, np = a.g.np;
 
     if (warp == 0) {
@@ -192,28 +293,30 @@ __global__ void __launch_bounds__(kLanes, 1) fused_kernel(FusedArgs a) {
         *s_fail = 0;
     }
     // weights image and zeroed activation buffers
-    for (uint32_t i = tid * 16; i < kImage; i += kLanes * 16)
+    for (uint32_t i = tid * 16; i < kImage; i += kThreads * 16)
         *reinterpret_cast<uint4 *>(smem + i) = *reinterpret_cast<const uint4 *>(a.image + i);
-    for (uint32_t i = kOffX0 + tid * 16; i < kOffBar; i += kLanes * 16)
+    for (uint32_t i = kOffX0 + tid * 16; i < kOffBar; i += kThreads * 16)
         *reinterpret_cast<uint4 *>(smem + i) = make_uint4(0, 0, 0, 0);
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *s_tmem;
-    const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's lane quarter
-    for (int c = 0; c < 512; c += 32) tzero32(tl + c);
-    wait_st();
+    // an epilogue thread's TMEM lane quarter (warp % 4)
+    const uint32_t tl = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+    if (!mma_warp) {
+        for (int c = 128 * grp; c < 128 * grp + 128; c += 32) tzero32(tl + c);
+        wait_st();
+    }
     const float *bias = reinterpret_cast<const float *>(smem + kOffBias);
     const uint32_t sbase = smem_u32(smem);
-    uint32_t phase = 0;  // bit l: parity of layer l's next commit completion
-    bool ok = true;
+    uint32_t phase = 0;  // bit b: parity of barrier b's next commit completion (per waiting thread)
 
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
 
-    for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x) {
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
         const int strip = tile % a.nstrips;
         const int rb = (tile / a.nstrips) % a.nrb;
         const int f = tile / (a.nstrips * a.nrb);
@@ -224,42 +327,56 @@ __global__ void __launch_bounds__(kLanes, 1) fused_kernel(FusedArgs a) {
             lo[l] = max(0, y0 - 4 + l);
             hi[l] = min(nt, y1 + 4 - l);
         }
-        const int xcol = strip * kOut - kHalo + tid;  // this lane's column (before wrap)
-        const int col = ((xcol % np) + np) % np;
-        const bool lane_out = tid >= kHalo && tid < kHalo + kOut && strip * kOut + (tid - kHalo) < np;
-        const int cw = col == 0 ? np - 1 : col - 1, ce = col + 1 == np ? 0 : col + 1;
-
-        for (int tau = lo[0]; tau <= hi[3] + 8 && ok; ++tau) {
-            // ---- features of row tau into X0[tau & 1]
-            if (tau < hi[0]) {
-                const int i = tau;
-                const float *rc = fd.h + (size_t)i * fd.pitch;
-                const float *rn = fd.h + (size_t)refl_row(i - 1, nt) * fd.pitch;
-                const float *rs = fd.h + (size_t)refl_row(i + 1, nt) * fd.pitch;
-                const float4 row = a.g.rows[i];
-                const float hc = rc[col], hn = rn[col], hs = rs[col], hw = rc[cw], he = rc[ce];
-                const float cc = fd.c[(size_t)i * fd.pitch + col];
-                const float h2 = __fadd_rn(hc, hc);
-                uint4 o;
-                o.x = pack2(clampf(__fmul_rn(__fsub_rn(hc, SBS_NN_H0), SBS_NN_INV_HS)),
-                            clampf(__fmul_rn(__fsub_rn(__fadd_rn(hn, hs), h2), a.g.ct)));
-                o.y = pack2(clampf(__fmul_rn(__fsub_rn(__fadd_rn(hw, he), h2), row.x)),
-                            clampf(__fmul_rn(__fsub_rn(hs, hn), row.y)));
-                o.z = pack2(clampf(__fmul_rn(__fsub_rn(cc, 0.5f), 10.f)), clampf(fd.f5));
-                o.w = pack2(clampf(fd.f6), clampf(__fmul_rn(__fmul_rn(__fmul_rn(hc, hc), hc), __fmul_rn(fd.gk, row.z))));
-                *reinterpret_cast<uint4 *>(smem + kOffX0 + (tau & 1) * kPlane + (tid + 1) * 16) = o;
-            }
-#pragma unroll 1
-            for (int l = 1; l <= 4; ++l) {
-                const int r = tau - 2 * l;          // epilogue row
-                const int s = tau - 2 * l + 2;      // MMA input row
-                const uint32_t bl = smem_u32(bar + (l - 1));
-                if (tau > lo[0]) {
-                    if (!mbar_wait_bounded(bl, (phase >> (l - 1)) & 1u)) {
-                        atomicOr(a.err, 1u);
-                        *s_fail = 1;
+        const int t_end = hi[3] + 8;
+        if (mma_warp) {
+            // ---- MMA warp: per row time, the features, then each layer's MMAs once its warpgroup has
+            //      freed the slot (and the previous layer's warpgroup has written the input row)
+            for (int tau = lo[0]; tau <= t_end; ++tau) {
+                nb_sync(5);
+                for (int l = 1; l <= 4; ++l) {
+                    nb_sync(l);
+                    const int s = tau - 2 * l + 2;
+                    if ((tid & 31) == 0 && !*s_fail) {
+                        tc_fence_after();
+                        if (s >= lo[l - 1] && s < hi[l - 1]) issue_layer(l, s, nt, lo, hi, sbase, tmem);
+                        commit(smem_u32(bar + (l - 1)));
                     }
-                    phase ^= 1u << (l - 1);
+                    __syncwarp();
+                }
+            }
+        } else {
+            const int xcol = strip * kOut - kHalo + lane;  // this lane's column (before wrap)
+            const int col = ((xcol % np) + np) % np;
+            const bool lane_out = lane >= kHalo && lane < kHalo + kOut && strip * kOut + (lane - kHalo) < np;
+            const int cw = col == 0 ? np - 1 : col - 1, ce = col + 1 == np ? 0 : col + 1;
+            const int l = grp + 1;  // this warpgroup's layer
+            FeatIn pre;
+            float hout_next = 0.f, hout_in = 0.f;
+            if (l == 4) {
+                if (lo[0] < hi[0]) feat_load(pre, lo[0], nt, fd, a.g, col, cw, ce);
+                if (lo[0] - 8 >= lo[4] && lo[0] - 8 < hi[4]) hout_next = fd.h[(size_t)(lo[0] - 8) * fd.pitch + col];
+            }
+            for (int tau = lo[0]; tau <= t_end; ++tau) {
+                const int r = tau - 2 * l;  // epilogue row
+                if (l == 4) {
+                    // features of row tau into X0[tau & 1]; its last reader MMA_1(tau - 2) is covered by
+                    // layer 1's commit of row time tau - 1
+                    if (tau > lo[0]) wait_commit(bar, 0, phase, s_fail, a.err);
+                    if (tau < hi[0]) {
+                        feat_store(pre, fd, a.g, smem + kOffX0 + (tau & 1) * kRowX0, lane);
+                        if (tau + 1 < hi[0]) feat_load(pre, tau + 1, nt, fd, a.g, col, cw, ce);
+                    }
+                    fence_async_smem();
+                    nb_arrive(5);
+                    hout_in = hout_next;
+                    const int rn = tau - 7;
+                    if (rn >= lo[4] && rn < hi[4]) hout_next = fd.h[(size_t)rn * fd.pitch + col];
+                }
+                if (tau > lo[0]) {
+                    wait_commit(bar, l - 1, phase, s_fail, a.err);  // this layer's MMAs of tau - 1
+                    // the next layer's MMAs of tau - 1: they, and so MMA_{l+1}(r - 2), are done reading
+                    // the X_l buffer written below
+                    if (l < 4) wait_commit(bar, l, phase, s_fail, a.err);
                     tc_fence_after();
                 }
                 if (r >= lo[l - 1] - 1 && r <= hi[l - 1]) {
@@ -272,31 +389,35 @@ __global__ void __launch_bounds__(kLanes, 1) fused_kernel(FusedArgs a) {
                         wait_ld();
 #pragma unroll
                         for (int k = 0; k < 32; ++k) pin(v[k]);
+                        tzero32(ta);  // completes while the GELUs run (waited below)
                         if (emit) {
                             const float *bl_ = bias + 32 * (l - 1);
-                            uint8_t *dst = smem + kOffX + ((l - 1) * 2 + (r & 1)) * kRowX + (tid + 1) * 16;
+                            uint8_t *dst = smem + kOffX + ((l - 1) * 2 + (r & 1)) * kRowX + (lane + 1) * 16;
 #pragma unroll
-                            for (int p = 0; p < 4; ++p) {
+                            for (int pl = 0; pl < 4; ++pl) {
                                 uint4 o;
                                 uint32_t *ow = reinterpret_cast<uint32_t *>(&o);
 #pragma unroll
                                 for (int e = 0; e < 4; ++e) {
-                                    const int c = p * 8 + 2 * e;
-                                    ow[e] = pack2(gelu(__fadd_rn(__uint_as_float(v[c]), bl_[c])),
-                                                  gelu(__fadd_rn(__uint_as_float(v[c + 1]), bl_[c + 1])));
+                                    const int c = pl * 8 + 2 * e;
+                                    const float2 y = __fadd2_rn(make_float2(__uint_as_float(v[c]), __uint_as_float(v[c + 1])),
+                                                                make_float2(bl_[c], bl_[c + 1]));
+                                    const float2 gy = gelu2(y);
+                                    ow[e] = pack2(gy.x, gy.y);
                                 }
-                                *reinterpret_cast<uint4 *>(dst + p * kPlane) = o;
+                                *reinterpret_cast<uint4 *>(dst + pl * kPlane) = o;
                             }
                         }
-                        tzero32(ta);
+                        wait_st();
                     } else {
                         const uint32_t ta = tl + acc_col(3) + j;
                         uint32_t yv = tld1(ta);
                         wait_ld();
                         pin(yv);
+                        tzero1(ta);
                         const float y = __fadd_rn(__uint_as_float(yv), bias[96]);
                         if (emit && lane_out) {
-                            const float hc = fd.h[(size_t)r * fd.pitch + col];
+                            const float hc = hout_in;
                             if (a.y_out) a.y_out[((size_t)f * nt + r) * np + col] = y;
                             if (a.h_out) {
                                 float o = hc;
@@ -304,104 +425,24 @@ __global__ void __launch_bounds__(kLanes, 1) fused_kernel(FusedArgs a) {
                                 a.h_out[(size_t)r * a.pitch_out + col] = o;
                             }
                         }
-                        tzero1(ta);
+                        wait_st();
                     }
-                    wait_st();
                 }
                 fence_async_smem();
                 tc_fence_before();
-                __syncthreads();
-                if (*s_fail) {
-                    ok = false;
-                    break;
-                }
-                if (tid == 0) {
-                    tc_fence_after();
-                    if (s >= lo[l - 1] && s < hi[l - 1]) {
-                        const int w = mod3(1 - mod3(s));
-                        const uint32_t dacc = tmem + acc_col(l - 1);
-                        if (l == 1) {
-                            const uint32_t xa = sbase + kOffX0 + (s & 1) * kPlane;
-                            for (int st = 0; st < 2; ++st) {
-                                const uint64_t ad = make_desc(xa + 32 * st, 16, 128);
-                                const uint64_t bd = make_desc(sbase + kOffB1 + st * kBStep + w * 512, kBChunk, 128);
-                                mma(dacc, ad, bd, idesc(96));
-                            }
-                        } else {
-                            const uint32_t xa = sbase + kOffX + ((l - 2) * 2 + (s & 1)) * kRowX;
-                            const uint32_t boff = l == 2 ? kOffB2 : (l == 3 ? kOffB3 : kOffB4);
-                            for (int st = 0; st < 6; ++st) {
-                                const int dxi = st >> 1, kk = st & 1;
-                                const uint64_t ad = make_desc(xa + 2 * kk * kPlane + 16 * dxi, kPlane, 128);
-                                if (l < 4) {
-                                    const uint64_t bd =
-                                        make_desc(sbase + boff + st * kBStep + w * 512, kBChunk, 128);
-                                    mma(dacc, ad, bd, idesc(96));
-                                } else {
-                                    const uint64_t bd = make_desc(sbase + boff + st * kB4Step + w * 16, kB4Chunk, 128);
-                                    mma(dacc, ad, bd, idesc(16));
-                                }
-                            }
-                        }
-                        // theta reflection: row -1 reads row 1, row nt reads row nt-2
-                        const bool top = s == 1 && lo[l] == 0;
-                        const bool bot = s == nt - 2 && hi[l] == nt;
-                        for (int e = 0; e < 2; ++e) {
-                            if (!(e == 0 ? top : bot)) continue;
-                            const int orow = e == 0 ? 0 : nt - 1;
-                            const int blk = e == 0 ? 2 : 0;  // W-1 block / W+1 block of the ring
-                            if (l < 4) {
-                                const uint32_t dx = tmem + acc_col(l - 1) + 32 * mod3(orow);
-                                if (l == 1) {
-                                    const uint32_t xa = sbase + kOffX0 + (s & 1) * kPlane;
-                                    for (int st = 0; st < 2; ++st)
-                                        mma(dx, make_desc(xa + 32 * st, 16, 128),
-                                            make_desc(sbase + kOffB1 + st * kBStep + blk * 512, kBChunk, 128),
-                                            idesc(32));
-                                } else {
-                                    const uint32_t xa = sbase + kOffX + ((l - 2) * 2 + (s & 1)) * kRowX;
-                                    const uint32_t boff = l == 2 ? kOffB2 : kOffB3;
-                                    for (int st = 0; st < 6; ++st) {
-                                        const int dxi = st >> 1, kk = st & 1;
-                                        mma(dx, make_desc(xa + 2 * kk * kPlane + 16 * dxi, kPlane, 128),
-                                            make_desc(sbase + boff + st * kBStep + blk * 512, kBChunk, 128),
-                                            idesc(32));
-                                    }
-                                }
-                            } else {
-                                // B tile row 2 holds the weights: window start 2 - slot puts them at
-                                // D column 288 + slot
-                                const uint32_t dx = tmem + acc_col(3);
-                                const uint32_t xa = sbase + kOffX + (4 + (s & 1)) * kRowX;
-                                const uint32_t boff = e == 0 ? kOffB4t : kOffB4b;
-                                const uint32_t wo = (uint32_t)(2 - mod3(orow)) * 16u;
-                                for (int st = 0; st < 6; ++st) {
-                                    const int dxi = st >> 1, kk = st & 1;
-                                    mma(dx, make_desc(xa + 2 * kk * kPlane + 16 * dxi, kPlane, 128),
-                                        make_desc(sbase + boff + st * kBxStep + wo, kBxChunk, 128), idesc(16));
-                                }
-                            }
-                        }
-                    }
-                    commit(bl);
-                }
+                nb_arrive(l);
             }
+            // drain: the commits of the tile's last row time on every barrier this thread tracks
+            if (l == 4) wait_commit(bar, 0, phase, s_fail, a.err);
+            wait_commit(bar, l - 1, phase, s_fail, a.err);
+            if (l < 4) wait_commit(bar, l, phase, s_fail, a.err);
+            tc_fence_after();
         }
-        if (!ok) break;
-        // drain: the commits of the tile's last row time
-        for (int l = 0; l < 4; ++l) {
-            if (!mbar_wait_bounded(smem_u32(bar + l), (phase >> l) & 1u)) {
-                atomicOr(a.err, 1u);
-                *s_fail = 1;
-            }
-            phase ^= 1u << l;
-        }
-        tc_fence_after();
         __syncthreads();
-        if (*s_fail) ok = false;
+        if (*s_fail) break;
     }
-    if (!ok && tid == 0) {
-        for (int l = 0; l < 4; ++l) mbar_wait_bounded(smem_u32(bar + l), (phase >> l) & 1u);
+    if (*s_fail && tid == 0) {
+        for (int l = 0; l < 4; ++l) mbar_wait_bounded(smem_u32(bar + l), 0u), mbar_wait_bounded(smem_u32(bar + l), 1u);
     }
     tc_fence_before();
     __syncthreads();
@@ -414,15 +455,12 @@ __global__ void pack_fused_kernel(const float *theta, uint8_t *img) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     const int dy_of_block[5] = {1, 0, -1, 1, 0};
     bf16 *B = reinterpret_cast<bf16 *>(img);
-    // layers 1-3: element (step, chunk, row n, e8)
-    const int per1 = 2 * 2 * kBRows * 8, per23 = 6 * 2 * kBRows * 8;
+    // layers 1-3: element (step, chunk, row n, e8); layer 1 step = dx, chunk = 8-feature plane
+    const int per1 = 3 * 2 * kBRows * 8, per23 = 6 * 2 * kBRows * 8;
     if (e < per1) {
         const int e8 = e % 8, n = (e / 8) % kBRows, ch = (e / (8 * kBRows)) % 2, st = e / (16 * kBRows);
-        const int dy = dy_of_block[n / 32], oc = n % 32;
-        // step 0: chunk 0 dx=-1, chunk 1 dx=0; step 1: chunk 0 dx=+1, chunk 1 zero
-        const int dx = st == 0 ? (ch == 0 ? -1 : 0) : (ch == 0 ? 1 : 2);
-        float v = 0.f;
-        if (dx <= 1) v = theta[SBS_NN_W1 + (((dy + 1) * 3 + (dx + 1)) * 32 + oc) * 8 + e8];
+        const int dy = dy_of_block[n / 32], oc = n % 32, dx = st - 1;
+        const float v = theta[SBS_NN_W1 + (((dy + 1) * 3 + (dx + 1)) * 32 + oc) * 16 + ch * 8 + e8];
         B[(kOffB1 + st * kBStep + ch * kBChunk) / 2 + n * 8 + e8] = __float2bfloat16_rn(v);
     }
     if (e < per23) {
@@ -538,7 +576,7 @@ int fused_forward(sbs_surrogate *s, const Fields &fields, int nf, const GridTab 
     const int grid = std::min(a.ntiles, sms);
     cudaStream_t stream = stream_of(s);
     SBS_CUDA_TRY(cudaMemsetAsync(st->err, 0, sizeof(unsigned), stream));
-    fused_kernel<<<grid, kLanes, kSmem, stream>>>(a);
+    fused_kernel<<<grid, kThreads, kSmem, stream>>>(a);
     SBS_CUDA_TRY(cudaGetLastError());
     unsigned herr = 0;
     SBS_CUDA_TRY(cudaMemcpyAsync(&herr, st->err, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));

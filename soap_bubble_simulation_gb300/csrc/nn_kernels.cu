@@ -4,7 +4,7 @@
 // gradient reduction, Adam, and weight packing.
 //
 // Layouts (channel-last, cells = fields x nt x np):
-//   features x        BF16 [cells][8]
+//   features x        BF16 [cells][16]
 //   pre-activations y FP32 [cells][32]       activations a BF16 [cells][32]
 //   output y4 / gradient g4 FP32 [cells]     layer gradients g BF16 [cells][32]
 // A convolution tile is one row segment of kTileCols = 128 cells of one field: the block stages
@@ -51,12 +51,14 @@ __device__ __forceinline__ void mma16816(float *d, const uint32_t *a, uint32_t b
 __device__ __forceinline__ int refl_row(int i, int nt) { return i < 0 ? 1 : (i >= nt ? nt - 2 : i); }
 
 // Byte offset of 16-byte channel chunk `ch` of staged cell `q` in a row buffer of cells with CIN
-// channels. 32-channel cells (64 B) are XOR-swizzled so that the 8 rows of an ldmatrix phase
-// fall into distinct bank groups.
+// channels. 16- and 32-channel cells (32 / 64 B) are XOR-swizzled so that the 8 rows of an
+// ldmatrix phase fall into distinct bank groups.
 template <int CIN>
 __device__ __forceinline__ uint32_t cell_off(int q, int ch) {
     if constexpr (CIN == 8) {
         return (uint32_t)q * 16u;
+    } else if constexpr (CIN == 16) {
+        return (uint32_t)q * 32u + ((uint32_t)(ch ^ ((q >> 2) & 1)) << 4);
     } else {
         return (uint32_t)q * 64u + ((uint32_t)(ch ^ ((q >> 1) & 3)) << 4);
     }
@@ -74,26 +76,12 @@ __global__ void features_kernel(Fields fs, GridTab g, uint4 *x) {
     const float *rc = f.h + (size_t)i * f.pitch;
     const float *rn = f.h + (size_t)refl_row(i - 1, nt) * f.pitch;
     const float *rs = f.h + (size_t)refl_row(i + 1, nt) * f.pitch;
-    const float4 row = g.rows[i];
-    const float hc = rc[j], hn = rn[j], hs = rs[j];
-    const float hw = rc[j == 0 ? np - 1 : j - 1], he = rc[j + 1 == np ? 0 : j + 1];
-    const float cc = f.c[(size_t)i * f.pitch + j];
-    const float h2 = __fadd_rn(hc, hc);
-    float v[8];
-    v[0] = __fmul_rn(__fsub_rn(hc, SBS_NN_H0), SBS_NN_INV_HS);
-    v[1] = __fmul_rn(__fsub_rn(__fadd_rn(hn, hs), h2), g.ct);
-    v[2] = __fmul_rn(__fsub_rn(__fadd_rn(hw, he), h2), row.x);
-    v[3] = __fmul_rn(__fsub_rn(hs, hn), row.y);
-    v[4] = __fmul_rn(__fsub_rn(cc, 0.5f), 10.f);
-    v[5] = f.f5;
-    v[6] = f.f6;
-    v[7] = __fmul_rn(__fmul_rn(__fmul_rn(hc, hc), hc), __fmul_rn(f.gk, row.z));
-    uint4 o;
-    o.x = pack2(clampf(v[0]), clampf(v[1]));
-    o.y = pack2(clampf(v[2]), clampf(v[3]));
-    o.z = pack2(clampf(v[4]), clampf(v[5]));
-    o.w = pack2(clampf(v[6]), clampf(v[7]));
-    x[((size_t)b * nt + i) * np + j] = o;
+    uint4 p0, p1;
+    cell_features(rc[j], rn[j], rs[j], rc[j == 0 ? np - 1 : j - 1], rc[j + 1 == np ? 0 : j + 1],
+                  f.c[(size_t)i * f.pitch + j], g.rows[i], g.lip[i], f, g, p0, p1);
+    uint4 *o = x + (((size_t)b * nt + i) * np + j) * 2;
+    o[0] = p0;
+    o[1] = p1;
 }
 
 // ------------------------------------------------------------------ 3x3 convolution (mma.sync)
@@ -546,12 +534,10 @@ __global__ void adam_kernel(float *theta, float *m, float *v, const float *grad,
 // BF16 weight layouts for the layered kernels from the FP32 parameter vector.
 __global__ void pack_kernel(const float *theta, Packed p) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    // forward layouts [oc][tap*CIN+ic], K padded (layer 1: 72 -> 80)
-    if (e < 32 * 80) {
-        const int oc = e / 80, k = e % 80;
-        float v = 0.f;
-        if (k < 72) v = theta[SBS_NN_W1 + ((k / 8) * 32 + oc) * 8 + (k % 8)];
-        p.wf1[e] = __float2bfloat16_rn(v);
+    // forward layouts [oc][tap*CIN+ic]
+    if (e < 32 * 144) {
+        const int oc = e / 144, k = e % 144;
+        p.wf1[e] = __float2bfloat16_rn(theta[SBS_NN_W1 + ((k / 16) * 32 + oc) * 16 + (k % 16)]);
     }
     if (e < 32 * 288) {
         const int n = e / 288, k = e % 288, t = k / 32, r = k % 32;
@@ -663,7 +649,7 @@ cudaError_t conv_forward(int layer, const bf16 *in, const Packed &p, float *y, b
     if (layer == 1) {
         c.w = p.wf1;
         c.bias = p.b;
-        return launch_conv<8, false>(c, nf, st);
+        return launch_conv<16, false>(c, nf, st);
     }
     c.w = layer == 2 ? p.wf2 : p.wf3;
     c.bias = p.b + 32 * (layer - 1);
@@ -693,15 +679,15 @@ cudaError_t conv_backward_weight(int layer, const bf16 *g, const bf16 *x, float 
     w.np = np;
     w.tiles_x = (np + kTileCols - 1) / kTileCols;
     w.ntiles = w.tiles_x * nt * nf;
-    const int ci = layer == 1 ? 8 : 32;
+    const int ci = layer == 1 ? 16 : 32;
     const int ow = layer == 1 ? SBS_NN_W1 : (layer == 2 ? SBS_NN_W2 : SBS_NN_W3);
     const int ob = layer == 1 ? SBS_NN_B1 : (layer == 2 ? SBS_NN_B2 : SBS_NN_B3);
     cudaError_t e;
-    if (ci == 8) {
-        const size_t sm = wgrad_smem<8>();
-        e = cudaFuncSetAttribute(wgrad_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (ci == 16) {
+        const size_t sm = wgrad_smem<16>();
+        e = cudaFuncSetAttribute(wgrad_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
-        wgrad_kernel<8><<<nblocks, 128, sm, st>>>(w);
+        wgrad_kernel<16><<<nblocks, 128, sm, st>>>(w);
     } else {
         const size_t sm = wgrad_smem<32>();
         e = cudaFuncSetAttribute(wgrad_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);

@@ -10,7 +10,7 @@ namespace nn {
 
 // Packed weights derived from the FP32 parameter vector by pack().
 struct Packed {
-    bf16 *wf1;  // [32][80]  layer 1, [oc][tap*8 + ic], K padded 72 -> 80
+    bf16 *wf1;  // [32][144] layer 1, [oc][tap*16 + ic]
     bf16 *wf2;  // [32][288] layer 2 forward  [oc][tap*32 + ic]
     bf16 *wf3;  // [32][288] layer 3 forward
     bf16 *wb2;  // [32][288] layer 2 transpose [ic][tap*32 + oc]

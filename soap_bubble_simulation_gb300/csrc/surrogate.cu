@@ -30,7 +30,7 @@ void fused_release(sbs_surrogate *s);
 namespace {
 
 struct FieldC {
-    float gk, f5, f6, kout;
+    float gk, f5, f6, kout, lm;
 };
 
 // include/sbs_nn.h field scalars, computed in double and rounded once.
@@ -42,16 +42,19 @@ FieldC field_consts(const sbs_drainage_params &p) {
     f.gk = (float)(-coef / (dr2 * S2));
     f.f5 = (float)std::log10((double)p.viscosity / 1e-3);
     f.f6 = (float)(3.0 * std::log10(2.0 * R / 0.035));
-    f.kout = (float)((double)SBS_NN_STEPS * (double)p.dt * dr2 * S2);
+    const double mu = (double)SBS_NN_STEPS * (double)p.dt * dr2;
+    f.kout = (float)(mu * S2);
+    f.lm = (float)std::log10(mu / SBS_NN_MU_REF);
     return f;
 }
 
 struct GridDev {
     float4 *rows = nullptr;
-    float ct = 0.f;
+    float *lip = nullptr;
+    float ct = 0.f, lith = 0.f;
     int nt = 0, np = 0;
     size_t mask_rows = 0;
-    GridTab tab() const { return GridTab{rows, ct, nt, np}; }
+    GridTab tab() const { return GridTab{rows, lip, ct, lith, nt, np}; }
 };
 
 struct Traj {
@@ -137,17 +140,22 @@ int grid_of(sbs_surrogate *s, int nt, int np, const GridDev **out) {
     g.np = np;
     const double dth = M_PI / (double)(nt - 1), dph = 2.0 * M_PI / (double)np, S2 = SBS_NN_S2;
     g.ct = (float)(1.0 / (dth * dth * S2));
+    g.lith = (float)std::log10(1.0 / (dth * dth));
     std::vector<float4> rows(nt);
+    std::vector<float> lip(nt);
     for (int i = 0; i < nt; ++i) {
         const double sn = std::sin((double)i * dth), cs = std::cos((double)i * dth);
         const double se = std::max(sn, SBS_NN_SIN_FLOOR);
         const bool mask = i > 0 && i + 1 < nt && sn >= SBS_NN_MASK_SIN;
         rows[i] = make_float4((float)(1.0 / (dph * dph * se * se * S2)), (float)(cs / (se * 2.0 * dth * S2)), (float)sn,
                               mask ? 1.f : 0.f);
+        lip[i] = (float)std::log10(1.0 / (dph * dph * se * se));
         g.mask_rows += mask ? 1 : 0;
     }
-    SBS_CUDA_TRY(cudaMalloc(&g.rows, sizeof(float4) * nt));
+    SBS_CUDA_TRY(cudaMalloc(&g.rows, sizeof(float4) * nt + sizeof(float) * nt));
+    g.lip = reinterpret_cast<float *>(g.rows + nt);
     SBS_CUDA_TRY(cudaMemcpy(g.rows, rows.data(), sizeof(float4) * nt, cudaMemcpyHostToDevice));
+    SBS_CUDA_TRY(cudaMemcpy(g.lip, lip.data(), sizeof(float) * nt, cudaMemcpyHostToDevice));
     auto res = s->grids.emplace(key, g);
     *out = &res.first->second;
     return SBS_OK;
@@ -159,8 +167,8 @@ int ensure_ws(sbs_surrogate *s, size_t cells) {
     cudaFree(s->ws);
     s->ws = nullptr;
     s->cap = 0;
-    // bytes per cell: x0 16, a1..a3 3*64, g1..g3 3*64, y1..y3 3*128, y4 g4 tgt 12
-    const size_t per = 16 + 6 * 64 + 3 * 128 + 12;
+    // bytes per cell: x0 32, a1..a3 3*64, g1..g3 3*64, y1..y3 3*128, y4 g4 tgt 12
+    const size_t per = 32 + 6 * 64 + 3 * 128 + 12;
     char *p = nullptr;
     SBS_CUDA_TRY(cudaMalloc(&p, per * cells + 1024));
     s->ws = p;
@@ -169,7 +177,7 @@ int ensure_ws(sbs_surrogate *s, size_t cells) {
         p += (bytes + 255) / 256 * 256;
         return r;
     };
-    s->x0 = (bf16 *)take(16 * cells);
+    s->x0 = (bf16 *)take(32 * cells);
     s->a1 = (bf16 *)take(64 * cells);
     s->a2 = (bf16 *)take(64 * cells);
     s->a3 = (bf16 *)take(64 * cells);
@@ -209,7 +217,7 @@ Fields make_fields(const float *h, const float *c, size_t pitch, size_t field_st
     Fields fs{};
     for (int b = 0; b < nf; ++b) {
         const FieldC fc = field_consts(p[b]);
-        fs.f[b] = Field{h + field_stride * b, c + field_stride * b, pitch, fc.gk, fc.f5, fc.f6, fc.kout};
+        fs.f[b] = Field{h + field_stride * b, c + field_stride * b, pitch, fc.gk, fc.f5, fc.f6, fc.kout, fc.lm};
     }
     return fs;
 }
@@ -328,15 +336,15 @@ int sbs_surrogate_create(uint64_t seed, sbs_surrogate **out) {
     s->m = s->theta + SBS_NN_PARAMS;
     s->v = s->m + SBS_NN_PARAMS;
     s->grad = s->v + SBS_NN_PARAMS;
-    // packed weights: wf1 32x80, wf2/wf3/wb2/wb3 32x288 (bf16), w4 288 + b 97 (f32)
-    const size_t pkb = (size_t)2 * (32 * 80 + 4 * 32 * 288) + 4 * (288 + 97) + 256;
+    // packed weights: wf1 32x144, wf2/wf3/wb2/wb3 32x288 (bf16), w4 288 + b 97 (f32)
+    const size_t pkb = (size_t)2 * (32 * 144 + 4 * 32 * 288) + 4 * (288 + 97) + 256;
     const size_t partial_floats = (size_t)s->nblocks * (32 * 9 * 32 + 32);
     char *pm = nullptr;
     if (cudaMalloc(&pm, pkb + sizeof(float) * partial_floats + 64) != cudaSuccess)
         return fail(set_error(SBS_E_NOMEM, "surrogate allocation failed"));
     s->pk_mem = pm;
     s->pk.wf1 = (bf16 *)pm;
-    s->pk.wf2 = s->pk.wf1 + 32 * 80;
+    s->pk.wf2 = s->pk.wf1 + 32 * 144;
     s->pk.wf3 = s->pk.wf2 + 32 * 288;
     s->pk.wb2 = s->pk.wf3 + 32 * 288;
     s->pk.wb3 = s->pk.wb2 + 32 * 288;
@@ -431,7 +439,7 @@ int sbs_surrogate_features(sbs_surrogate *s, uint32_t nf, const float *h, const 
     if ((rc = stage_inputs(s, nf, cells1, h, c, mem, &hd, &cd))) return rc;
     SBS_CUDA_TRY(features(make_fields(hd, cd, np, cells1, p, nf), nf, g->tab(), s->x0, s->stream));
     // BF16 -> f32 on the host side of the copy
-    std::vector<uint16_t> raw(nf * cells1 * 8);
+    std::vector<uint16_t> raw(nf * cells1 * SBS_NN_NF);
     SBS_CUDA_TRY(cudaMemcpyAsync(raw.data(), s->x0, raw.size() * 2, cudaMemcpyDeviceToHost, s->stream));
     SBS_CUDA_TRY(cudaStreamSynchronize(s->stream));
     std::vector<float> xf(raw.size());
@@ -491,13 +499,14 @@ int sbs_surrogate_loss_grad(sbs_surrogate *s, uint32_t nf, const float *h, const
 }
 
 int sbs_surrogate_add_trajectory(sbs_surrogate *s, const float *h0, const float *c0, const sbs_drainage_params *p,
-                                 uint32_t pairs) {
+                                 uint32_t pairs, uint32_t substeps) {
     clear_error();
     CHECK_S(s);
     int rc = check_grid_params(1, p);
     if (rc) return rc;
     SBS_CHECK_ARG(h0 && c0, "null buffer");
     SBS_CHECK_ARG(pairs >= 1 && pairs <= 64, "pairs must be 1..64");
+    SBS_CHECK_ARG(substeps <= 4096, "substeps must be 0 (automatic) .. 4096");
     SBS_CHECK_ARG(p->marangoni_enabled == 0, "the surrogate models marangoni_enabled = 0");
     const int nt = (int)p->grid_height, np = (int)p->grid_width;
     if (s->data.empty()) {
@@ -513,7 +522,19 @@ int sbs_surrogate_add_trajectory(sbs_surrogate *s, const float *h0, const float 
     if (!s->plain) {
         if ((rc = sbs_gpu_drainage_create(500e-9f, (uint32_t)np, (uint32_t)nt, &s->plain))) return rc;
     }
-    if ((rc = sbs_gpu_drainage_update_params(s->plain, p))) return rc;
+    if (substeps == 0) {
+        // largest per-pass diffusion number of the grid (theta + phi at the row nearest a pole, with
+        // the WGSL kernel's sin floor 1e-4) kept at or below 0.2
+        const double dth = M_PI / (double)(nt - 1), dph = 2.0 * M_PI / (double)np;
+        const double s1 = std::max(std::sin(dth), 1e-4);
+        const double mu = (double)p->dt * (double)p->diffusion_coeff / ((double)p->bubble_radius * p->bubble_radius) *
+                          (2.0 / (dth * dth) + 2.0 / (dph * dph * s1 * s1));
+        substeps = 1;
+        while (mu / substeps > 0.2 && substeps < 4096) substeps *= 2;
+    }
+    sbs_drainage_params ps = *p;
+    ps.dt = (float)((double)p->dt / substeps);
+    if ((rc = sbs_gpu_drainage_update_params(s->plain, &ps))) return rc;
     const size_t cells = (size_t)nt * np;
     Traj t;
     t.p = *p;
@@ -532,7 +553,7 @@ int sbs_surrogate_add_trajectory(sbs_surrogate *s, const float *h0, const float 
     if ((rc = sbs_drainage_set_thickness(s->plain, h0, cells, SBS_MEM_HOST))) return fail(rc);
     if ((rc = sbs_drainage_set_concentration(s->plain, c0, cells, SBS_MEM_HOST))) return fail(rc);
     for (uint32_t k = 0; k <= pairs; ++k) {
-        if (k > 0 && (rc = sbs_gpu_drainage_run(s->plain, SBS_NN_STEPS))) return fail(rc);
+        if (k > 0 && (rc = sbs_gpu_drainage_run(s->plain, SBS_NN_STEPS * substeps))) return fail(rc);
         if ((rc = sbs_drainage_get_thickness_field(s->plain, t.h + cells * k, cells, SBS_MEM_DEVICE))) return fail(rc);
         if ((rc = sbs_drainage_get_concentration_field(s->plain, t.c + cells * k, cells, SBS_MEM_DEVICE)))
             return fail(rc);
@@ -587,7 +608,7 @@ int sbs_surrogate_train(sbs_surrogate *s, uint32_t n_train, uint32_t iters, uint
             const auto &pr = pool[splitmix64(st) % pool.size()];
             const Traj &t = s->data[pr.first];
             const float *hp = t.h + cells1 * pr.second, *cp = t.c + cells1 * pr.second;
-            fs.f[b] = Field{hp, cp, (size_t)np, t.fc.gk, t.fc.f5, t.fc.f6, t.fc.kout};
+            fs.f[b] = Field{hp, cp, (size_t)np, t.fc.gk, t.fc.f5, t.fc.f6, t.fc.kout, t.fc.lm};
             h0[b] = hp;
             h1[b] = hp + cells1;
             kout[b] = t.fc.kout;
@@ -633,7 +654,7 @@ int sbs_surrogate_evaluate(sbs_surrogate *s, uint32_t first, uint32_t count, int
         for (uint32_t q = 0; q < t.pairs; ++q) {
             const float *hp = t.h + cells1 * q, *cp = t.c + cells1 * q, *hn = hp + cells1;
             Fields fs{};
-            fs.f[0] = Field{hp, cp, (size_t)np, t.fc.gk, t.fc.f5, t.fc.f6, t.fc.kout};
+            fs.f[0] = Field{hp, cp, (size_t)np, t.fc.gk, t.fc.f5, t.fc.f6, t.fc.kout, t.fc.lm};
             if ((rc = forward_any(s, fs, 1, *g, mode, s->scratch, (size_t)np))) return rc;
             if (mode == SBS_NN_FUSED) {
                 // the fused kernel writes h' directly; y = (h' - h) / kout is not needed for rel_linf, the loss
@@ -731,7 +752,7 @@ int advance_into(sbs_surrogate *s, sbs_drainage *d, int mode, float *into) {
     if (rc) return rc;
     const FieldC fc = field_consts(d->params);
     Fields fs{};
-    fs.f[0] = Field{d->h[d->cur], d->c[d->cur], d->pitch, fc.gk, fc.f5, fc.f6, fc.kout};
+    fs.f[0] = Field{d->h[d->cur], d->c[d->cur], d->pitch, fc.gk, fc.f5, fc.f6, fc.kout, fc.lm};
     // order the handle's queued work before ours
     cudaEvent_t ev;
     SBS_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));

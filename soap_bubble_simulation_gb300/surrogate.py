@@ -103,7 +103,7 @@ class DrainageSurrogate:
     def features(self, h, c, params) -> np.ndarray:
         h, c = _fields(h, c)
         nf = h.shape[0]
-        x = np.empty(h.shape + (8,), dtype=np.float32)
+        x = np.empty(h.shape + (16,), dtype=np.float32)
         N.call("sbs_surrogate_features", self._h, nf, N.ptr(h), N.ptr(c), _param_array(params, nf), N.ptr(x),
                N.MEM_HOST)
         return x
@@ -127,13 +127,13 @@ class DrainageSurrogate:
         return loss.value, g
 
     # ------------------------------------------------------------------ training
-    def add_trajectory(self, h0, c0, params: DrainageParams, pairs: int = 4) -> None:
+    def add_trajectory(self, h0, c0, params: DrainageParams, pairs: int = 4, substeps: int = 0) -> None:
         h0 = np.ascontiguousarray(h0, dtype=np.float32)
         c0 = np.ascontiguousarray(c0, dtype=np.float32)
         if h0.shape != (params.grid_height, params.grid_width) or c0.shape != h0.shape:
             raise ValueError("h0 / c0 must be grid_height x grid_width")
         p = params.to_c()
-        N.call("sbs_surrogate_add_trajectory", self._h, N.ptr(h0), N.ptr(c0), C.byref(p), int(pairs))
+        N.call("sbs_surrogate_add_trajectory", self._h, N.ptr(h0), N.ptr(c0), C.byref(p), int(pairs), int(substeps))
 
     def num_trajectories(self) -> int:
         out = C.c_uint32()

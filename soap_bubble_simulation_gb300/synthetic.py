@@ -44,6 +44,49 @@ def smooth_modes(nt: int, np_: int, seed: int = 1, modes: int = 16, base: float 
     return np.clip(h, lo, hi)
 
 
+def smooth_modes_window(full_nt: int, full_np: int, r0: int, c0: int, nt: int, np_: int, seed: int = 1,
+                        **kw) -> np.ndarray:
+    """Rows r0 .. r0+nt-1 and columns c0 .. c0+np_-1 (mod full_np) of smooth_modes(full_nt, full_np, seed)."""
+    g = rng(seed)
+    modes = kw.get("modes", 16)
+    a = g.normal(0.0, kw.get("amp", 60e-9), size=modes)
+    m = g.integers(1, 9, size=modes)
+    n = g.integers(0, 9, size=modes)
+    psi = g.uniform(0.0, 2 * math.pi, size=modes)
+    chi = g.uniform(0.0, 2 * math.pi, size=modes)
+    theta = (r0 + np.arange(nt)) * (math.pi / (full_nt - 1))
+    phi = ((c0 + np.arange(np_)) % full_np) * (2 * math.pi / full_np)
+    U = a[None, :] * np.cos(m[None, :] * theta[:, None] + psi[None, :])
+    V = np.cos(n[None, :] * phi[:, None] + chi[None, :])
+    h = kw.get("base", 550e-9) + U @ V.T
+    return np.clip(h, kw.get("lo", 100e-9), kw.get("hi", 1000e-9))
+
+
+def surrogate_trajectories(count: int = 512, seed: int = 21, resolution: int = 256, fine: int = 2048):
+    """Initial states of the surrogate's training trajectories on a resolution x 2 resolution grid.
+
+    Even k: a config-1 field at `resolution` (bubble_c1). Odd k: a resolution x 2 resolution window
+    of a config-1 field at `fine` (the cell-scale content - kinks where the clamp to [100, 1000] nm
+    bites, nearly flat smooth modes - that a `fine` field shows the network). Viscosity is
+    log-uniform in [1e-4, 1e-2] Pa s and the diameter log-uniform in [3, 80] mm; the small end gives,
+    at `resolution`, the per-cell diffusion numbers of 25-40 mm bubbles at `fine`.
+    Yields (h f32, c f32, viscosity, radius)."""
+    g = rng(seed)
+    nt, np_ = resolution, 2 * resolution
+    for k in range(count):
+        visc = float(10 ** g.uniform(-4.0, -2.0))
+        radius = float(0.5 * 10 ** g.uniform(math.log10(0.003), math.log10(0.08)))
+        s = int(g.integers(0, 2**31 - 1))
+        if k % 2 == 0:
+            h = smooth_modes(nt, np_, seed=s).astype(np.float32)
+        else:
+            r0 = int(g.integers(0, fine - nt + 1))
+            c0 = int(g.integers(0, 2 * fine))
+            h = smooth_modes_window(fine, 2 * fine, r0, c0, nt, np_, seed=s).astype(np.float32)
+        c = surfactant_noise(nt, np_, seed=s + 1)
+        yield h, c, visc, radius
+
+
 def surfactant_noise(nt: int, np_: int, seed: int = 2, mean: float = 0.5, spread: float = 0.1) -> np.ndarray:
     g = rng(seed)
     return (mean + g.uniform(-spread, spread, size=(nt, np_))).astype(np.float32)

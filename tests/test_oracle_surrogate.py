@@ -59,7 +59,15 @@ def test_features_match_closed_form_derivatives(orc):
     want7 = gk * np.sin(th) * h.astype(np.float64) ** 3
     assert np.abs(x[:, :, 7] - want7).max() < 1e-2 * np.abs(want7).max()
     kout = orc.nn_kout(p)
-    assert abs(kout - 64 * 1e-3 * 1e-9 / R**2 * S2) < 1e-6 * kout
+    mu = 64 * 1e-3 * 1e-9 / R**2
+    assert abs(kout - mu * S2) < 1e-6 * kout
+    # diffusion numbers of the 64-pass interval and the latitude
+    dth, dph = np.pi / (nt - 1), 2 * np.pi / np_
+    assert np.allclose(x[:, :, 8], np.log10(mu / dth**2 / 0.044), atol=2e-2)
+    se = np.maximum(np.sin(th), 0.05)
+    assert np.allclose(x[:, :, 9], np.log10(mu / (dph**2 * se**2) / 0.044) + 0 * ph, atol=2e-2)
+    assert np.allclose(x[:, :, 10], np.sin(th) + 0 * ph, atol=4e-3)
+    assert (x[:, :, 11:] == 0).all()
 
 
 def test_features_are_finite_for_nonfinite_input(orc):
@@ -75,14 +83,14 @@ def test_features_are_finite_for_nonfinite_input(orc):
 def test_backward_matches_finite_differences(orc, nb, nt, np_):
     g = np.random.default_rng(nb * 100 + nt)
     theta = (0.08 * g.standard_normal(orc.NN_PARAMS)).astype(np.float32)
-    x = g.standard_normal((nb, nt, np_, 8)).astype(np.float32)
+    x = g.standard_normal((nb, nt, np_, 16)).astype(np.float32)
     target = g.standard_normal((nb, nt, np_)).astype(np.float32)
     orc.nn_set_exact(True)
     try:
         loss, grad = orc.nn_loss_grad(theta, x, target)
         # parameters in every layer: weights at the reflected (dy = -1 / +1) and periodic taps, biases
-        idx = np.concatenate([g.integers(0, 2304, 6), [2304, 2335], g.integers(2336, 11552, 6), [11552],
-                              g.integers(11584, 20800, 6), [20800], g.integers(20832, 21120, 6), [21120]])
+        idx = np.concatenate([g.integers(0, 4608, 6), [4608, 4639], g.integers(4640, 13856, 6), [13856],
+                              g.integers(13888, 23104, 6), [23104], g.integers(23136, 23424, 6), [23424]])
         for k in idx:
             eps = 1e-5
             tp, tm = theta.copy(), theta.copy()
