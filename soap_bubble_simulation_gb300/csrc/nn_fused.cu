@@ -4,13 +4,15 @@
 //
 // Tiling. A tile is a strip of 128 consecutive phi columns (lanes; the middle 120 are output, the
 // 4 on each side are the halo the four layers consume) times a block of theta rows of one field.
-// The block has four epilogue warpgroups and one MMA warp. Warpgroup l-1 runs layer l's epilogue
-// (all 32 channels of its 128 lanes: read the finished accumulator slot, bias, GELU, write the
-// activation row, zero the slot), warpgroup 3 also computes the features; the four epilogues of a
-// row time run concurrently and signal the MMA warp through named barriers.
-// The block streams its rows top to bottom through all four layers at once, layer l two rows
-// behind layer l-1 ("row time" tau: layer l consumes its input row tau - 2(l-1) and finishes its
-// output row tau - 2l).
+// The block runs eight agents that only talk through mbarriers: four MMA warps (one per layer:
+// for each input row, wait for the row and for the accumulator slot it starts, issue, commit) and
+// four epilogue warpgroups (warpgroup l-1 reads layer l's finished row from TMEM, zeroes the slot,
+// adds the bias, applies GELU and writes the activation row into one of three input buffers of layer
+// l+1; warpgroup 3 writes the features and the thickness update). Every ring (activation buffers:
+// full / empty; accumulator rows: full / empty, and a per-tile barrier for the last three rows) is
+// balanced per tile, so each waiter is at most one phase behind and parity waits are exact.
+// The block streams its rows top to bottom through all four layers at once, each layer as far
+// behind the one before as its inputs require.
 //
 // Convolution as MMAs. Activations of one row live in shared memory as planes of 8 channels with
 // 16 B per cell (K-major, rows of the A operand = cells, SBO = 128 B), so the dx = -1/0/+1 taps
@@ -53,33 +55,41 @@ namespace {
 constexpr int kLanes = 128;                    // TMEM lanes = cells of a strip
 constexpr int kGroups = 4;                     // warpgroups: each owns one 8-channel plane
 constexpr int kEpi = kLanes * kGroups;         // epilogue threads (16 warps)
-constexpr int kThreads = kEpi + 32;            // + one MMA-issuing warp
+constexpr int kThreads = kEpi + 4 * 32;        // + one MMA-issuing warp per layer
 constexpr int kOut = 120;                      // output columns per strip
 constexpr int kHalo = 4;                       // lanes on each side of the outputs
 constexpr int kCells = 136;                    // staged cells per plane (q = lane + 1)
 constexpr uint32_t kPlane = kCells * 16;       // 2176 B
 constexpr uint32_t kRowX = 4 * kPlane;         // one 32-channel row buffer
 constexpr uint32_t kRowX0 = 2 * kPlane;        // one 16-feature row buffer
-constexpr uint32_t kBRows = 160;               // stacked dy ring rows (5 x 32)
+constexpr uint32_t kBRows = 96;                // dy blocks [W+1; W0; W-1] (3 x 32 rows)
 constexpr uint32_t kBChunk = kBRows * 16;      // one 8-channel K chunk
 constexpr uint32_t kBStep = 2 * kBChunk;       // one K16 step
-constexpr uint32_t kB4Rows = 24, kB4Chunk = kB4Rows * 16, kB4Step = 2 * kB4Chunk;
-constexpr uint32_t kBxRows = 24, kBxChunk = kBxRows * 16, kBxStep = 2 * kBxChunk;  // weights at row 2
+constexpr uint32_t kBlk = 32 * 16;             // one 32-row block
+constexpr uint32_t kB4Rows = 40, kB4Chunk = kB4Rows * 16, kB4Step = 2 * kB4Chunk;  // W4 at rows 15, 16, 17
+constexpr uint32_t kBxRows = 32, kBxChunk = kBxRows * 16, kBxStep = 2 * kBxChunk;  // one W4 block at row 15
 // smem image of the packed weights (built once per parameter change by pack_fused_kernel)
 constexpr uint32_t kOffB1 = 0;                          // 3 steps (dx)
 constexpr uint32_t kOffB2 = kOffB1 + 3 * kBStep;        // 6 steps (dx x 16-channel half)
 constexpr uint32_t kOffB3 = kOffB2 + 6 * kBStep;        // 6 steps
-constexpr uint32_t kOffB4 = kOffB3 + 6 * kBStep;        // 6 steps, 24 rows
+constexpr uint32_t kOffB4 = kOffB3 + 6 * kBStep;        // 6 steps, 40 rows
 constexpr uint32_t kOffB4t = kOffB4 + 6 * kB4Step;      // W4(dy=-1) alone (top pole extra)
 constexpr uint32_t kOffB4b = kOffB4t + 6 * kBxStep;     // W4(dy=+1) alone (bottom pole extra)
 constexpr uint32_t kOffBias = kOffB4b + 6 * kBxStep;    // 97 floats (padded to 128)
 constexpr uint32_t kImage = kOffBias + 128 * 4;
+// accumulator rings: layers 1-3 keep kDepth rows of 32 columns, layer 4 kDepth4 single columns
+constexpr int kDepth = 4, kDepth4 = 16;
+__host__ __device__ constexpr int depth_of(int l) { return l < 4 ? kDepth : kDepth4; }  // l 1-based
+__host__ __device__ constexpr uint32_t acc_col(int l) { return 128u * (uint32_t)l; }    // l 0-based; 3 -> 384
 // rest of shared memory
-constexpr uint32_t kOffX0 = (kImage + 1023) / 1024 * 1024;  // 2 feature rows
-constexpr uint32_t kOffX = kOffX0 + 2 * kRowX0;             // 3 layers x 2 rows
-constexpr uint32_t kOffBar = kOffX + 6 * kRowX;
-constexpr uint32_t kSmem = kOffBar + 64;
-__host__ __device__ constexpr uint32_t acc_col(int l) { return 96u * (uint32_t)l; }  // layer l (0-based)
+constexpr int kNBuf = 3;                                   // activation rows in flight per layer input
+constexpr uint32_t kOffX0 = (kImage + 1023) / 1024 * 1024;  // feature rows
+constexpr uint32_t kOffX = kOffX0 + kNBuf * kRowX0;         // 3 layers x kNBuf rows
+constexpr uint32_t kOffBar = kOffX + 3 * kNBuf * kRowX;
+// barriers of layer l: xfull[kNBuf], xempty[kNBuf], afull[depth], aempty[depth]
+__host__ __device__ constexpr int bar_base(int l) { return (l - 1) * (2 * kNBuf + 2 * kDepth); }
+constexpr int kNumBars = 3 * (2 * kNBuf + 2 * kDepth) + 2 * kNBuf + 2 * kDepth4;
+constexpr uint32_t kSmem = kOffBar + 8 * (kNumBars + 1) + 64;  // + the exit drain barrier
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at 2 GHz
 
 __host__ __device__ constexpr uint32_t idesc(int n) {
@@ -102,6 +112,14 @@ __device__ __forceinline__ void mma(uint32_t dtmem, uint64_t a, uint64_t b, uint
         "{\n .reg .pred p;\n setp.ne.b32 p, 1, 0;\n"
         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
         "l"(a), "l"(b), "r"(id));
+}
+
+// One lane of a converged warp (the elected issuer of tensor-core instructions).
+__device__ __forceinline__ bool elect_one() {
+    uint32_t pred = 0;
+    asm volatile("{\n .reg .pred P;\n .reg .b32 L;\n elect.sync L|P, 0xffffffff;\n selp.b32 %0, 1, 0, P;\n}\n"
+                 : "=r"(pred));
+    return pred != 0;
 }
 
 __device__ __forceinline__ void commit(uint32_t bar) {
@@ -148,7 +166,6 @@ __device__ __forceinline__ void wait_ld() { asm volatile("tcgen05.wait::ld.sync.
 __device__ __forceinline__ void pin(uint32_t &r) { asm volatile("" : "+r"(r)); }
 __device__ __forceinline__ void wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
-__device__ __forceinline__ int mod3(int r) { return ((r % 3) + 3) % 3; }
 __device__ __forceinline__ int refl_row(int i, int nt) { return i < 0 ? 1 : (i >= nt ? nt - 2 : i); }
 
 struct FusedArgs {
@@ -167,53 +184,83 @@ struct FusedArgs {
 // Descriptor of the no-swizzle K-major tile at smem byte address addr (< 256 KB): base | addr >> 4.
 __device__ __forceinline__ uint64_t desc_at(uint64_t base, uint32_t addr) { return base | (uint64_t)(addr >> 4); }
 
-__device__ __forceinline__ void issue_layer(int l, int s, int nt, const int *lo, const int *hi, uint32_t sbase,
-                                            uint32_t tmem) {
-    const int w = mod3(1 - mod3(s));
-    const uint32_t xin = l == 1 ? sbase + kOffX0 + (s & 1) * kRowX0 : sbase + kOffX + ((l - 2) * 2 + (s & 1)) * kRowX;
-    const uint32_t boff = sbase + (l == 1 ? kOffB1 : (l == 2 ? kOffB2 : (l == 3 ? kOffB3 : kOffB4)));
-    const int nsteps = l == 1 ? 3 : 6;
-    const uint32_t dacc = tmem + acc_col(l - 1);
-    const uint64_t da = make_desc(0, kPlane, 128);
-    const uint64_t db = make_desc(0, l < 4 ? kBChunk : kB4Chunk, 128);
-    const uint32_t bstep = l < 4 ? kBStep : kB4Step, woff = l < 4 ? (uint32_t)w * 512u : (uint32_t)w * 16u;
-    const uint32_t id = idesc(l < 4 ? 96 : 16);
-#pragma unroll 1
-    for (int st = 0; st < nsteps; ++st) {
-        const int dxi = l == 1 ? st : st >> 1, kk = l == 1 ? 0 : st & 1;
-        mma(dacc, desc_at(da, xin + 2 * kk * kPlane + 16 * dxi), desc_at(db, boff + st * bstep + woff), id);
-    }
-    // theta reflection: row -1 reads row 1, row nt reads row nt-2
-    const bool top = s == 1 && lo[l] == 0;
-    const bool bot = s == nt - 2 && hi[l] == nt;
-    for (int e = 0; e < 2; ++e) {
-        if (!(e == 0 ? top : bot)) continue;
-        const int orow = e == 0 ? 0 : nt - 1;
-        for (int st = 0; st < nsteps; ++st) {
-            const int dxi = l == 1 ? st : st >> 1, kk = l == 1 ? 0 : st & 1;
-            const uint64_t ad = desc_at(da, xin + 2 * kk * kPlane + 16 * dxi);
-            if (l < 4) {
-                const int blk = e == 0 ? 2 : 0;  // W-1 block / W+1 block of the ring
-                mma(dacc + 32 * mod3(orow), ad, desc_at(db, boff + st * kBStep + blk * 512), idesc(32));
-            } else {
-                // B tile row 2 holds the weights: window start 2 - slot puts them at D column 288 + slot
-                const uint32_t wo = (uint32_t)(2 - mod3(orow)) * 16u;
-                mma(dacc, ad,
-                    desc_at(make_desc(0, kBxChunk, 128), sbase + (e == 0 ? kOffB4t : kOffB4b) + st * kBxStep + wo),
-                    idesc(16));
+// MMAs of layer L (1-based) for one input row, fully unrolled: ad0 / bd0 are the descriptors of
+// the row's activation buffer and of the layer's B tile, the per-step offsets are compile-time
+// (descriptor address fields count 16-byte units). c = ring slot of output row s-1.
+// Operands of one input row of layer L (computed by the whole warp from warp-uniform values, so
+// they stay in uniform registers), then the MMAs back to back from one elected lane.
+template <int L>
+struct RowOps {
+    static constexpr int NS = L == 1 ? 3 : 6;
+    uint64_t ad[NS], b1[NS], b2[NS];
+    uint32_t d1, d2, i1, i2;
+    bool two;
+    __device__ __forceinline__ RowOps(uint32_t dacc, uint64_t ad0, uint64_t bd0, int c) {
+        if constexpr (L < 4) {
+            two = c > kDepth - 3;
+            d1 = dacc + 32 * c;
+            d2 = dacc;
+            i1 = c <= kDepth - 3 ? idesc(96) : (c == kDepth - 2 ? idesc(64) : idesc(32));
+            i2 = c == kDepth - 2 ? idesc(32) : idesc(64);
+            const uint64_t o2 = c == kDepth - 2 ? (2 * kBlk >> 4) : (kBlk >> 4);
+#pragma unroll
+            for (int st = 0; st < NS; ++st) {
+                const int dxi = L == 1 ? st : st >> 1, kk = L == 1 ? 0 : st & 1;
+                ad[st] = ad0 + (uint64_t)((2 * kk * kPlane + 16 * dxi) >> 4);
+                b1[st] = bd0 + (uint64_t)((st * kBStep) >> 4);
+                b2[st] = b1[st] + o2;
+            }
+        } else {
+            // B rows 15..17 hold W4(dy = +1, 0, -1): window start 15 - c puts them at columns c..c+2;
+            // the part past the last slot wraps to column 0 through a second window
+            two = c >= kDepth4 - 2;
+            d1 = d2 = dacc;
+            i1 = i2 = idesc(16);
+#pragma unroll
+            for (int st = 0; st < NS; ++st) {
+                const int dxi = st >> 1, kk = st & 1;
+                ad[st] = ad0 + (uint64_t)((2 * kk * kPlane + 16 * dxi) >> 4);
+                b1[st] = bd0 + (uint64_t)((st * kB4Step) >> 4) + (uint64_t)(15 - c);
+                b2[st] = bd0 + (uint64_t)((st * kB4Step) >> 4) + (uint64_t)(31 - c);
             }
         }
     }
-}
+    __device__ __forceinline__ void issue() const {
+        if (!two) {
+#pragma unroll
+            for (int st = 0; st < NS; ++st) mma(d1, ad[st], b1[st], i1);
+        } else {
+#pragma unroll
+            for (int st = 0; st < NS; ++st) {
+                mma(d1, ad[st], b1[st], i1);
+                mma(d2, ad[st], b2[st], i2);
+            }
+        }
+    }
+};
 
-// Named barrier `id` between one epilogue warpgroup (arrive) and the MMA warp (sync): the epilogue
-// never waits for the MMA warp, the MMA warp waits for the epilogue of its layer. Barrier l (1..4)
-// signals layer l's epilogue, barrier 5 the features.
-constexpr int kNbCount = kLanes + 32;  // one warpgroup + the MMA warp
-__device__ __forceinline__ void nb_arrive(int id) {
-    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(kNbCount) : "memory");
+// theta-reflection extra MMAs of layer L: input row 1 into output row 0 with W(dy=-1) (top) or input
+// row nt-2 into output row nt-1 with W(dy=+1) (bottom), oslot = that output row's ring slot.
+template <int L>
+__device__ __forceinline__ void issue_pole(uint32_t dacc, uint64_t ad0, uint32_t sbase, bool top, int oslot) {
+    constexpr int NS = L == 1 ? 3 : 6;
+    const uint32_t boff = sbase + (L == 1 ? kOffB1 : (L == 2 ? kOffB2 : (L == 3 ? kOffB3 : 0u)));
+#pragma unroll
+    for (int st = 0; st < NS; ++st) {
+        const int dxi = L == 1 ? st : st >> 1, kk = L == 1 ? 0 : st & 1;
+        const uint64_t ad = ad0 + (uint64_t)((2 * kk * kPlane + 16 * dxi) >> 4);
+        if constexpr (L < 4) {
+            const uint32_t blk = top ? 2 * kBlk : 0;  // W-1 block / W+1 block
+            mma(dacc + 32 * oslot, ad, desc_at(make_desc(0, kBChunk, 128), boff + st * kBStep + blk), idesc(32));
+        } else {
+            // B tile row 15 holds the weights: window start 15 - slot puts them at D column 384 + slot
+            mma(dacc, ad,
+                desc_at(make_desc(0, kBxChunk, 128),
+                        sbase + (top ? kOffB4t : kOffB4b) + st * kBxStep + (uint32_t)(15 - oslot) * 16u),
+                idesc(16));
+        }
+    }
 }
-__device__ __forceinline__ void nb_sync(int id) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(kNbCount) : "memory"); }
 
 // Inputs of one row's features for one lane, loaded a row ahead of their use.
 struct FeatIn {
@@ -263,32 +310,71 @@ __device__ __forceinline__ void tzero32(uint32_t taddr) {
         : "memory");
 }
 
-// Bounded wait for the commit of `bar` this thread tracks next; flips its parity bit. Skipped once
-// the block has failed, so a failed block drains quickly.
-__device__ __forceinline__ void wait_commit(uint64_t *bar, int b, uint32_t &phase, volatile int *s_fail, unsigned *err) {
-    if (!*s_fail && !mbar_wait_bounded(smem_u32(bar + b), (phase >> b) & 1u)) {
-        atomicOr(err, 1u);
-        *s_fail = 1;
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// Per-thread phase tracking of one barrier: waits for completion number `count` (0, 1, ...).
+struct Waiter {
+    volatile int *fail;
+    unsigned *err;
+    __device__ __forceinline__ void wait(uint32_t bar, uint32_t count) {
+        if (*fail) return;
+        if (!mbar_wait_bounded(bar, count & 1u)) {
+            atomicOr(err, 1u);
+            *fail = 1;
+        }
     }
-    phase ^= 1u << b;
+};
+
+__device__ __forceinline__ void tile_rows(const FusedArgs &a, int tile, int *lo, int *hi, int &strip, int &f) {
+    strip = tile % a.nstrips;
+    const int rb = (tile / a.nstrips) % a.nrb;
+    f = tile / (a.nstrips * a.nrb);
+    const int y0 = rb * a.rows_per_block, y1 = min(a.g.nt, y0 + a.rows_per_block);
+    for (int l = 0; l <= 4; ++l) {
+        lo[l] = max(0, y0 - 4 + l);
+        hi[l] = min(a.g.nt, y1 + 4 - l);
+    }
 }
 
 __global__ void __launch_bounds__(kThreads, 1) fused_kernel(FusedArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kOffBar);  // 4 layer barriers
-    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(bar + 4);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kOffBar);
+    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(bar + kNumBars + 1);
+    const uint32_t drain = smem_u32(bar + kNumBars);  // every MMA warp's final commit (4 arrivals)
     volatile int *s_fail = reinterpret_cast<volatile int *>(s_tmem + 1);
     const int tid = threadIdx.x, warp = tid >> 5;
-    const bool mma_warp = tid >= kEpi;
     const int grp = tid >> 7, lane = tid & (kLanes - 1);
     const int nt = a.g.nt, np = a.g.np;
+    const uint32_t sbase = smem_u32(smem);
+    // barriers of layer l (1-based): input-row buffers of layer l (full: written by the producer
+    // warpgroup, empty: released by layer l's MMAs) and accumulator ring slots (full: the slot's row
+    // has all its contributions, empty: its epilogue has read and zeroed it)
+    auto xfull = [&](int l, int b) { return smem_u32(bar + bar_base(l) + b); };
+    auto xempty = [&](int l, int b) { return smem_u32(bar + bar_base(l) + kNBuf + b); };
+    auto afull = [&](int l, int j) { return smem_u32(bar + bar_base(l) + 2 * kNBuf + j); };
+    auto aempty = [&](int l, int j) { return smem_u32(bar + bar_base(l) + 2 * kNBuf + depth_of(l) + j); };
+    auto xbuf = [&](int l, int b) {  // input row buffer b of layer l
+        return l == 1 ? kOffX0 + (uint32_t)b * kRowX0 : kOffX + ((uint32_t)(l - 2) * kNBuf + b) * kRowX;
+    };
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(s_tmem)));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        for (int l = 0; l < 4; ++l) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar + l)));
+        for (int l = 1; l <= 4; ++l) {
+            for (int b = 0; b < kNBuf; ++b) {
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(xfull(l, b)), "r"(kLanes));
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(xempty(l, b)));
+            }
+            for (int j = 0; j < depth_of(l); ++j) {
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(afull(l, j)));
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(aempty(l, j)), "r"(kLanes));
+            }
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(drain));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         *s_fail = 0;
     }
@@ -302,148 +388,223 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(FusedArgs a) {
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *s_tmem;
-    // an epilogue thread's TMEM lane quarter (warp % 4)
-    const uint32_t tl = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-    if (!mma_warp) {
+    const uint32_t tl = tmem + ((uint32_t)((warp & 3) * 32) << 16);  // epilogue thread's lane quarter
+    if (tid < kEpi) {
         for (int c = 128 * grp; c < 128 * grp + 128; c += 32) tzero32(tl + c);
         wait_st();
     }
     const float *bias = reinterpret_cast<const float *>(smem + kOffBias);
-    const uint32_t sbase = smem_u32(smem);
-    uint32_t phase = 0;  // bit b: parity of barrier b's next commit completion (per waiting thread)
-
+    Waiter wt{s_fail, a.err};
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
 
-    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
-        const int strip = tile % a.nstrips;
-        const int rb = (tile / a.nstrips) % a.nrb;
-        const int f = tile / (a.nstrips * a.nrb);
-        const Field &fd = a.fs.f[f];
-        const int y0 = rb * a.rows_per_block, y1 = min(nt, y0 + a.rows_per_block);
-        int lo[5], hi[5];
-        for (int l = 0; l <= 4; ++l) {
-            lo[l] = max(0, y0 - 4 + l);
-            hi[l] = min(nt, y1 + 4 - l);
-        }
-        const int t_end = hi[3] + 8;
-        if (mma_warp) {
-            // ---- MMA warp: per row time, the features, then each layer's MMAs once its warpgroup has
-            //      freed the slot (and the previous layer's warpgroup has written the input row)
-            for (int tau = lo[0]; tau <= t_end; ++tau) {
-                nb_sync(5);
-                for (int l = 1; l <= 4; ++l) {
-                    nb_sync(l);
-                    const int s = tau - 2 * l + 2;
-                    if ((tid & 31) == 0 && !*s_fail) {
-                        tc_fence_after();
-                        if (s >= lo[l - 1] && s < hi[l - 1]) issue_layer(l, s, nt, lo, hi, sbase, tmem);
-                        commit(smem_u32(bar + (l - 1)));
-                    }
-                    __syncwarp();
+    if (tid >= kEpi) {
+        // ================= MMA warp of layer l: for each input row s, wait for the row and for the
+        // ring slot it starts (row s+1's, last used by row s+1-depth), issue, then commit to the row
+        // buffer's release and to "row s-1 complete"
+        const int l = ((tid - kEpi) >> 5) + 1;
+        const int D = depth_of(l);
+        uint32_t use[kNBuf] = {0, 0, 0}, ce[kDepth4];
+        for (int j = 0; j < kDepth4; ++j) ce[j] = 0;
+        const uint32_t dacc = tmem + acc_col(l - 1);
+        uint64_t adb[kNBuf];
+        for (int b = 0; b < kNBuf; ++b) adb[b] = make_desc(sbase + xbuf(l, b), kPlane, 128);
+        const uint64_t bd0 = l < 4 ? make_desc(sbase + (l == 1 ? kOffB1 : (l == 2 ? kOffB2 : kOffB3)), kBChunk, 128)
+                                   : make_desc(sbase + kOffB4, kB4Chunk, 128);
+        for (int tile = blockIdx.x; tile < a.ntiles && !*s_fail; tile += gridDim.x) {
+            int lo[5], hi[5], strip, f;
+            tile_rows(a, tile, lo, hi, strip, f);
+            const int L = lo[l - 1], H = hi[l - 1];
+            const bool top_ok = lo[l] == 0, bot_ok = hi[l] == nt;
+            for (int s = L; s < H && !*s_fail; ++s) {
+                const int b = s % kNBuf;
+                wt.wait(xfull(l, b), use[b]++);
+                if (s + 1 - D >= L - 1) {
+                    const int j = (s + 1) & (D - 1);
+                    wt.wait(aempty(l, j), ce[j]++);
                 }
+                {
+                    const int c = (s - 1) & (D - 1);
+                    const uint64_t ad0 = b == 0 ? adb[0] : (b == 1 ? adb[1] : adb[2]);
+                    const bool top = s == 1 && top_ok, bot = s == nt - 2 && bot_ok;
+                    const int oslot = (nt - 1) & (D - 1);
+                    const bool go = !*s_fail;
+                    switch (l) {
+                        case 1: {
+                            const RowOps<1> ops(dacc, ad0, bd0, c);
+                            if (go && elect_one()) {
+                                tc_fence_after();
+                                ops.issue();
+                                if (top) issue_pole<1>(dacc, ad0, sbase, true, 0);
+                                if (bot) issue_pole<1>(dacc, ad0, sbase, false, oslot);
+                                commit(xempty(l, b));
+                                commit(afull(l, c));
+                            }
+                            break;
+                        }
+                        case 2: {
+                            const RowOps<2> ops(dacc, ad0, bd0, c);
+                            if (go && elect_one()) {
+                                tc_fence_after();
+                                ops.issue();
+                                if (top) issue_pole<2>(dacc, ad0, sbase, true, 0);
+                                if (bot) issue_pole<2>(dacc, ad0, sbase, false, oslot);
+                                commit(xempty(l, b));
+                                commit(afull(l, c));
+                            }
+                            break;
+                        }
+                        case 3: {
+                            const RowOps<3> ops(dacc, ad0, bd0, c);
+                            if (go && elect_one()) {
+                                tc_fence_after();
+                                ops.issue();
+                                if (top) issue_pole<3>(dacc, ad0, sbase, true, 0);
+                                if (bot) issue_pole<3>(dacc, ad0, sbase, false, oslot);
+                                commit(xempty(l, b));
+                                commit(afull(l, c));
+                            }
+                            break;
+                        }
+                        default: {
+                            const RowOps<4> ops(dacc, ad0, bd0, c);
+                            if (go && elect_one()) {
+                                tc_fence_after();
+                                ops.issue();
+                                if (top) issue_pole<4>(dacc, ad0, sbase, true, 0);
+                                if (bot) issue_pole<4>(dacc, ad0, sbase, false, oslot);
+                                commit(xempty(l, b));
+                                commit(afull(l, c));
+                            }
+                            break;
+                        }
+                    }
+                }
+                __syncwarp();
             }
-        } else {
+            // rows H-1 and H are complete with the last row's MMAs
+            if (!*s_fail && elect_one()) {
+                commit(afull(l, (H - 1) & (D - 1)));
+                commit(afull(l, H & (D - 1)));
+            }
+            __syncwarp();
+            // the epilogue of the slots the next tile starts on
+            for (int r = max(L - 1, H - D + 1); r <= H; ++r) {
+                const int j = r & (D - 1);
+                wt.wait(aempty(l, j), ce[j]++);
+            }
+            tc_fence_after();
+        }
+        // completes when every MMA this warp issued has finished
+        if (elect_one()) commit(drain);
+        __syncwarp();
+    } else if (grp < 3) {
+        // ================= epilogue of layer l = grp + 1, producer of layer l+1's input rows
+        const int l = grp + 1;
+        uint32_t ca[kDepth] = {0, 0, 0, 0}, fills[kNBuf] = {0, 0, 0};
+        for (int tile = blockIdx.x; tile < a.ntiles && !*s_fail; tile += gridDim.x) {
+            int lo[5], hi[5], strip, f;
+            tile_rows(a, tile, lo, hi, strip, f);
+            for (int r = lo[l - 1] - 1; r <= hi[l - 1] && !*s_fail; ++r) {
+                const int j = r & (kDepth - 1);
+                wt.wait(afull(l, j), ca[j]++);
+                tc_fence_after();
+                const uint32_t ta = tl + acc_col(l - 1) + 32 * j;
+                uint32_t v[32];
+                tld32(ta, v);
+                wait_ld();
+#pragma unroll
+                for (int k = 0; k < 32; ++k) pin(v[k]);
+                tzero32(ta);  // completes while the GELUs run (waited below)
+                if (r >= lo[l] && r < hi[l]) {
+                    const int bx = r % kNBuf;
+                    if (fills[bx] > 0) wt.wait(xempty(l + 1, bx), fills[bx] - 1);  // previous row consumed
+                    const float *bl_ = bias + 32 * (l - 1);
+                    uint8_t *dst = smem + xbuf(l + 1, bx) + (lane + 1) * 16;
+#pragma unroll
+                    for (int pl = 0; pl < 4; ++pl) {
+                        uint4 o;
+                        uint32_t *ow = reinterpret_cast<uint32_t *>(&o);
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            const int c = pl * 8 + 2 * e;
+                            const float2 y = __fadd2_rn(make_float2(__uint_as_float(v[c]), __uint_as_float(v[c + 1])),
+                                                        make_float2(bl_[c], bl_[c + 1]));
+                            const float2 gy = gelu2(y);
+                            ow[e] = pack2(gy.x, gy.y);
+                        }
+                        *reinterpret_cast<uint4 *>(dst + pl * kPlane) = o;
+                    }
+                    fills[bx]++;
+                    fence_async_smem();
+                    mbar_arrive(xfull(l + 1, bx));
+                }
+                wait_st();
+                tc_fence_before();
+                mbar_arrive(aempty(l, j));
+            }
+        }
+    } else {
+        // ================= warpgroup 3: features (input rows of layer 1), running 8 rows ahead of the
+        // layer-4 epilogue (output rows)
+        uint32_t ca[kDepth4], fills[kNBuf] = {0, 0, 0};
+        for (int j = 0; j < kDepth4; ++j) ca[j] = 0;
+        for (int tile = blockIdx.x; tile < a.ntiles && !*s_fail; tile += gridDim.x) {
+            int lo[5], hi[5], strip, f;
+            tile_rows(a, tile, lo, hi, strip, f);
+            const Field &fd = a.fs.f[f];
             const int xcol = strip * kOut - kHalo + lane;  // this lane's column (before wrap)
             const int col = ((xcol % np) + np) % np;
             const bool lane_out = lane >= kHalo && lane < kHalo + kOut && strip * kOut + (lane - kHalo) < np;
-            const int cw = col == 0 ? np - 1 : col - 1, ce = col + 1 == np ? 0 : col + 1;
-            const int l = grp + 1;  // this warpgroup's layer
+            const int cw = col == 0 ? np - 1 : col - 1, ce_ = col + 1 == np ? 0 : col + 1;
+            constexpr int kLead = 8;
+            const int nfeat = hi[0] - lo[0], nepi = hi[3] - lo[3] + 2;
             FeatIn pre;
-            float hout_next = 0.f, hout_in = 0.f;
-            if (l == 4) {
-                if (lo[0] < hi[0]) feat_load(pre, lo[0], nt, fd, a.g, col, cw, ce);
-                if (lo[0] - 8 >= lo[4] && lo[0] - 8 < hi[4]) hout_next = fd.h[(size_t)(lo[0] - 8) * fd.pitch + col];
-            }
-            for (int tau = lo[0]; tau <= t_end; ++tau) {
-                const int r = tau - 2 * l;  // epilogue row
-                if (l == 4) {
-                    // features of row tau into X0[tau & 1]; its last reader MMA_1(tau - 2) is covered by
-                    // layer 1's commit of row time tau - 1
-                    if (tau > lo[0]) wait_commit(bar, 0, phase, s_fail, a.err);
-                    if (tau < hi[0]) {
-                        feat_store(pre, fd, a.g, smem + kOffX0 + (tau & 1) * kRowX0, lane);
-                        if (tau + 1 < hi[0]) feat_load(pre, tau + 1, nt, fd, a.g, col, cw, ce);
-                    }
+            if (nfeat > 0) feat_load(pre, lo[0], nt, fd, a.g, col, cw, ce_);
+            float hout = 0.f;
+            for (int t = 0; t < max(nfeat, nepi + kLead) && !*s_fail; ++t) {
+                if (t < nfeat) {
+                    const int srow = lo[0] + t, b = srow % kNBuf;
+                    if (fills[b] > 0) wt.wait(xempty(1, b), fills[b] - 1);
+                    feat_store(pre, fd, a.g, smem + xbuf(1, b), lane);
+                    fills[b]++;
                     fence_async_smem();
-                    nb_arrive(5);
-                    hout_in = hout_next;
-                    const int rn = tau - 7;
-                    if (rn >= lo[4] && rn < hi[4]) hout_next = fd.h[(size_t)rn * fd.pitch + col];
+                    mbar_arrive(xfull(1, b));
+                    if (t + 1 < nfeat) feat_load(pre, srow + 1, nt, fd, a.g, col, cw, ce_);
                 }
-                if (tau > lo[0]) {
-                    wait_commit(bar, l - 1, phase, s_fail, a.err);  // this layer's MMAs of tau - 1
-                    // the next layer's MMAs of tau - 1: they, and so MMA_{l+1}(r - 2), are done reading
-                    // the X_l buffer written below
-                    if (l < 4) wait_commit(bar, l, phase, s_fail, a.err);
+                const int te = t - kLead;
+                if (te >= 0 && te < nepi) {
+                    const int r = lo[3] - 1 + te;
+                    const bool emit = r >= lo[4] && r < hi[4];
+                    if (emit && lane_out) hout = fd.h[(size_t)r * fd.pitch + col];
+                    const int j = r & (kDepth4 - 1);
+                    wt.wait(afull(4, j), ca[j]++);
                     tc_fence_after();
-                }
-                if (r >= lo[l - 1] - 1 && r <= hi[l - 1]) {
-                    const int j = mod3(r);
-                    const bool emit = r >= lo[l] && r < hi[l];
-                    if (l < 4) {
-                        const uint32_t ta = tl + acc_col(l - 1) + 32 * j;
-                        uint32_t v[32];
-                        tld32(ta, v);
-                        wait_ld();
-#pragma unroll
-                        for (int k = 0; k < 32; ++k) pin(v[k]);
-                        tzero32(ta);  // completes while the GELUs run (waited below)
-                        if (emit) {
-                            const float *bl_ = bias + 32 * (l - 1);
-                            uint8_t *dst = smem + kOffX + ((l - 1) * 2 + (r & 1)) * kRowX + (lane + 1) * 16;
-#pragma unroll
-                            for (int pl = 0; pl < 4; ++pl) {
-                                uint4 o;
-                                uint32_t *ow = reinterpret_cast<uint32_t *>(&o);
-#pragma unroll
-                                for (int e = 0; e < 4; ++e) {
-                                    const int c = pl * 8 + 2 * e;
-                                    const float2 y = __fadd2_rn(make_float2(__uint_as_float(v[c]), __uint_as_float(v[c + 1])),
-                                                                make_float2(bl_[c], bl_[c + 1]));
-                                    const float2 gy = gelu2(y);
-                                    ow[e] = pack2(gy.x, gy.y);
-                                }
-                                *reinterpret_cast<uint4 *>(dst + pl * kPlane) = o;
-                            }
+                    const uint32_t ta = tl + acc_col(3) + j;
+                    uint32_t yv = tld1(ta);
+                    wait_ld();
+                    pin(yv);
+                    tzero1(ta);
+                    const float y = __fadd_rn(__uint_as_float(yv), bias[96]);
+                    if (emit && lane_out) {
+                        if (a.y_out) a.y_out[((size_t)f * nt + r) * np + col] = y;
+                        if (a.h_out) {
+                            float o = hout;
+                            if (r > 0 && r + 1 < nt) o = fmaxf(__fadd_rn(hout, __fmul_rn(fd.kout, y)), 0.f);
+                            a.h_out[(size_t)r * a.pitch_out + col] = o;
                         }
-                        wait_st();
-                    } else {
-                        const uint32_t ta = tl + acc_col(3) + j;
-                        uint32_t yv = tld1(ta);
-                        wait_ld();
-                        pin(yv);
-                        tzero1(ta);
-                        const float y = __fadd_rn(__uint_as_float(yv), bias[96]);
-                        if (emit && lane_out) {
-                            const float hc = hout_in;
-                            if (a.y_out) a.y_out[((size_t)f * nt + r) * np + col] = y;
-                            if (a.h_out) {
-                                float o = hc;
-                                if (r > 0 && r + 1 < nt) o = fmaxf(__fadd_rn(hc, __fmul_rn(fd.kout, y)), 0.f);
-                                a.h_out[(size_t)r * a.pitch_out + col] = o;
-                            }
-                        }
-                        wait_st();
                     }
+                    wait_st();
+                    tc_fence_before();
+                    mbar_arrive(aempty(4, j));
                 }
-                fence_async_smem();
-                tc_fence_before();
-                nb_arrive(l);
             }
-            // drain: the commits of the tile's last row time on every barrier this thread tracks
-            if (l == 4) wait_commit(bar, 0, phase, s_fail, a.err);
-            wait_commit(bar, l - 1, phase, s_fail, a.err);
-            if (l < 4) wait_commit(bar, l, phase, s_fail, a.err);
-            tc_fence_after();
         }
-        __syncthreads();
-        if (*s_fail) break;
     }
-    if (*s_fail && tid == 0) {
-        for (int l = 0; l < 4; ++l) mbar_wait_bounded(smem_u32(bar + l), 0u), mbar_wait_bounded(smem_u32(bar + l), 1u);
-    }
+    __syncthreads();
+    // no MMA may still write the accumulators when the columns are released
+    if (tid == 0 && !mbar_wait_bounded(drain, 0u)) atomicOr(a.err, 1u);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -453,7 +614,7 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(FusedArgs a) {
 // Packs the parameter vector into the shared-memory image of fused_kernel.
 __global__ void pack_fused_kernel(const float *theta, uint8_t *img) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    const int dy_of_block[5] = {1, 0, -1, 1, 0};
+    const int dy_of_block[3] = {1, 0, -1};
     bf16 *B = reinterpret_cast<bf16 *>(img);
     // layers 1-3: element (step, chunk, row n, e8); layer 1 step = dx, chunk = 8-feature plane
     const int per1 = 3 * 2 * kBRows * 8, per23 = 6 * 2 * kBRows * 8;
@@ -471,18 +632,19 @@ __global__ void pack_fused_kernel(const float *theta, uint8_t *img) {
         B[kOffB2 / 2 + o] = __float2bfloat16_rn(theta[SBS_NN_W2 + (t * 32 + oc) * 32 + ic]);
         B[kOffB3 / 2 + o] = __float2bfloat16_rn(theta[SBS_NN_W3 + (t * 32 + oc) * 32 + ic]);
     }
+    // layer 4: rows 15, 16, 17 = dy +1, 0, -1 (all other rows zero)
     if (e < 6 * 2 * kB4Rows * 8) {
         const int e8 = e % 8, n = (e / 8) % kB4Rows, ch = (e / (8 * kB4Rows)) % 2, st = e / (16 * kB4Rows);
         const int dx = (st >> 1) - 1, kk = st & 1, ic = kk * 16 + ch * 8 + e8;
         float v = 0.f;
-        if (n < 5) v = theta[SBS_NN_W4 + ((dy_of_block[n] + 1) * 3 + (dx + 1)) * 32 + ic];
+        if (n >= 15 && n <= 17) v = theta[SBS_NN_W4 + ((1 - (n - 15) + 1) * 3 + (dx + 1)) * 32 + ic];
         B[(kOffB4 + st * kB4Step + ch * kB4Chunk) / 2 + n * 8 + e8] = __float2bfloat16_rn(v);
     }
     if (e < 6 * 2 * kBxRows * 8) {
         const int e8 = e % 8, n = (e / 8) % kBxRows, ch = (e / (8 * kBxRows)) % 2, st = e / (16 * kBxRows);
         const int dx = (st >> 1) - 1, kk = st & 1, ic = kk * 16 + ch * 8 + e8;
         float vt = 0.f, vb = 0.f;
-        if (n == 2) {
+        if (n == 15) {
             vt = theta[SBS_NN_W4 + (0 * 3 + (dx + 1)) * 32 + ic];  // dy = -1
             vb = theta[SBS_NN_W4 + (2 * 3 + (dx + 1)) * 32 + ic];  // dy = +1
         }
@@ -520,7 +682,7 @@ int fused_pack(sbs_surrogate *s) {
             return set_error(SBS_E_NOMEM, "fused weight image allocation failed");
         SBS_CUDA_TRY(cudaFuncSetAttribute(fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem));
     }
-    const int n = 6 * 2 * kBRows * 8;
+    const int n = 6 * 2 * kBRows * 8;  // the largest element count of the image's parts
     pack_fused_kernel<<<(n + 255) / 256, 256, 0, stream_of(s)>>>(theta_of(s), fs->image);
     SBS_CUDA_TRY(cudaGetLastError());
     *fused_dirty_flag(s) = 0;
