@@ -11,9 +11,17 @@ synthetic (seeded); the field keeps evolving from step to step. L2 (129 MB) is f
 value: cell-steps/s over the K timed bench steps, device-resident, CUDA events on the
 handle's stream. e2e: the same through the C ABI with host buffers: each step uploads h and
 surfactant from pinned host memory, runs, and reads both fields and the volumes back.
-roofline: the step kernel at 16 algorithmic bytes per cell-step (read h, Gamma; write h, Gamma).
+roofline: the dominant kernel, the temporally blocked step (wtb_wgsl_kernel, 4 steps per
+launch), at 16 algorithmic bytes per cell-step (read h, Gamma; write h, Gamma) times the steps
+of a launch, against the measured copy bandwidth; `traffic` is its ncu DRAM bytes per launch.
 cpu_baseline: the oracle's f64 restatement of DrainageSimulator::step (drainage.rs:298-392) on
-all host cores, on a bounded sample of the same field (a few dozen steps).
+all host cores, on a bounded sample of the same field (about --cpu-seconds of work).
+surrogate: the learned 64-step operator (include/sbs_nn.h) trained here on 512 plain-solver
+trajectories at 256 x 512, then a 10,000-step rollout of the same 2048 x 4096 field with a plain
+check every 8 intervals; effective cell-steps/s and the masked relative L-inf error of the final
+thickness against the plain run (rows with sin(theta) >= 0.2; nearer the poles the explicit
+scheme is unstable at this resolution).
+foam / spectral: the batched-foam and spectral-contraction workloads, device-resident.
 
 --impl reference: times that CPU restatement alone (the reference is Rust and cannot be
 built here), same metric and config.
@@ -49,6 +57,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU baseline sample length")
+    p.add_argument("--skip-aux", action="store_true",
+                   help="plain path only (no surrogate / foam / spectral / CPU baseline), e.g. for an ncu launch list")
     return p.parse_args()
 
 
@@ -69,7 +79,7 @@ def hbm_peak():
 
 def ncu_traffic():
     """Per-launch DRAM bytes of the step kernel from the committed ncu summary (or None)."""
-    path = os.path.join(ROOT, "profiles", "drain_step_wgsl_c1.md")
+    path = os.path.join(ROOT, "profiles", "drain_wtb_wgsl_c1.md")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -137,7 +147,7 @@ def cpu_baseline(h: np.ndarray, target_s: float, threads: int):
     t0 = time.perf_counter()
     sim.step(0.001)
     one = time.perf_counter() - t0
-    n = int(max(2, min(400, target_s / max(one, 1e-6))))
+    n = int(max(2, min(20000, target_s / max(one, 1e-6))))
     t0 = time.perf_counter()
     sim.step_n(0.001, n)
     dt = time.perf_counter() - t0
@@ -167,6 +177,163 @@ def run_reference(args):
             "cpu_baseline": {**vals[-1], "value": v},
             "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def launches_per_run(k: int) -> int:
+    """Kernel launches of one run of STEPS_PER_RUN steps with a volume check every CHECK_EVERY (the
+    library's chunking: chunks end at each check; within a chunk k-step launches, then single
+    steps for the remainder, the run's very last step single)."""
+    total, done = 0, 0
+    while done < STEPS_PER_RUN:
+        g = min(256, STEPS_PER_RUN - done, CHECK_EVERY - done % CHECK_EVERY)
+        tail = 1 if done + g == STEPS_PER_RUN else 0
+        body = g - tail
+        total += (body // k + body % k + tail) if k > 1 else g
+        done += g
+    return total
+
+
+def surrogate_section(sbs, synthetic, h0, c0, torch):
+    """C4: train on 512 plain trajectories at 256 x 512, then the checked 10,000-step rollout."""
+    N = sbs._native
+    nt, np_ = h0.shape
+    cells = h0.size
+    s = sbs.DrainageSurrogate(seed=7)
+    t0 = time.perf_counter()
+    ntraj = 512
+    for h, c, visc, rad in synthetic.surrogate_trajectories(ntraj):
+        s.add_trajectory(h, c, sbs.field_params(256, 512, viscosity=visc, bubble_radius=rad), pairs=4)
+    t1 = time.perf_counter()
+    iters = 3000
+    losses = s.train(ntraj - 32, iters, batch=8, lr=2e-3, seed=5)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    ev = s.evaluate(ntraj - 32, 32, mode="fused")
+    p = sbs.field_params(nt, np_, bubble_radius=0.025)
+
+    def fresh():
+        sim = sbs.GPUDrainageSimulator(None, 550e-9, np_, nt)
+        sim.update_params(p)
+        sim.set_thickness_array(h0)
+        sim.set_concentration_array(c0)
+        return sim
+
+    # plain reference run (same stream semantics as the rollout's plain intervals, no volume checks)
+    ref = fresh()
+    ref.run(64)
+    ref.set_thickness_array(h0)
+    ref.set_concentration_array(c0)
+    torch.cuda.synchronize()
+    ta = time.perf_counter()
+    ref.run(STEPS_PER_RUN)
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - ta
+    h_ref = ref.thickness_array()
+    # fused forward pass alone (one 64-pass interval)
+    sim = fresh()
+    for _ in range(3):
+        s.advance(sim, mode="fused")
+    reps = 20
+    torch.cuda.synchronize()
+    ta = time.perf_counter()
+    for _ in range(reps):
+        s.advance(sim, mode="fused")
+    torch.cuda.synchronize()
+    fused_ms = (time.perf_counter() - ta) / reps * 1e3
+    # the checked rollout: 156 intervals (9,984 passes) + 16 plain passes = 10,000 steps
+    sim = fresh()
+    torch.cuda.synchronize()
+    ta = time.perf_counter()
+    st = s.rollout(sim, STEPS_PER_RUN // 64 * 64, check_every=8, tol=1e-3, mode="fused")
+    sim.run(STEPS_PER_RUN % 64)
+    torch.cuda.synchronize()
+    roll_s = time.perf_counter() - ta
+    h_sur = sim.thickness_array()
+    err = sbs.masked_error(h_sur, h_ref)
+    err_id = sbs.masked_error(h0, h_ref)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    tf_peak = float(peaks.get("bf16_tflops", 1900.0))
+    flop_cell = 2 * 9 * (16 * 32 + 32 * 32 * 2 + 32 * 1)  # useful multiply-adds x 2 per cell and interval
+    tflops = flop_cell * cells / (fused_ms * 1e-3) / 1e12
+    rate = cells * STEPS_PER_RUN / roll_s
+    plain_rate = cells * STEPS_PER_RUN / plain_s
+    out = {"value": rate, "unit": "cell-steps/s", "speedup_vs_plain": rate / plain_rate,
+           "plain_value": plain_rate, "masked_rel_linf_vs_plain": err, "identity_rel_linf_vs_plain": err_id,
+           "tol": 1e-3, "stats": st, "fused_ms_per_interval": fused_ms,
+           "fused_interval_cell_steps_per_s": cells * 64 / (fused_ms * 1e-3),
+           "tensor": {"bound": "tensor", "achieved": tflops, "peak": tf_peak, "unit": "TFLOP/s",
+                      "frac": tflops / tf_peak, "flop_per_cell": flop_cell, "peak_kind": "measured bf16 burst"},
+           "train": {"trajectories": ntraj, "grid": "256 x 512", "pairs_per_trajectory": 4, "iters": iters,
+                     "batch": 8, "data_s": t1 - t0, "train_s": t2 - t1, "loss_first": float(losses[:10].mean()),
+                     "loss_last": float(losses[-50:].mean())},
+           "heldout_256": ev}
+    s.close()
+    return out
+
+
+def foam_section(sbs, synthetic, torch):
+    res, rad = synthetic.foam_bubbles()
+    foam = sbs.FoamDrainage(res, rad)
+    hs = synthetic.foam_fields(res)
+    for b in range(len(res)):
+        foam.set_thickness(b, hs[b])
+    k, rb = foam.autotune(8)
+    foam.run(100)
+    st = torch.cuda.ExternalStream(foam.stream())
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    foam.run(1000)
+    b.record(st)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    cells = foam.total_cells()
+    foam.close()
+    return {"value": cells * 1000 / (ms * 1e-3), "unit": "cell-steps/s", "bubbles": int(len(res)), "cells": int(cells),
+            "steps": 1000, "ms": ms, "tiles": {"steps_per_phase": k, "strip_rows": rb},
+            "algorithmic_gbs": cells * 1000 * 16 / (ms * 1e-3) / 1e9}
+
+
+def spectral_section(sbs, synthetic, torch):
+    N = sbs._native
+    n = 8_388_608
+    t, c, nf = synthetic.spectral_points(n)
+    wl = synthetic.WAVELENGTHS_81.astype(np.float32)
+    cmf = synthetic.spectral_cmf().astype(np.float32)
+    dt, dc, dn = (torch.from_numpy(x).cuda() for x in (t, c, nf))
+    out = {}
+    res = {}
+    for mode, name in ((N.SPECTRAL_TC_BF16, "tc_bf16"), (N.SPECTRAL_FP32, "fp32")):
+        o = torch.empty((n, 3), device="cuda")
+
+        def run():
+            N.call("sbs_spectral_rgb", ctypes.c_void_p(dt.data_ptr()), ctypes.c_void_p(dc.data_ptr()),
+                   ctypes.c_void_p(dn.data_ptr()), n, N.ptr(wl), wl.size, N.ptr(cmf), mode,
+                   ctypes.c_void_p(o.data_ptr()), N.MEM_DEVICE, None)
+
+        run()
+        torch.cuda.synchronize()
+        reps = 10
+        ta = time.perf_counter()
+        for _ in range(reps):
+            run()
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - ta) / reps * 1e3
+        out[name] = {"value": n / (ms * 1e-3), "unit": "points/s", "ms": ms}
+        res[name] = o[:262144].cpu().numpy()
+    # precision on a 262,144-point subset against the FP64 oracle
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+
+    m = 262144
+    want = orc.spectral_rgb(t[:m], c[:m], nf[:m], wl.astype(np.float64), cmf.astype(np.float64))
+    for name in res:
+        rel = float(np.max(np.abs(res[name] - want)) / np.max(np.abs(want)))
+        de = synthetic.delta_e76(res[name], want, cmf.astype(np.float64).sum(0))
+        out[name].update({"rel_linf_vs_fp64": rel, "delta_e76_mean": float(de.mean()), "delta_e76_max": float(de.max())})
+    out["points"] = n
+    out["wavelengths"] = int(wl.size)
+    return out
 
 
 def main():
@@ -227,9 +394,15 @@ def main():
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
     total_ms, kern_ms = float(t[0]), float(t[1])
     value = world * cells * STEPS_PER_RUN * args.steps / (total_ms / 1e3)
-    launch_us = kern_ms * 1e3 / (args.steps * STEPS_PER_RUN)
+    kb = ctypes.c_int()
+    N.call("sbs_gpu_drainage_time_blocking", sim.handle, ctypes.byref(kb))
+    k_block = max(1, kb.value)
+    launches = launches_per_run(k_block)
+    # the dominant kernel: k-step launches; algorithmic bytes per launch = 16 B x cells x k
+    step_us = kern_ms * 1e3 / (args.steps * STEPS_PER_RUN)
+    launch_us = step_us * k_block
     peak, peak_kind = hbm_peak()
-    achieved = BYTES_PER_CELL_STEP * cells / (launch_us * 1e-6) / 1e9
+    achieved = BYTES_PER_CELL_STEP * cells * k_block / (launch_us * 1e-6) / 1e9
     traffic = ncu_traffic()
     vol_drift = float(abs(vols[-1] - vols[0]) / vols[0]) if vols is not None and len(vols) else None
 
@@ -279,8 +452,14 @@ def main():
     cpu_sem_ms = a_ev.elapsed_time(b_ev)
     cpu_sem_rate = cells * 2000 / (cpu_sem_ms / 1e3)
 
+    surrogate = foam = spectral = None
+    if not args.skip_aux:
+        surrogate = surrogate_section(sbs, synthetic, h0, c0, torch)
+        foam = foam_section(sbs, synthetic, torch)
+        spectral = spectral_section(sbs, synthetic, torch)
+
     base = None
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and not args.skip_aux:
         base = cpu_baseline(h0, args.cpu_seconds, os.cpu_count() or 1)
 
     if rank == 0:
@@ -295,16 +474,23 @@ def main():
                        "l2": "512 MB write before every bench step (working set 128 MB)",
                        "replicas": world},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "peak_kind": peak_kind, "bytes_per_cell_step": BYTES_PER_CELL_STEP,
-                         "launch_us": launch_us, "kernel": "drain_step_kernel<WGSL>"},
+                         "traffic": traffic, "peak_kind": peak_kind,
+                         "bytes_per_launch": BYTES_PER_CELL_STEP * cells * k_block,
+                         "steps_per_launch": k_block, "launch_us": launch_us,
+                         "kernel": f"wtb_wgsl_kernel<{k_block}> (temporally blocked WGSL step)",
+                         "note": "algorithmic bytes: 16 B per cell-step; temporal blocking keeps k steps on chip, "
+                                 "so achieved can exceed the copy peak and traffic is ~1/k of the algorithmic bytes"},
             "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": 2 * cells * 4,
                     "d2h_bytes_per_step": 2 * cells * 4 + 8 * (STEPS_PER_RUN // CHECK_EVERY)},
-            "gpu_launches": args.steps * STEPS_PER_RUN,
+            "gpu_launches": args.steps * launches,
             "clocks": clk.summary(),
             "volume_rel_drift_per_run": vol_drift,
             "cpu_semantics": {"value": cpu_sem_rate, "unit": "cell-steps/s", "storage": "f32x2 (16 B/cell-step)",
                               "frac_hbm": BYTES_PER_CELL_STEP * cells * 2000 / (cpu_sem_ms / 1e3) / 1e9 / peak},
             "cpu_baseline": base,
+            "surrogate": surrogate,
+            "foam": foam,
+            "spectral": spectral,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
