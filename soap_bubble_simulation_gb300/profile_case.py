@@ -4,7 +4,10 @@
 
 Cases: `wgsl` (GPUDrainageSimulator semantics, h + surfactant), `cpu` (DrainageSimulator
 semantics, compensated f32x2), `cpu32` (plain f32), `spectral-tc` / `spectral-fp32` (81-wavelength
-spectral colour of --points seeded points, tensor-core or FP32 contraction). The field is the seeded smooth-mode field of
+spectral colour of --points seeded points, tensor-core or FP32 contraction), `surrogate-fused` /
+`surrogate-layered` (--steps 64-pass surrogate intervals of the field, untrained seeded weights:
+the same kernels and shapes as a trained network), `foam` (the 4096-bubble foam batch, --steps
+steps with the default tiles). The field is the seeded smooth-mode field of
 the 2048-resolution workload, built at the requested resolution. Steps launch one kernel each
 (graph replay for runs of 8 or more).
 """
@@ -21,11 +24,14 @@ from .drainage import DrainageSimulator, GPUDrainageSimulator, _Handle
 
 def main(argv=None) -> None:
     p = argparse.ArgumentParser()
-    p.add_argument("--case", default="wgsl", choices=["wgsl", "cpu", "cpu32", "spectral-tc", "spectral-fp32"])
+    p.add_argument("--case", default="wgsl",
+                   choices=["wgsl", "cpu", "cpu32", "spectral-tc", "spectral-fp32", "surrogate-fused", "surrogate-layered",
+                            "foam"])
     p.add_argument("--points", type=int, default=1 << 20, help="spectral cases: number of points")
     p.add_argument("--res", type=int, default=2048)
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--blocking", type=int, default=-1, help="WGSL steps per launch (default: library choice)")
+    p.add_argument("--bubbles", type=int, default=4096, help="foam case: number of bubbles")
     a = p.parse_args(argv)
     if a.case.startswith("spectral"):
         from .interference import spectral_rgb
@@ -37,7 +43,33 @@ def main(argv=None) -> None:
             spectral_rgb(t, ci, nf, wl, cmf, mode="tc" if a.case == "spectral-tc" else "fp32")
         print(f"ran {a.steps} spectral evaluations of {a.points} points ({a.case})")
         return
+    if a.case == "foam":
+        from .foam import FoamDrainage
+
+        res, rad = synthetic.foam_bubbles(a.bubbles)
+        foam = FoamDrainage(res, rad)
+        hs = synthetic.foam_fields(res)
+        for b in range(len(res)):
+            foam.set_thickness(b, hs[b])
+        foam.run(a.steps)
+        foam.close()
+        print(f"ran {a.steps} foam steps of {len(res)} bubbles")
+        return
     h, c = synthetic.bubble_c1(a.res)
+    if a.case.startswith("surrogate"):
+        from .surrogate import DrainageSurrogate, field_params
+
+        s = DrainageSurrogate(seed=7)
+        sim = GPUDrainageSimulator(None, 550e-9, 2 * a.res, a.res)
+        sim.update_params(field_params(a.res, 2 * a.res, bubble_radius=0.025))
+        sim.set_thickness_array(h)
+        sim.set_concentration_array(c)
+        for _ in range(a.steps):
+            s.advance(sim, mode="fused" if a.case == "surrogate-fused" else "layered")
+        s.close()
+        sim.close()
+        print(f"ran {a.steps} surrogate intervals ({a.case}) at resolution {a.res}")
+        return
     if a.case == "wgsl":
         sim = GPUDrainageSimulator(None, 550e-9, 2 * a.res, a.res)
         if a.blocking >= 0:
