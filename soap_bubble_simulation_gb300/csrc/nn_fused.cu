@@ -4,31 +4,41 @@
 //
 // Tiling. A tile is a strip of 128 consecutive phi columns (lanes; the middle 120 are output, the
 // 4 on each side are the halo the four layers consume) times a block of theta rows of one field.
-// The block runs eight agents that only talk through mbarriers: four MMA warps (one per layer:
-// for each input row, wait for the row and for the accumulator slot it starts, issue, commit) and
-// four epilogue warpgroups (warpgroup l-1 reads layer l's finished row from TMEM, zeroes the slot,
-// adds the bias, applies GELU and writes the activation row into one of three input buffers of layer
-// l+1; warpgroup 3 writes the features and the thickness update). Every ring (activation buffers:
-// full / empty; accumulator rows: full / empty, and a per-tile barrier for the last three rows) is
-// balanced per tile, so each waiter is at most one phase behind and parity waits are exact.
-// The block streams its rows top to bottom through all four layers at once, each layer as far
-// behind the one before as its inputs require.
+// The block runs nine agents that only talk through mbarriers: four MMA warps (one per layer:
+// for each input row, wait for the row and for the accumulator slot it starts, issue, commit),
+// three epilogue warpgroups (warpgroup l-1 reads layer l's finished row from TMEM, zeroes and
+// releases the slot at once, then adds the bias, applies GELU and writes the activation row into
+// one of four input buffers of layer l+1), a feature warpgroup (the input rows of layer 1) and an
+// output warpgroup (layer 4's rows: y and the thickness update). Every ring (activation buffers:
+// full / empty; accumulator rows: full / empty) is balanced per tile, so each waiter is at most
+// one phase behind and parity waits are exact. The block streams its rows top to bottom through
+// all four layers at once, each layer as far behind the one before as its inputs require.
+// The epilogue and the MMA loop are one code copy each for all layers (the layer is a runtime
+// value): separate instantiations of these unrolled bodies cost ~30 % in instruction-cache misses.
 //
 // Convolution as MMAs. Activations of one row live in shared memory as planes of 8 channels with
 // 16 B per cell (K-major, rows of the A operand = cells, SBO = 128 B), so the dx = -1/0/+1 taps
 // are the same tile read at start offsets of 16 B apart: no im2col buffer. The three dy taps are
-// stacked along N: one M=128 x N=96 MMA multiplies an input row by [W(dy) for three output rows]
-// and accumulates into a ring of three 32-column TMEM slots (output row r lives in slot r mod 3).
-// B holds the dy blocks as [W+1; W0; W-1; W+1; W0]; a window of three consecutive blocks, chosen by
-// the input row mod 3, matches the ring order, so each input row is one contiguous N=96 operand.
-// A slot is read by the epilogue once its row's three input rows are in, then zeroed for reuse.
-// theta reflection at the poles adds one N=32 MMA (input row 1 into output row 0 with W-1, input
-// row nt-2 into output row nt-1 with W+1).
+// stacked along N: one M=128 x N=96 MMA multiplies an input row by [W(+1); W(0); W(-1)] and
+// accumulates into three consecutive 32-column slots of a ring of four (output rows s-1, s, s+1
+// of input row s; row r lives in slot r mod 4). Where the three slots wrap past the end of the
+// ring the MMA is split in two (N = 64 + 32 or 32 + 64). A slot is read by the epilogue once its
+// row's three input rows are in, then zeroed for reuse. theta reflection at the poles adds one
+// N=32 MMA (input row 1 into output row 0 with W-1, input row nt-2 into output row nt-1 with W+1).
+// Operand bandwidth: an N=96 MMA reads 4 KB of A and 3 KB of B from shared memory (~56 cycles at
+// 128 B/clk), which is the measured issue-to-issue time of back-to-back MMAs of this shape.
 //
-// TMEM columns: layer 1 [0, 96), layer 2 [96, 192), layer 3 [192, 288), layer 4 [288, 304)
-// (N = 16, rows of B beyond the dy ring are zero). Every MMA's D column is a multiple of 16: the
-// layer-4 pole extras keep D at column 288 and place their single weight row at the target slot
-// by the B window offset. One CTA per SM (it allocates all 512 columns).
+// TMEM columns: layer 1 [0, 128), layer 2 [128, 256), layer 3 [256, 384), layer 4 [384, 400)
+// (a ring of 16 single columns; the N=16 MMA always writes columns 384..399 and B places the three
+// dy weight rows at the right columns by its window offset). Every MMA's D column is a multiple of
+// 16. One CTA per SM (it allocates all 512 columns).
+// Because every layer-4 MMA also adds exact zeros to the 13 columns it does not own, no column of
+// that ring may be zeroed while a layer-4 MMA is in flight (the MMA's read-modify-write could put
+// the old value back). The output warpgroup therefore never zeroes a column inside a tile: it
+// reads the running sum and subtracts its previous reading of the column (kept in shared memory),
+// and it zeroes the whole ring at the end of the tile, when every MMA of the tile has completed
+// (the last row's completion barrier is committed after them) and before it releases the last
+// slot. Tiles are at most 256 rows, so a column sums at most 17 rows (FP32 error ~1e-6 relative).
 // Every mbarrier wait is bounded; a timeout sets the error flag and the kernel drains and exits.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -54,8 +64,9 @@ namespace {
 
 constexpr int kLanes = 128;                    // TMEM lanes = cells of a strip
 constexpr int kGroups = 4;                     // warpgroups: each owns one 8-channel plane
-constexpr int kEpi = kLanes * kGroups;         // epilogue threads (16 warps)
-constexpr int kThreads = kEpi + 4 * 32;        // + one MMA-issuing warp per layer
+constexpr int kEpi = kLanes * kGroups;         // epilogue + feature threads (16 warps)
+constexpr int kOutT = kEpi + kLanes;           // + the layer-4 epilogue warpgroup
+constexpr int kThreads = kOutT + 4 * 32;       // + one MMA-issuing warp per layer
 constexpr int kOut = 120;                      // output columns per strip
 constexpr int kHalo = 4;                       // lanes on each side of the outputs
 constexpr int kCells = 136;                    // staged cells per plane (q = lane + 1)
@@ -81,15 +92,25 @@ constexpr uint32_t kImage = kOffBias + 128 * 4;
 constexpr int kDepth = 4, kDepth4 = 16;
 __host__ __device__ constexpr int depth_of(int l) { return l < 4 ? kDepth : kDepth4; }  // l 1-based
 __host__ __device__ constexpr uint32_t acc_col(int l) { return 128u * (uint32_t)l; }    // l 0-based; 3 -> 384
+static_assert(acc_col(3) + 16 <= 512, "TMEM columns");
+// ring slot of row r >= -D
+template <int D>
+__device__ __forceinline__ int ring(int r) { return (r + D) % D; }
 // rest of shared memory
-constexpr int kNBuf = 3;                                   // activation rows in flight per layer input
+constexpr int kNBuf = 4;                                   // activation rows in flight per layer input
+static_assert((kNBuf & (kNBuf - 1)) == 0, "kNBuf is a power of two");
 constexpr uint32_t kOffX0 = (kImage + 1023) / 1024 * 1024;  // feature rows
 constexpr uint32_t kOffX = kOffX0 + kNBuf * kRowX0;         // 3 layers x kNBuf rows
 constexpr uint32_t kOffBar = kOffX + 3 * kNBuf * kRowX;
 // barriers of layer l: xfull[kNBuf], xempty[kNBuf], afull[depth], aempty[depth]
 __host__ __device__ constexpr int bar_base(int l) { return (l - 1) * (2 * kNBuf + 2 * kDepth); }
 constexpr int kNumBars = 3 * (2 * kNBuf + 2 * kDepth) + 2 * kNBuf + 2 * kDepth4;
-constexpr uint32_t kSmem = kOffBar + 8 * (kNumBars + 1) + 64;  // + the exit drain barrier
+// + the exit drain barrier, the TMEM base and the fail flag; then the layer-4 epilogue's previous
+// readings [16 columns][128 lanes]
+constexpr uint32_t kOffPrev = (kOffBar + 8 * (kNumBars + 1) + 64 + 15) / 16 * 16;
+constexpr uint32_t kSmem = kOffPrev + kDepth4 * kLanes * 4;
+constexpr int kMaxTileRows = 256;
+static_assert(kSmem <= 227 * 1024, "shared memory per CTA");
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at 2 GHz
 
 __host__ __device__ constexpr uint32_t idesc(int n) {
@@ -154,9 +175,13 @@ __device__ __forceinline__ uint32_t tld1(uint32_t taddr) {
     return v;
 }
 
-__device__ __forceinline__ void tzero1(uint32_t taddr) {
+__device__ __forceinline__ void tzero16(uint32_t taddr) {
     const uint32_t z = 0;
-    asm volatile("tcgen05.st.sync.aligned.32x32b.x1.b32 [%0], {%1};" ::"r"(taddr), "r"(z) : "memory");
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, "
+        "%1};" ::"r"(taddr),
+        "r"(z)
+        : "memory");
 }
 
 __device__ __forceinline__ void wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
@@ -197,7 +222,7 @@ struct RowOps {
     bool two;
     __device__ __forceinline__ RowOps(uint32_t dacc, uint64_t ad0, uint64_t bd0, int c) {
         if constexpr (L < 4) {
-            two = c > kDepth - 3;
+            two = c > kDepth - 3;  // the window of three slots wraps
             d1 = dacc + 32 * c;
             d2 = dacc;
             i1 = c <= kDepth - 3 ? idesc(96) : (c == kDepth - 2 ? idesc(64) : idesc(32));
@@ -338,6 +363,238 @@ __device__ __forceinline__ void tile_rows(const FusedArgs &a, int tile, int *lo,
     }
 }
 
+// Barriers of layer l (1-based): input-row buffers of layer l (full: written by the producer
+// warpgroup, empty: released by layer l's MMAs) and accumulator ring slots (full: the slot's row
+// has all its contributions, empty: its epilogue has read and zeroed it).
+struct Bars {
+    uint32_t base;  // shared-memory address of barrier 0
+    __device__ __forceinline__ uint32_t xfull(int l, int b) const { return base + 8u * (bar_base(l) + b); }
+    __device__ __forceinline__ uint32_t xempty(int l, int b) const { return base + 8u * (bar_base(l) + kNBuf + b); }
+    __device__ __forceinline__ uint32_t afull(int l, int j) const { return base + 8u * (bar_base(l) + 2 * kNBuf + j); }
+    __device__ __forceinline__ uint32_t aempty(int l, int j) const {
+        return base + 8u * (bar_base(l) + 2 * kNBuf + depth_of(l) + j);
+    }
+};
+
+// Byte offset of input row buffer b of layer l (1-based).
+__host__ __device__ constexpr uint32_t xbuf(int l, int b) {
+    return l == 1 ? kOffX0 + (uint32_t)b * kRowX0 : kOffX + ((uint32_t)(l - 2) * kNBuf + b) * kRowX;
+}
+
+// Phase parity of each barrier of a ring, one bit per barrier: wait on the bit, then flip it.
+__device__ __forceinline__ uint32_t take(uint32_t &bits, int i) {
+    const uint32_t p = (bits >> i) & 1u;
+    bits ^= 1u << i;
+    return p;
+}
+
+// Layer-specific MMAs of one input row, issued by one elected lane.
+template <int L>
+__device__ __forceinline__ void issue_row(uint32_t dacc, uint64_t ad0, uint64_t bd0, int c, uint32_t sbase, bool top,
+                                          bool bot, int oslot) {
+    const RowOps<L> ops(dacc, ad0, bd0, c);
+    if (elect_one()) {
+        tc_fence_after();
+        ops.issue();
+        if (top) issue_pole<L>(dacc, ad0, sbase, true, 0);
+        if (bot) issue_pole<L>(dacc, ad0, sbase, false, oslot);
+    }
+}
+
+// MMA warp of layer L: for each input row s, wait for the row and for the ring slot it starts (row
+// s+1's, last used by row s+1-D), issue, then commit to the row buffer's release and to "row s-1
+// complete". One loop for all four layers; only the issue differs.
+__device__ void mma_agent(const int L, const FusedArgs &a, const Bars &bars, uint32_t tmem, uint32_t sbase, Waiter &wt,
+                          volatile int *s_fail) {
+    const int D = depth_of(L);
+    const int nt = a.g.nt;
+    const uint32_t row_step = (L == 1 ? kRowX0 : kRowX) >> 4;  // descriptor units between buffers
+    const uint32_t dacc = tmem + acc_col(L - 1);
+    const uint64_t adb = make_desc(sbase + xbuf(L, 0), kPlane, 128);
+    const uint64_t bd0 = L < 4 ? make_desc(sbase + (L == 1 ? kOffB1 : (L == 2 ? kOffB2 : kOffB3)), kBChunk, 128)
+                               : make_desc(sbase + kOffB4, kB4Chunk, 128);
+    auto slot = [D](int r) { return D == kDepth ? ring<kDepth>(r) : ring<kDepth4>(r); };
+    uint32_t xph = 0, eph = 0;
+    for (int tile = blockIdx.x; tile < a.ntiles && !*s_fail; tile += gridDim.x) {
+        int lo[5], hi[5], strip, f;
+        tile_rows(a, tile, lo, hi, strip, f);
+        const int R0 = lo[L - 1], H = hi[L - 1];
+        const bool top_ok = lo[L] == 0, bot_ok = hi[L] == nt;
+        const int oslot = slot(nt - 1);
+        for (int s = R0; s < H && !*s_fail; ++s) {
+            const int b = s & (kNBuf - 1);
+            wt.wait(bars.xfull(L, b), take(xph, b));
+            if (s + 1 - D >= R0 - 1) {
+                const int j = slot(s + 1);
+                wt.wait(bars.aempty(L, j), take(eph, j));
+            }
+            const int c = slot(s - 1);
+            const uint64_t ad0 = adb + (uint64_t)((uint32_t)b * row_step);
+            const bool top = s == 1 && top_ok, bot = s == nt - 2 && bot_ok;
+            if (!*s_fail) {
+                switch (L) {
+                    case 1: issue_row<1>(dacc, ad0, bd0, c, sbase, top, bot, oslot); break;
+                    case 2: issue_row<2>(dacc, ad0, bd0, c, sbase, top, bot, oslot); break;
+                    case 3: issue_row<3>(dacc, ad0, bd0, c, sbase, top, bot, oslot); break;
+                    default: issue_row<4>(dacc, ad0, bd0, c, sbase, top, bot, oslot); break;
+                }
+                __syncwarp();
+                if (elect_one()) {
+                    commit(bars.xempty(L, b));
+                    commit(bars.afull(L, c));
+                }
+            }
+            __syncwarp();
+        }
+        // rows H-1 and H are complete with the last row's MMAs
+        if (!*s_fail && elect_one()) {
+            commit(bars.afull(L, slot(H - 1)));
+            commit(bars.afull(L, slot(H)));
+        }
+        __syncwarp();
+        // the epilogue of the slots the next tile starts on
+        for (int r = max(R0 - 1, H - D + 1); r <= H; ++r) {
+            const int j = slot(r);
+            wt.wait(bars.aempty(L, j), take(eph, j));
+        }
+        tc_fence_after();
+    }
+}
+
+// One code copy serves the three warpgroups (L is a runtime value): the epilogue is the largest
+// code of the kernel, and three instantiations cost instruction-cache misses.
+__device__ void epi_agent(const int L, const FusedArgs &a, const Bars &bars, uint8_t *smem, uint32_t tl, int lane,
+                          const float *bias, Waiter &wt, volatile int *s_fail) {
+    constexpr int D = kDepth;
+    uint32_t aph = 0, pph = 0, used = 0;
+    const float *bl_ = bias + 32 * (L - 1);
+    for (int tile = blockIdx.x; tile < a.ntiles && !*s_fail; tile += gridDim.x) {
+        int lo[5], hi[5], strip, f;
+        tile_rows(a, tile, lo, hi, strip, f);
+        for (int r = lo[L - 1] - 1; r <= hi[L - 1] && !*s_fail; ++r) {
+            const int j = ring<D>(r);
+            wt.wait(bars.afull(L, j), take(aph, j));
+            tc_fence_after();
+            const uint32_t ta = tl + acc_col(L - 1) + 32 * j;
+            uint32_t v[32];
+            tld32(ta, v);
+            wait_ld();
+#pragma unroll
+            for (int k = 0; k < 32; ++k) pin(v[k]);
+            tzero32(ta);
+            wait_st();
+            tc_fence_before();
+            mbar_arrive(bars.aempty(L, j));  // the slot is free before the GELUs run
+            if (r >= lo[L] && r < hi[L]) {
+                const int bx = r & (kNBuf - 1);
+                if ((used >> bx) & 1u) wt.wait(bars.xempty(L + 1, bx), ((pph >> bx) & 1u) ^ 1u);  // previous row consumed
+                used |= 1u << bx;
+                pph ^= 1u << bx;
+                uint8_t *dst = smem + xbuf(L + 1, bx) + (lane + 1) * 16;
+#pragma unroll
+                for (int pl = 0; pl < 4; ++pl) {
+                    uint4 o;
+                    uint32_t *ow = reinterpret_cast<uint32_t *>(&o);
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const int c = pl * 8 + 2 * e;
+                        const float2 y = __fadd2_rn(make_float2(__uint_as_float(v[c]), __uint_as_float(v[c + 1])),
+                                                    make_float2(bl_[c], bl_[c + 1]));
+                        const float2 gy = gelu2(y);
+                        ow[e] = pack2(gy.x, gy.y);
+                    }
+                    *reinterpret_cast<uint4 *>(dst + pl * kPlane) = o;
+                }
+                fence_async_smem();
+                mbar_arrive(bars.xfull(L + 1, bx));
+            }
+        }
+    }
+}
+
+// The lane's column in the field and whether it is one of the strip's output columns.
+struct LaneCol {
+    int col, cw, ce;
+    bool out;
+    __device__ __forceinline__ LaneCol(int strip, int lane, int np) {
+        const int xcol = strip * kOut - kHalo + lane;  // before wrap
+        col = ((xcol % np) + np) % np;
+        out = lane >= kHalo && lane < kHalo + kOut && strip * kOut + (lane - kHalo) < np;
+        cw = col == 0 ? np - 1 : col - 1;
+        ce = col + 1 == np ? 0 : col + 1;
+    }
+};
+
+// Warpgroup 3: the features of every input row of layer 1, each row's inputs loaded a row ahead.
+__device__ void feature_agent(const FusedArgs &a, const Bars &bars, uint8_t *smem, int lane, Waiter &wt,
+                              volatile int *s_fail) {
+    const int nt = a.g.nt;
+    uint32_t pph = 0, used = 0;
+    for (int tile = blockIdx.x; tile < a.ntiles && !*s_fail; tile += gridDim.x) {
+        int lo[5], hi[5], strip, f;
+        tile_rows(a, tile, lo, hi, strip, f);
+        const Field &fd = a.fs.f[f];
+        const LaneCol lc(strip, lane, a.g.np);
+        FeatIn pre;
+        if (hi[0] > lo[0]) feat_load(pre, lo[0], nt, fd, a.g, lc.col, lc.cw, lc.ce);
+        for (int srow = lo[0]; srow < hi[0] && !*s_fail; ++srow) {
+            const int b = srow & (kNBuf - 1);
+            if ((used >> b) & 1u) wt.wait(bars.xempty(1, b), ((pph >> b) & 1u) ^ 1u);
+            used |= 1u << b;
+            pph ^= 1u << b;
+            feat_store(pre, fd, a.g, smem + xbuf(1, b), lane);
+            fence_async_smem();
+            mbar_arrive(bars.xfull(1, b));
+            if (srow + 1 < hi[0]) feat_load(pre, srow + 1, nt, fd, a.g, lc.col, lc.cw, lc.ce);
+        }
+    }
+}
+
+// Warpgroup 4: the layer-4 epilogue (output rows: y and the thickness update).
+__device__ void output_agent(const FusedArgs &a, const Bars &bars, uint8_t *smem, uint32_t tl, int lane,
+                             const float *bias, Waiter &wt, volatile int *s_fail) {
+    const int nt = a.g.nt, np = a.g.np;
+    uint32_t aph = 0;
+    float *prev = reinterpret_cast<float *>(smem + kOffPrev) + lane;  // [column][lane]
+    for (int j = 0; j < kDepth4; ++j) prev[j * kLanes] = 0.f;
+    for (int tile = blockIdx.x; tile < a.ntiles && !*s_fail; tile += gridDim.x) {
+        int lo[5], hi[5], strip, f;
+        tile_rows(a, tile, lo, hi, strip, f);
+        const Field &fd = a.fs.f[f];
+        const LaneCol lc(strip, lane, np);
+        for (int r = lo[3] - 1; r <= hi[3] && !*s_fail; ++r) {
+            const bool emit = r >= lo[4] && r < hi[4] && lc.out;
+            float hout = 0.f;
+            if (emit && a.h_out) hout = fd.h[(size_t)r * fd.pitch + lc.col];
+            const int j = ring<kDepth4>(r);
+            wt.wait(bars.afull(4, j), take(aph, j));
+            tc_fence_after();
+            uint32_t yv = tld1(tl + acc_col(3) + j);
+            wait_ld();
+            pin(yv);
+            const float sum = __uint_as_float(yv), acc = __fsub_rn(sum, prev[j * kLanes]);
+            prev[j * kLanes] = sum;
+            if (r == hi[3]) {
+                // every MMA of the tile has completed: restart the ring from zero
+                tzero16(tl + acc_col(3));
+                wait_st();
+                for (int k = 0; k < kDepth4; ++k) prev[k * kLanes] = 0.f;
+            }
+            tc_fence_before();
+            mbar_arrive(bars.aempty(4, j));
+            const float y = __fadd_rn(acc, bias[96]);
+            if (emit) {
+                if (a.y_out) a.y_out[((size_t)f * nt + r) * np + lc.col] = y;
+                if (a.h_out) {
+                    float o = hout;
+                    if (r > 0 && r + 1 < nt) o = fmaxf(__fadd_rn(hout, __fmul_rn(fd.kout, y)), 0.f);
+                    a.h_out[(size_t)r * a.pitch_out + lc.col] = o;
+                }
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kThreads, 1) fused_kernel(FusedArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kOffBar);
@@ -346,18 +603,8 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(FusedArgs a) {
     volatile int *s_fail = reinterpret_cast<volatile int *>(s_tmem + 1);
     const int tid = threadIdx.x, warp = tid >> 5;
     const int grp = tid >> 7, lane = tid & (kLanes - 1);
-    const int nt = a.g.nt, np = a.g.np;
     const uint32_t sbase = smem_u32(smem);
-    // barriers of layer l (1-based): input-row buffers of layer l (full: written by the producer
-    // warpgroup, empty: released by layer l's MMAs) and accumulator ring slots (full: the slot's row
-    // has all its contributions, empty: its epilogue has read and zeroed it)
-    auto xfull = [&](int l, int b) { return smem_u32(bar + bar_base(l) + b); };
-    auto xempty = [&](int l, int b) { return smem_u32(bar + bar_base(l) + kNBuf + b); };
-    auto afull = [&](int l, int j) { return smem_u32(bar + bar_base(l) + 2 * kNBuf + j); };
-    auto aempty = [&](int l, int j) { return smem_u32(bar + bar_base(l) + 2 * kNBuf + depth_of(l) + j); };
-    auto xbuf = [&](int l, int b) {  // input row buffer b of layer l
-        return l == 1 ? kOffX0 + (uint32_t)b * kRowX0 : kOffX + ((uint32_t)(l - 2) * kNBuf + b) * kRowX;
-    };
+    const Bars bars{smem_u32(bar)};
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(s_tmem)));
@@ -366,12 +613,12 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(FusedArgs a) {
     if (tid == 0) {
         for (int l = 1; l <= 4; ++l) {
             for (int b = 0; b < kNBuf; ++b) {
-                asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(xfull(l, b)), "r"(kLanes));
-                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(xempty(l, b)));
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bars.xfull(l, b)), "r"(kLanes));
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bars.xempty(l, b)));
             }
             for (int j = 0; j < depth_of(l); ++j) {
-                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(afull(l, j)));
-                asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(aempty(l, j)), "r"(kLanes));
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bars.afull(l, j)));
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bars.aempty(l, j)), "r"(kLanes));
             }
         }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(drain));
@@ -399,208 +646,17 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(FusedArgs a) {
     __syncthreads();
     tc_fence_after();
 
-    if (tid >= kEpi) {
-        // ================= MMA warp of layer l: for each input row s, wait for the row and for the
-        // ring slot it starts (row s+1's, last used by row s+1-depth), issue, then commit to the row
-        // buffer's release and to "row s-1 complete"
-        const int l = ((tid - kEpi) >> 5) + 1;
-        const int D = depth_of(l);
-        uint32_t use[kNBuf] = {0, 0, 0}, ce[kDepth4];
-        for (int j = 0; j < kDepth4; ++j) ce[j] = 0;
-        const uint32_t dacc = tmem + acc_col(l - 1);
-        uint64_t adb[kNBuf];
-        for (int b = 0; b < kNBuf; ++b) adb[b] = make_desc(sbase + xbuf(l, b), kPlane, 128);
-        const uint64_t bd0 = l < 4 ? make_desc(sbase + (l == 1 ? kOffB1 : (l == 2 ? kOffB2 : kOffB3)), kBChunk, 128)
-                                   : make_desc(sbase + kOffB4, kB4Chunk, 128);
-        for (int tile = blockIdx.x; tile < a.ntiles && !*s_fail; tile += gridDim.x) {
-            int lo[5], hi[5], strip, f;
-            tile_rows(a, tile, lo, hi, strip, f);
-            const int L = lo[l - 1], H = hi[l - 1];
-            const bool top_ok = lo[l] == 0, bot_ok = hi[l] == nt;
-            for (int s = L; s < H && !*s_fail; ++s) {
-                const int b = s % kNBuf;
-                wt.wait(xfull(l, b), use[b]++);
-                if (s + 1 - D >= L - 1) {
-                    const int j = (s + 1) & (D - 1);
-                    wt.wait(aempty(l, j), ce[j]++);
-                }
-                {
-                    const int c = (s - 1) & (D - 1);
-                    const uint64_t ad0 = b == 0 ? adb[0] : (b == 1 ? adb[1] : adb[2]);
-                    const bool top = s == 1 && top_ok, bot = s == nt - 2 && bot_ok;
-                    const int oslot = (nt - 1) & (D - 1);
-                    const bool go = !*s_fail;
-                    switch (l) {
-                        case 1: {
-                            const RowOps<1> ops(dacc, ad0, bd0, c);
-                            if (go && elect_one()) {
-                                tc_fence_after();
-                                ops.issue();
-                                if (top) issue_pole<1>(dacc, ad0, sbase, true, 0);
-                                if (bot) issue_pole<1>(dacc, ad0, sbase, false, oslot);
-                                commit(xempty(l, b));
-                                commit(afull(l, c));
-                            }
-                            break;
-                        }
-                        case 2: {
-                            const RowOps<2> ops(dacc, ad0, bd0, c);
-                            if (go && elect_one()) {
-                                tc_fence_after();
-                                ops.issue();
-                                if (top) issue_pole<2>(dacc, ad0, sbase, true, 0);
-                                if (bot) issue_pole<2>(dacc, ad0, sbase, false, oslot);
-                                commit(xempty(l, b));
-                                commit(afull(l, c));
-                            }
-                            break;
-                        }
-                        case 3: {
-                            const RowOps<3> ops(dacc, ad0, bd0, c);
-                            if (go && elect_one()) {
-                                tc_fence_after();
-                                ops.issue();
-                                if (top) issue_pole<3>(dacc, ad0, sbase, true, 0);
-                                if (bot) issue_pole<3>(dacc, ad0, sbase, false, oslot);
-                                commit(xempty(l, b));
-                                commit(afull(l, c));
-                            }
-                            break;
-                        }
-                        default: {
-                            const RowOps<4> ops(dacc, ad0, bd0, c);
-                            if (go && elect_one()) {
-                                tc_fence_after();
-                                ops.issue();
-                                if (top) issue_pole<4>(dacc, ad0, sbase, true, 0);
-                                if (bot) issue_pole<4>(dacc, ad0, sbase, false, oslot);
-                                commit(xempty(l, b));
-                                commit(afull(l, c));
-                            }
-                            break;
-                        }
-                    }
-                }
-                __syncwarp();
-            }
-            // rows H-1 and H are complete with the last row's MMAs
-            if (!*s_fail && elect_one()) {
-                commit(afull(l, (H - 1) & (D - 1)));
-                commit(afull(l, H & (D - 1)));
-            }
-            __syncwarp();
-            // the epilogue of the slots the next tile starts on
-            for (int r = max(L - 1, H - D + 1); r <= H; ++r) {
-                const int j = r & (D - 1);
-                wt.wait(aempty(l, j), ce[j]++);
-            }
-            tc_fence_after();
-        }
+    if (tid >= kOutT) {
+        mma_agent(((tid - kOutT) >> 5) + 1, a, bars, tmem, sbase, wt, s_fail);
         // completes when every MMA this warp issued has finished
         if (elect_one()) commit(drain);
         __syncwarp();
     } else if (grp < 3) {
-        // ================= epilogue of layer l = grp + 1, producer of layer l+1's input rows
-        const int l = grp + 1;
-        uint32_t ca[kDepth] = {0, 0, 0, 0}, fills[kNBuf] = {0, 0, 0};
-        for (int tile = blockIdx.x; tile < a.ntiles && !*s_fail; tile += gridDim.x) {
-            int lo[5], hi[5], strip, f;
-            tile_rows(a, tile, lo, hi, strip, f);
-            for (int r = lo[l - 1] - 1; r <= hi[l - 1] && !*s_fail; ++r) {
-                const int j = r & (kDepth - 1);
-                wt.wait(afull(l, j), ca[j]++);
-                tc_fence_after();
-                const uint32_t ta = tl + acc_col(l - 1) + 32 * j;
-                uint32_t v[32];
-                tld32(ta, v);
-                wait_ld();
-#pragma unroll
-                for (int k = 0; k < 32; ++k) pin(v[k]);
-                tzero32(ta);  // completes while the GELUs run (waited below)
-                if (r >= lo[l] && r < hi[l]) {
-                    const int bx = r % kNBuf;
-                    if (fills[bx] > 0) wt.wait(xempty(l + 1, bx), fills[bx] - 1);  // previous row consumed
-                    const float *bl_ = bias + 32 * (l - 1);
-                    uint8_t *dst = smem + xbuf(l + 1, bx) + (lane + 1) * 16;
-#pragma unroll
-                    for (int pl = 0; pl < 4; ++pl) {
-                        uint4 o;
-                        uint32_t *ow = reinterpret_cast<uint32_t *>(&o);
-#pragma unroll
-                        for (int e = 0; e < 4; ++e) {
-                            const int c = pl * 8 + 2 * e;
-                            const float2 y = __fadd2_rn(make_float2(__uint_as_float(v[c]), __uint_as_float(v[c + 1])),
-                                                        make_float2(bl_[c], bl_[c + 1]));
-                            const float2 gy = gelu2(y);
-                            ow[e] = pack2(gy.x, gy.y);
-                        }
-                        *reinterpret_cast<uint4 *>(dst + pl * kPlane) = o;
-                    }
-                    fills[bx]++;
-                    fence_async_smem();
-                    mbar_arrive(xfull(l + 1, bx));
-                }
-                wait_st();
-                tc_fence_before();
-                mbar_arrive(aempty(l, j));
-            }
-        }
+        epi_agent(grp + 1, a, bars, smem, tl, lane, bias, wt, s_fail);
+    } else if (grp == 3) {
+        feature_agent(a, bars, smem, lane, wt, s_fail);
     } else {
-        // ================= warpgroup 3: features (input rows of layer 1), running 8 rows ahead of the
-        // layer-4 epilogue (output rows)
-        uint32_t ca[kDepth4], fills[kNBuf] = {0, 0, 0};
-        for (int j = 0; j < kDepth4; ++j) ca[j] = 0;
-        for (int tile = blockIdx.x; tile < a.ntiles && !*s_fail; tile += gridDim.x) {
-            int lo[5], hi[5], strip, f;
-            tile_rows(a, tile, lo, hi, strip, f);
-            const Field &fd = a.fs.f[f];
-            const int xcol = strip * kOut - kHalo + lane;  // this lane's column (before wrap)
-            const int col = ((xcol % np) + np) % np;
-            const bool lane_out = lane >= kHalo && lane < kHalo + kOut && strip * kOut + (lane - kHalo) < np;
-            const int cw = col == 0 ? np - 1 : col - 1, ce_ = col + 1 == np ? 0 : col + 1;
-            constexpr int kLead = 8;
-            const int nfeat = hi[0] - lo[0], nepi = hi[3] - lo[3] + 2;
-            FeatIn pre;
-            if (nfeat > 0) feat_load(pre, lo[0], nt, fd, a.g, col, cw, ce_);
-            float hout = 0.f;
-            for (int t = 0; t < max(nfeat, nepi + kLead) && !*s_fail; ++t) {
-                if (t < nfeat) {
-                    const int srow = lo[0] + t, b = srow % kNBuf;
-                    if (fills[b] > 0) wt.wait(xempty(1, b), fills[b] - 1);
-                    feat_store(pre, fd, a.g, smem + xbuf(1, b), lane);
-                    fills[b]++;
-                    fence_async_smem();
-                    mbar_arrive(xfull(1, b));
-                    if (t + 1 < nfeat) feat_load(pre, srow + 1, nt, fd, a.g, col, cw, ce_);
-                }
-                const int te = t - kLead;
-                if (te >= 0 && te < nepi) {
-                    const int r = lo[3] - 1 + te;
-                    const bool emit = r >= lo[4] && r < hi[4];
-                    if (emit && lane_out) hout = fd.h[(size_t)r * fd.pitch + col];
-                    const int j = r & (kDepth4 - 1);
-                    wt.wait(afull(4, j), ca[j]++);
-                    tc_fence_after();
-                    const uint32_t ta = tl + acc_col(3) + j;
-                    uint32_t yv = tld1(ta);
-                    wait_ld();
-                    pin(yv);
-                    tzero1(ta);
-                    const float y = __fadd_rn(__uint_as_float(yv), bias[96]);
-                    if (emit && lane_out) {
-                        if (a.y_out) a.y_out[((size_t)f * nt + r) * np + col] = y;
-                        if (a.h_out) {
-                            float o = hout;
-                            if (r > 0 && r + 1 < nt) o = fmaxf(__fadd_rn(hout, __fmul_rn(fd.kout, y)), 0.f);
-                            a.h_out[(size_t)r * a.pitch_out + col] = o;
-                        }
-                    }
-                    wait_st();
-                    tc_fence_before();
-                    mbar_arrive(aempty(4, j));
-                }
-            }
-        }
+        output_agent(a, bars, smem, tl, lane, bias, wt, s_fail);
     }
     __syncthreads();
     // no MMA may still write the accumulators when the columns are released
@@ -731,6 +787,7 @@ int fused_forward(sbs_surrogate *s, const Fields &fields, int nf, const GridTab 
             best_nrb = nrb;
         }
     }
+    best_nrb = std::max(best_nrb, (g.nt + kMaxTileRows - 1) / kMaxTileRows);
     a.nrb = best_nrb;
     a.rows_per_block = (g.nt + best_nrb - 1) / best_nrb;
     a.nrb = (g.nt + a.rows_per_block - 1) / a.rows_per_block;
