@@ -398,7 +398,7 @@ int sbs_spectral_rgb(const float *t_nm, const float *cos_i, const float *n_film,
 /* ------------------------------------------------------------------ */
 /* Drainage surrogate: conv neural operator over SBS_NN_STEPS passes   */
 /* ------------------------------------------------------------------ */
-/* The network, its features, parameter layout and GELU are defined in
+/* The network, its features, parameter layout and activation are defined in
  * sbs_nn.h. The surrogate approximates SBS_NN_STEPS WGSL-semantics passes
  * (drainage.wgsl:72-202 with marangoni_enabled = 0, where the surfactant does
  * not feed back into the thickness) and is trained here, on this GPU, on

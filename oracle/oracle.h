@@ -173,9 +173,9 @@ double orc_nn_loss_grad(const float *params, uint32_t nb, uint32_t nt, uint32_t 
 void orc_nn_apply(const float *h, const float *y, uint32_t nt, uint32_t np, float kout, float *h_out);
 /* 1: drop every BF16 / float rounding (all-double network), for finite-difference checks */
 void orc_nn_set_exact(int exact);
-/* gelu and its derivative in the FP32 form of include/sbs_nn.h */
-float orc_nn_gelu(float x);
-float orc_nn_gelu_grad(float x);
+/* the hard-swish activation and its derivative in the FP32 form of include/sbs_nn.h */
+float orc_nn_act(float x);
+float orc_nn_act_grad(float x);
 
 #ifdef __cplusplus
 }

@@ -107,9 +107,9 @@ _SIGS = {
     "orc_nn_forward": ([_P, _U32, _U32, _U32, _P, _P], None),
     "orc_nn_loss_grad": ([_P, _U32, _U32, _U32, _P, _P, _P], _D),
     "orc_nn_apply": ([_P, _P, _U32, _U32, _F, _P], None),
-    "orc_nn_gelu": ([_F], _F),
+    "orc_nn_act": ([_F], _F),
     "orc_nn_set_exact": ([_I], None),
-    "orc_nn_gelu_grad": ([_F], _F),
+    "orc_nn_act_grad": ([_F], _F),
 }
 
 
@@ -397,9 +397,9 @@ def nn_set_exact(exact: bool) -> None:
     lib().orc_nn_set_exact(1 if exact else 0)
 
 
-def nn_gelu(x: float) -> float:
-    return float(lib().orc_nn_gelu(float(x)))
+def nn_act(x: float) -> float:
+    return float(lib().orc_nn_act(float(x)))
 
 
-def nn_gelu_grad(x: float) -> float:
-    return float(lib().orc_nn_gelu_grad(float(x)))
+def nn_act_grad(x: float) -> float:
+    return float(lib().orc_nn_act_grad(float(x)))

@@ -4,8 +4,8 @@
 //
 // Arithmetic: every convolution sums in double over operands rounded to BF16 exactly where the
 // CUDA path rounds them (features, weights, activations, per-layer output gradients); values the
-// CUDA path keeps in FP32 (pre-activations, the layer-4 gradient, input gradients before the GELU
-// derivative) are rounded to float here too. The remaining difference to the GPU is the order of
+// CUDA path keeps in FP32 (pre-activations, the layer-4 gradient, input gradients before the
+// activation derivative) are rounded to float here too. The remaining difference to the GPU is the order of
 // FP32 accumulation inside the tensor-core sums.
 //
 // The surrogate has no counterpart in the reference; what it approximates is the WGSL drainage
@@ -41,19 +41,15 @@ int g_exact = 0;
 inline double rb(double v) { return g_exact ? v : (double)bf16r((float)v); }
 inline double rf(double v) { return g_exact ? v : (double)(float)v; }
 
-double gelu_d(double x) {
-    const double t = std::fmin(std::fmax(x, -3.0), 3.0), u = t * t;
-    const double p = (((SBS_NN_Q4 * u + SBS_NN_Q3) * u + SBS_NN_Q2) * u + SBS_NN_Q1) * u + SBS_NN_Q0;
-    return x * (0.5 + t * p);
+// hard-swish of include/sbs_nn.h in double (exact mode)
+double act_d(double x) {
+    const double s = std::fmin(std::fmax(x * (double)SBS_NN_HS_SLOPE + 0.5, 0.0), 1.0);
+    return x * s;
 }
 
-double gelu_grad_d(double x) {
-    const double t = std::fmin(std::fmax(x, -3.0), 3.0), u = t * t;
-    const double p = (((SBS_NN_Q4 * u + SBS_NN_Q3) * u + SBS_NN_Q2) * u + SBS_NN_Q1) * u + SBS_NN_Q0;
-    const double dp = ((4.0 * (double)SBS_NN_Q4 * u + 3.0 * (double)SBS_NN_Q3) * u + 2.0 * (double)SBS_NN_Q2) * u +
-                      (double)SBS_NN_Q1;
-    const double dphi = std::fabs(x) < 3.0 ? p + 2.0 * u * dp : 0.0;
-    return (0.5 + t * p) + x * dphi;
+double act_grad_d(double x) {
+    const double r = x * (double)SBS_NN_HS_SLOPE + 0.5;
+    return r <= 0.0 ? 0.0 : (r >= 1.0 ? 1.0 : r + x * (double)SBS_NN_HS_SLOPE);
 }
 
 struct Grid {
@@ -112,24 +108,15 @@ inline uint32_t refl(int64_t i, uint32_t nt) {
     return (uint32_t)i;
 }
 
-float gelu_f(float x) {
-    const float t = std::fmin(std::fmax(x, -3.f), 3.f);
-    const float u = t * t;
-    const float p = std::fma(std::fma(std::fma(std::fma(SBS_NN_Q4, u, SBS_NN_Q3), u, SBS_NN_Q2), u, SBS_NN_Q1),
-                             u, SBS_NN_Q0);
-    const float phi = std::fma(t, p, 0.5f);
-    return x * phi;
-}
+// sat() of include/sbs_nn.h: clamp to [0, 1], NaN -> 0
+inline float sat01(float r) { return r > 0.f ? (r < 1.f ? r : 1.f) : 0.f; }
 
-float gelu_grad_f(float x) {
-    const float t = std::fmin(std::fmax(x, -3.f), 3.f);
-    const float u = t * t;
-    const float p = std::fma(std::fma(std::fma(std::fma(SBS_NN_Q4, u, SBS_NN_Q3), u, SBS_NN_Q2), u, SBS_NN_Q1),
-                             u, SBS_NN_Q0);
-    const float phi = std::fma(t, p, 0.5f);
-    const float dp = std::fma(std::fma(std::fma(SBS_NN_Q4X4, u, SBS_NN_Q3X3), u, SBS_NN_Q2X2), u, SBS_NN_Q1);
-    const float dphi = std::fabs(x) < 3.f ? std::fma(u + u, dp, p) : 0.f;
-    return std::fma(x, dphi, phi);
+// hard-swish and its derivative in the FP32 operation order of include/sbs_nn.h
+float act_f(float x) { return x * sat01(std::fma(x, SBS_NN_HS_SLOPE, 0.5f)); }
+
+float act_grad_f(float x) {
+    const float r = std::fma(x, SBS_NN_HS_SLOPE, 0.5f), s = sat01(r);
+    return (r > 0.f && r < 1.f) ? std::fma(x, SBS_NN_HS_SLOPE, s) : s;
 }
 
 struct Layer {
@@ -189,7 +176,7 @@ void forward(const std::vector<Layer> &L, const float *x, uint32_t nb, uint32_t 
         if (l < 3) {
             F.a[l].resize(F.y[l].size());
             for (size_t k = 0; k < F.y[l].size(); ++k)
-                F.a[l][k] = g_exact ? gelu_d(F.y[l][k]) : (double)bf16r(gelu_f((float)F.y[l][k]));
+                F.a[l][k] = g_exact ? act_d(F.y[l][k]) : (double)bf16r(act_f((float)F.y[l][k]));
             in = F.a[l].data();
         }
     }
@@ -245,8 +232,8 @@ extern "C" {
 
 void orc_nn_set_exact(int exact) { g_exact = exact ? 1 : 0; }
 
-float orc_nn_gelu(float x) { return gelu_f(x); }
-float orc_nn_gelu_grad(float x) { return gelu_grad_f(x); }
+float orc_nn_act(float x) { return act_f(x); }
+float orc_nn_act_grad(float x) { return act_grad_f(x); }
 
 float orc_nn_kout(const orc_wgsl_params *p) { return field_consts(p).kout; }
 
@@ -315,11 +302,11 @@ double orc_nn_loss_grad(const float *params, uint32_t nb, uint32_t nt, uint32_t 
         for (size_t k = 0; k < dW.size(); ++k) grad[off_w[l] + k] = (float)dW[k];
         for (size_t k = 0; k < db.size(); ++k) grad[off_b[l] + k] = (float)db[k];
         if (l == 0) break;
-        // g of the layer below: bf16( float(dx) * gelu'(y) )
+        // g of the layer below: bf16( float(dx) * act'(y) )
         const std::vector<double> &yl = F.y[l - 1];
         gy.assign(dx.size(), 0.0);
         for (size_t k = 0; k < dx.size(); ++k)
-            gy[k] = g_exact ? dx[k] * gelu_grad_d(yl[k]) : (double)bf16r((float)dx[k] * gelu_grad_f((float)yl[k]));
+            gy[k] = g_exact ? dx[k] * act_grad_d(yl[k]) : (double)bf16r((float)dx[k] * act_grad_f((float)yl[k]));
     }
     return loss;
 }

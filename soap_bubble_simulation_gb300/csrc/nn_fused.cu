@@ -1,5 +1,5 @@
 // Fused forward pass of the drainage surrogate (include/sbs_nn.h) on the tcgen05 tensor cores:
-// features, the four 3x3 convolutions, GELUs and the thickness update in one persistent kernel,
+// features, the four 3x3 convolutions, activations and the thickness update in one persistent kernel,
 // activations kept in shared memory and accumulators in tensor memory.
 //
 // Tiling. A tile is a strip of 128 consecutive phi columns (lanes; the middle 120 are output, the
@@ -7,7 +7,7 @@
 // The block runs nine agents that only talk through mbarriers: four MMA warps (one per layer:
 // for each input row, wait for the row and for the accumulator slot it starts, issue, commit),
 // three epilogue warpgroups (warpgroup l-1 reads layer l's finished row from TMEM, zeroes and
-// releases the slot at once, then adds the bias, applies GELU and writes the activation row into
+// releases the slot at once, then adds the bias, applies the activation and writes the row into
 // one of four input buffers of layer l+1), a feature warpgroup (the input rows of layer 1) and an
 // output warpgroup (layer 4's rows: y and the thickness update). Every ring (activation buffers:
 // full / empty; accumulator rows: full / empty) is balanced per tile, so each waiter is at most
@@ -112,6 +112,9 @@ constexpr uint32_t kSmem = kOffPrev + kDepth4 * kLanes * 4;
 constexpr int kMaxTileRows = 256;
 static_assert(kSmem <= 227 * 1024, "shared memory per CTA");
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at 2 GHz
+// try_wait may suspend the thread until the phase completes or this many ns pass (waiting warps
+// then take no issue slots from the working ones)
+constexpr uint32_t kSuspendNs = 1000000;
 
 __host__ __device__ constexpr uint32_t idesc(int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kLanes >> 4) << 24);
@@ -151,9 +154,9 @@ __device__ __forceinline__ void commit(uint32_t bar) {
 __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
-        : "r"(bar), "r"(parity)
+        : "r"(bar), "r"(parity), "r"(kSuspendNs)
         : "memory");
     return ok != 0;
 }
@@ -484,7 +487,7 @@ __device__ void epi_agent(const int L, const FusedArgs &a, const Bars &bars, uin
             tzero32(ta);
             wait_st();
             tc_fence_before();
-            mbar_arrive(bars.aempty(L, j));  // the slot is free before the GELUs run
+            mbar_arrive(bars.aempty(L, j));  // the slot is free before the activations run
             if (r >= lo[L] && r < hi[L]) {
                 const int bx = r & (kNBuf - 1);
                 if ((used >> bx) & 1u) wt.wait(bars.xempty(L + 1, bx), ((pph >> bx) & 1u) ^ 1u);  // previous row consumed
@@ -500,7 +503,7 @@ __device__ void epi_agent(const int L, const FusedArgs &a, const Bars &bars, uin
                         const int c = pl * 8 + 2 * e;
                         const float2 y = __fadd2_rn(make_float2(__uint_as_float(v[c]), __uint_as_float(v[c + 1])),
                                                     make_float2(bl_[c], bl_[c + 1]));
-                        const float2 gy = gelu2(y);
+                        const float2 gy = act2(y);
                         ow[e] = pack2(gy.x, gy.y);
                     }
                     *reinterpret_cast<uint4 *>(dst + pl * kPlane) = o;

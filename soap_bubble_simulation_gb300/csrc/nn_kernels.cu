@@ -85,8 +85,8 @@ __global__ void features_kernel(Fields fs, GridTab g, uint4 *x) {
 }
 
 // ------------------------------------------------------------------ 3x3 convolution (mma.sync)
-// BWD = false: y = conv(x, W) + b, a = bf16(gelu(y))     (x: CIN channels, packed W [oc][tap*CIN+ic])
-// BWD = true : dX = conv^T(g, W), g_prev = bf16(dX * gelu'(y_prev))  (g: 32 channels, packed W
+// BWD = false: y = conv(x, W) + b, a = bf16(act(y))     (x: CIN channels, packed W [oc][tap*CIN+ic])
+// BWD = true : dX = conv^T(g, W), g_prev = bf16(dX * act'(y_prev))  (g: 32 channels, packed W
 //              [ic][tap*32+oc]); the transpose reads g at (i - dy, j - dx) with zero rows outside
 //              the grid, plus the reflected sources: row 1 also receives output row 0's dy = -1
 //              taps, row nt-2 output row nt-1's dy = +1 taps.
@@ -222,11 +222,11 @@ __global__ void __launch_bounds__(128) conv_kernel(ConvArgs a) {
                 if (!BWD) {
                     const float y0 = __fadd_rn(v0, a.bias[n]), y1 = __fadd_rn(v1, a.bias[n + 1]);
                     *(float2 *)(a.yout + cell * 32 + n) = make_float2(y0, y1);
-                    *(uint32_t *)(a.aout + cell * 32 + n) = pack2(gelu(y0), gelu(y1));
+                    *(uint32_t *)(a.aout + cell * 32 + n) = pack2(act(y0), act(y1));
                 } else {
                     const float2 yp = *(const float2 *)(a.yprev + cell * 32 + n);
                     *(uint32_t *)(a.aout + cell * 32 + n) =
-                        pack2(__fmul_rn(v0, gelu_grad(yp.x)), __fmul_rn(v1, gelu_grad(yp.y)));
+                        pack2(__fmul_rn(v0, act_grad(yp.x)), __fmul_rn(v1, act_grad(yp.y)));
                 }
             }
         }
@@ -459,7 +459,7 @@ __global__ void wgrad4_kernel(Wgrad4Args a) {
     if (tid < 289) a.partial[(size_t)blockIdx.x * 289 + tid] = acc;
 }
 
-// g3[cell][ic] = bf16( (sum over the taps that read `cell` of g4[out] W4[tap][ic]) * gelu'(y3) ),
+// g3[cell][ic] = bf16( (sum over the taps that read `cell` of g4[out] W4[tap][ic]) * act'(y3) ),
 // one warp per cell, lane = ic.
 struct Dgrad4Args {
     const float *g4;
@@ -487,7 +487,7 @@ __global__ void dgrad4_kernel(Dgrad4Args a) {
         if (i == 1 && dy == -1) s = __fmaf_rn(a.g4[fb + q], a.w4[t * 32 + ic], s);
         if (i == nt - 2 && dy == 1) s = __fmaf_rn(a.g4[fb + (size_t)(nt - 1) * np + q], a.w4[t * 32 + ic], s);
     }
-    a.g3[c * 32 + ic] = __float2bfloat16_rn(__fmul_rn(s, gelu_grad(a.y3[c * 32 + ic])));
+    a.g3[c * 32 + ic] = __float2bfloat16_rn(__fmul_rn(s, act_grad(a.y3[c * 32 + ic])));
 }
 
 // sum of partial rows (fixed order) scattered into the canonical parameter layout

@@ -1,25 +1,25 @@
-"""The surrogate oracle (include/sbs_nn.h restated on the CPU) pinned by analytic checks: the GELU
-polynomial against x * normal CDF, the finite-difference features against closed-form derivatives,
+"""The surrogate oracle (include/sbs_nn.h restated on the CPU) pinned by analytic checks: the
+hard-swish activation against its closed form, the finite-difference features against closed-form derivatives,
 and the backward pass against central finite differences of the forward pass (exact mode)."""
-import math
 
 import numpy as np
 import pytest
-from scipy.special import erf
 
 S2 = 1e-5
 
 
-def test_gelu_polynomial_and_derivative(orc):
+def test_hardswish_and_derivative(orc):
     xs = np.linspace(-6, 6, 241)
-    g = np.array([orc.nn_gelu(v) for v in xs])
-    gt = xs * 0.5 * (1 + erf(xs / math.sqrt(2)))
-    assert np.abs(g - gt).max() < 4.1e-3
-    assert abs(orc.nn_gelu(-3.5)) < 1e-6 and abs(orc.nn_gelu(3.5) - 3.5) < 1e-6
+    a = np.array([orc.nn_act(v) for v in xs])
+    want = xs * np.clip(xs / 6 + 0.5, 0, 1)
+    assert np.abs(a - want).max() <= 1e-6 * np.abs(xs).max()
+    assert orc.nn_act(-3.5) == 0.0 and orc.nn_act(3.5) == 3.5 and orc.nn_act(float("nan")) != orc.nn_act(float("nan"))
+    # away from the kinks at +-3 the derivative matches central differences
     pts = np.concatenate([np.linspace(-5, -3.05, 9), np.linspace(-2.95, 2.95, 31), np.linspace(3.05, 5, 9)])
-    fd = np.array([(orc.nn_gelu(v + 1e-2) - orc.nn_gelu(v - 1e-2)) / 2e-2 for v in pts])
-    gd = np.array([orc.nn_gelu_grad(v) for v in pts])
+    fd = np.array([(orc.nn_act(v + 1e-2) - orc.nn_act(v - 1e-2)) / 2e-2 for v in pts])
+    gd = np.array([orc.nn_act_grad(v) for v in pts])
     assert np.abs(fd - gd).max() < 2e-4
+    assert orc.nn_act_grad(-4.0) == 0.0 and orc.nn_act_grad(4.0) == 1.0 and orc.nn_act_grad(0.0) == 0.5
 
 
 def _params(orc, nt, np_, **kw):
