@@ -19,16 +19,18 @@
 // Convolution as MMAs. Activations of one row live in shared memory as planes of 8 channels with
 // 16 B per cell (K-major, rows of the A operand = cells, SBO = 128 B), so the dx = -1/0/+1 taps
 // are the same tile read at start offsets of 16 B apart: no im2col buffer. The three dy taps are
-// stacked along N: one M=128 x N=96 MMA multiplies an input row by [W(+1); W(0); W(-1)] and
-// accumulates into three consecutive 32-column slots of a ring of four (output rows s-1, s, s+1
-// of input row s; row r lives in slot r mod 4). Where the three slots wrap past the end of the
-// ring the MMA is split in two (N = 64 + 32 or 32 + 64). A slot is read by the epilogue once its
-// row's three input rows are in, then zeroed for reuse. theta reflection at the poles adds one
+// stacked along N: one M=128 x N=96 MMA multiplies an input row by the three dy blocks of W and
+// accumulates into a ring of three 32-column slots (output row r lives in slot r mod 3). B holds
+// the blocks as [W+1; W0; W-1; W+1; W0]; the window of three blocks that starts at (1 - s) mod 3
+// lines them up with the slots of rows s-1, s, s+1, so every input row is one N=96 MMA per K step
+// whatever its position in the ring. A slot is read by the epilogue once its row's three input
+// rows are in, then zeroed for reuse; the next row's MMAs wait for that (the ring has no spare
+// slot), and the other layers' MMAs keep the tensor pipe busy meanwhile. theta reflection at the poles adds one
 // N=32 MMA (input row 1 into output row 0 with W-1, input row nt-2 into output row nt-1 with W+1).
 // Operand bandwidth: an N=96 MMA reads 4 KB of A and 3 KB of B from shared memory (~56 cycles at
 // 128 B/clk), which is the measured issue-to-issue time of back-to-back MMAs of this shape.
 //
-// TMEM columns: layer 1 [0, 128), layer 2 [128, 256), layer 3 [256, 384), layer 4 [384, 400)
+// TMEM columns: layer 1 [0, 96), layer 2 [128, 224), layer 3 [256, 352), layer 4 [384, 400)
 // (a ring of 16 single columns; the N=16 MMA always writes columns 384..399 and B places the three
 // dy weight rows at the right columns by its window offset). Every MMA's D column is a multiple of
 // 16. One CTA per SM (it allocates all 512 columns).
@@ -73,7 +75,7 @@ constexpr int kCells = 136;                    // staged cells per plane (q = la
 constexpr uint32_t kPlane = kCells * 16;       // 2176 B
 constexpr uint32_t kRowX = 4 * kPlane;         // one 32-channel row buffer
 constexpr uint32_t kRowX0 = 2 * kPlane;        // one 16-feature row buffer
-constexpr uint32_t kBRows = 96;                // dy blocks [W+1; W0; W-1] (3 x 32 rows)
+constexpr uint32_t kBRows = 160;               // dy blocks [W+1; W0; W-1; W+1; W0] (5 x 32 rows)
 constexpr uint32_t kBChunk = kBRows * 16;      // one 8-channel K chunk
 constexpr uint32_t kBStep = 2 * kBChunk;       // one K16 step
 constexpr uint32_t kBlk = 32 * 16;             // one 32-row block
@@ -89,7 +91,7 @@ constexpr uint32_t kOffB4b = kOffB4t + 6 * kBxStep;     // W4(dy=+1) alone (bott
 constexpr uint32_t kOffBias = kOffB4b + 6 * kBxStep;    // 97 floats (padded to 128)
 constexpr uint32_t kImage = kOffBias + 128 * 4;
 // accumulator rings: layers 1-3 keep kDepth rows of 32 columns, layer 4 kDepth4 single columns
-constexpr int kDepth = 4, kDepth4 = 16;
+constexpr int kDepth = 3, kDepth4 = 16;
 __host__ __device__ constexpr int depth_of(int l) { return l < 4 ? kDepth : kDepth4; }  // l 1-based
 __host__ __device__ constexpr uint32_t acc_col(int l) { return 128u * (uint32_t)l; }    // l 0-based; 3 -> 384
 static_assert(acc_col(3) + 16 <= 512, "TMEM columns");
@@ -225,18 +227,20 @@ struct RowOps {
     bool two;
     __device__ __forceinline__ RowOps(uint32_t dacc, uint64_t ad0, uint64_t bd0, int c) {
         if constexpr (L < 4) {
-            two = c > kDepth - 3;  // the window of three slots wraps
-            d1 = dacc + 32 * c;
-            d2 = dacc;
-            i1 = c <= kDepth - 3 ? idesc(96) : (c == kDepth - 2 ? idesc(64) : idesc(32));
-            i2 = c == kDepth - 2 ? idesc(32) : idesc(64);
-            const uint64_t o2 = c == kDepth - 2 ? (2 * kBlk >> 4) : (kBlk >> 4);
+            // one N=96 MMA over the whole ring: the B window starting at block (3 - c) mod 3 of
+            // [W+1; W0; W-1; W+1; W0] puts W+1 at slot c (row s-1), W0 at slot c+1 (row s) and W-1 at
+            // slot c+2 (row s+1), mod 3
+            static_assert(kDepth == 3, "the rotated B window covers a ring of three slots");
+            two = false;
+            d1 = d2 = dacc;
+            i1 = i2 = idesc(96);
+            const uint64_t blk = (uint64_t)(((3 - c) % 3) * (kBlk >> 4));
 #pragma unroll
             for (int st = 0; st < NS; ++st) {
                 const int dxi = L == 1 ? st : st >> 1, kk = L == 1 ? 0 : st & 1;
                 ad[st] = ad0 + (uint64_t)((2 * kk * kPlane + 16 * dxi) >> 4);
-                b1[st] = bd0 + (uint64_t)((st * kBStep) >> 4);
-                b2[st] = b1[st] + o2;
+                b1[st] = bd0 + (uint64_t)((st * kBStep) >> 4) + blk;
+                b2[st] = b1[st];
             }
         } else {
             // B rows 15..17 hold W4(dy = +1, 0, -1): window start 15 - c puts them at columns c..c+2;
@@ -673,7 +677,7 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(FusedArgs a) {
 // Packs the parameter vector into the shared-memory image of fused_kernel.
 __global__ void pack_fused_kernel(const float *theta, uint8_t *img) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    const int dy_of_block[3] = {1, 0, -1};
+    const int dy_of_block[5] = {1, 0, -1, 1, 0};
     bf16 *B = reinterpret_cast<bf16 *>(img);
     // layers 1-3: element (step, chunk, row n, e8); layer 1 step = dx, chunk = 8-feature plane
     const int per1 = 3 * 2 * kBRows * 8, per23 = 6 * 2 * kBRows * 8;
