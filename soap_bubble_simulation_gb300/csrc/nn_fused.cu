@@ -342,6 +342,18 @@ __device__ __forceinline__ void tzero32(uint32_t taddr) {
         : "memory");
 }
 
+// Writes layer bias b[0..31] into the 32 columns at taddr (every lane of the warp's quarter): the
+// accumulator of a row then starts at the bias and the MMAs add onto it.
+__device__ __forceinline__ void tset_bias(uint32_t taddr, const float *b) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const float4 u = *reinterpret_cast<const float4 *>(b + 4 * k);
+        asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(taddr + 4 * k), "f"(u.x),
+                     "f"(u.y), "f"(u.z), "f"(u.w)
+                     : "memory");
+    }
+}
+
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
@@ -488,7 +500,7 @@ __device__ void epi_agent(const int L, const FusedArgs &a, const Bars &bars, uin
             wait_ld();
 #pragma unroll
             for (int k = 0; k < 32; ++k) pin(v[k]);
-            tzero32(ta);
+            tset_bias(ta, bl_);  // the slot's next row starts from the bias
             wait_st();
             tc_fence_before();
             mbar_arrive(bars.aempty(L, j));  // the slot is free before the activations run
@@ -505,9 +517,7 @@ __device__ void epi_agent(const int L, const FusedArgs &a, const Bars &bars, uin
 #pragma unroll
                     for (int e = 0; e < 4; ++e) {
                         const int c = pl * 8 + 2 * e;
-                        const float2 y = __fadd2_rn(make_float2(__uint_as_float(v[c]), __uint_as_float(v[c + 1])),
-                                                    make_float2(bl_[c], bl_[c + 1]));
-                        const float2 gy = act2(y);
+                        const float2 gy = act2(make_float2(__uint_as_float(v[c]), __uint_as_float(v[c + 1])));
                         ow[e] = pack2(gy.x, gy.y);
                     }
                     *reinterpret_cast<uint4 *>(dst + pl * kPlane) = o;
@@ -643,11 +653,18 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(FusedArgs a) {
     tc_fence_after();
     const uint32_t tmem = *s_tmem;
     const uint32_t tl = tmem + ((uint32_t)((warp & 3) * 32) << 16);  // epilogue thread's lane quarter
+    const float *bias = reinterpret_cast<const float *>(smem + kOffBias);
     if (tid < kEpi) {
-        for (int c = 128 * grp; c < 128 * grp + 128; c += 32) tzero32(tl + c);
+        // warpgroup g < 3 owns layer g+1's columns [128 g, 128 g + 128): its ring slots start at the
+        // bias; everything else (and layer 4's ring, owned by warpgroup 3 here) starts at zero
+        for (int c = 0; c < 128; c += 32) {
+            if (grp < 3 && c < 32 * kDepth)
+                tset_bias(tl + 128 * grp + c, bias + 32 * grp);
+            else
+                tzero32(tl + 128 * grp + c);
+        }
         wait_st();
     }
-    const float *bias = reinterpret_cast<const float *>(smem + kOffBias);
     Waiter wt{s_fail, a.err};
     tc_fence_before();
     __syncthreads();
