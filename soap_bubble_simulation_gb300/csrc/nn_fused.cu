@@ -371,16 +371,21 @@ struct Waiter {
     }
 };
 
-__device__ __forceinline__ void tile_rows(const FusedArgs &a, int tile, int *lo, int *hi, int &strip, int &f) {
-    strip = tile % a.nstrips;
-    const int rb = (tile / a.nstrips) % a.nrb;
-    f = tile / (a.nstrips * a.nrb);
-    const int y0 = rb * a.rows_per_block, y1 = min(a.g.nt, y0 + a.rows_per_block);
-    for (int l = 0; l <= 4; ++l) {
-        lo[l] = max(0, y0 - 4 + l);
-        hi[l] = min(a.g.nt, y1 + 4 - l);
+// Rows of one tile: the block's output rows are [y0, y1); layer l (0 = features) needs rows
+// [lo(l), hi(l)) of its input. Computed on demand (an array indexed by a runtime layer would live
+// in local memory).
+struct TileRows {
+    int y0, y1, nt, strip, f;
+    __device__ __forceinline__ TileRows(const FusedArgs &a, int tile) : nt(a.g.nt) {
+        strip = tile % a.nstrips;
+        const int rb = (tile / a.nstrips) % a.nrb;
+        f = tile / (a.nstrips * a.nrb);
+        y0 = rb * a.rows_per_block;
+        y1 = min(nt, y0 + a.rows_per_block);
     }
-}
+    __device__ __forceinline__ int lo(int l) const { return max(0, y0 - 4 + l); }
+    __device__ __forceinline__ int hi(int l) const { return min(nt, y1 + 4 - l); }
+};
 
 // Barriers of layer l (1-based): input-row buffers of layer l (full: written by the producer
 // warpgroup, empty: released by layer l's MMAs) and accumulator ring slots (full: the slot's row
@@ -407,16 +412,19 @@ __device__ __forceinline__ uint32_t take(uint32_t &bits, int i) {
     return p;
 }
 
-// Layer-specific MMAs of one input row, issued by one elected lane.
+// Layer-specific MMAs of one input row, issued by one elected lane, then the commits that release
+// the row buffer (xempty) and mark row s-1 complete (afull).
 template <int L>
 __device__ __forceinline__ void issue_row(uint32_t dacc, uint64_t ad0, uint64_t bd0, int c, uint32_t sbase, bool top,
-                                          bool bot, int oslot) {
+                                          bool bot, int oslot, uint32_t xempty, uint32_t afull) {
     const RowOps<L> ops(dacc, ad0, bd0, c);
     if (elect_one()) {
         tc_fence_after();
         ops.issue();
         if (top) issue_pole<L>(dacc, ad0, sbase, true, 0);
         if (bot) issue_pole<L>(dacc, ad0, sbase, false, oslot);
+        commit(xempty);
+        commit(afull);
     }
 }
 
@@ -435,10 +443,9 @@ __device__ void mma_agent(const int L, const FusedArgs &a, const Bars &bars, uin
     auto slot = [D](int r) { return D == kDepth ? ring<kDepth>(r) : ring<kDepth4>(r); };
     uint32_t xph = 0, eph = 0;
     for (int tile = blockIdx.x; tile < a.ntiles && !*s_fail; tile += gridDim.x) {
-        int lo[5], hi[5], strip, f;
-        tile_rows(a, tile, lo, hi, strip, f);
-        const int R0 = lo[L - 1], H = hi[L - 1];
-        const bool top_ok = lo[L] == 0, bot_ok = hi[L] == nt;
+        const TileRows tr(a, tile);
+        const int R0 = tr.lo(L - 1), H = tr.hi(L - 1);
+        const bool top_ok = tr.lo(L) == 0, bot_ok = tr.hi(L) == nt;
         const int oslot = slot(nt - 1);
         for (int s = R0; s < H && !*s_fail; ++s) {
             const int b = s & (kNBuf - 1);
@@ -451,16 +458,12 @@ __device__ void mma_agent(const int L, const FusedArgs &a, const Bars &bars, uin
             const uint64_t ad0 = adb + (uint64_t)((uint32_t)b * row_step);
             const bool top = s == 1 && top_ok, bot = s == nt - 2 && bot_ok;
             if (!*s_fail) {
+                const uint32_t xe = bars.xempty(L, b), af = bars.afull(L, c);
                 switch (L) {
-                    case 1: issue_row<1>(dacc, ad0, bd0, c, sbase, top, bot, oslot); break;
-                    case 2: issue_row<2>(dacc, ad0, bd0, c, sbase, top, bot, oslot); break;
-                    case 3: issue_row<3>(dacc, ad0, bd0, c, sbase, top, bot, oslot); break;
-                    default: issue_row<4>(dacc, ad0, bd0, c, sbase, top, bot, oslot); break;
-                }
-                __syncwarp();
-                if (elect_one()) {
-                    commit(bars.xempty(L, b));
-                    commit(bars.afull(L, c));
+                    case 1: issue_row<1>(dacc, ad0, bd0, c, sbase, top, bot, oslot, xe, af); break;
+                    case 2: issue_row<2>(dacc, ad0, bd0, c, sbase, top, bot, oslot, xe, af); break;
+                    case 3: issue_row<3>(dacc, ad0, bd0, c, sbase, top, bot, oslot, xe, af); break;
+                    default: issue_row<4>(dacc, ad0, bd0, c, sbase, top, bot, oslot, xe, af); break;
                 }
             }
             __syncwarp();
@@ -488,9 +491,9 @@ __device__ void epi_agent(const int L, const FusedArgs &a, const Bars &bars, uin
     uint32_t aph = 0, pph = 0, used = 0;
     const float *bl_ = bias + 32 * (L - 1);
     for (int tile = blockIdx.x; tile < a.ntiles && !*s_fail; tile += gridDim.x) {
-        int lo[5], hi[5], strip, f;
-        tile_rows(a, tile, lo, hi, strip, f);
-        for (int r = lo[L - 1] - 1; r <= hi[L - 1] && !*s_fail; ++r) {
+        const TileRows tr(a, tile);
+        const int r_end = tr.hi(L - 1), o_lo = tr.lo(L), o_hi = tr.hi(L);
+        for (int r = tr.lo(L - 1) - 1; r <= r_end && !*s_fail; ++r) {
             const int j = ring<D>(r);
             wt.wait(bars.afull(L, j), take(aph, j));
             tc_fence_after();
@@ -504,7 +507,7 @@ __device__ void epi_agent(const int L, const FusedArgs &a, const Bars &bars, uin
             wait_st();
             tc_fence_before();
             mbar_arrive(bars.aempty(L, j));  // the slot is free before the activations run
-            if (r >= lo[L] && r < hi[L]) {
+            if (r >= o_lo && r < o_hi) {
                 const int bx = r & (kNBuf - 1);
                 if ((used >> bx) & 1u) wt.wait(bars.xempty(L + 1, bx), ((pph >> bx) & 1u) ^ 1u);  // previous row consumed
                 used |= 1u << bx;
@@ -548,13 +551,13 @@ __device__ void feature_agent(const FusedArgs &a, const Bars &bars, uint8_t *sme
     const int nt = a.g.nt;
     uint32_t pph = 0, used = 0;
     for (int tile = blockIdx.x; tile < a.ntiles && !*s_fail; tile += gridDim.x) {
-        int lo[5], hi[5], strip, f;
-        tile_rows(a, tile, lo, hi, strip, f);
-        const Field &fd = a.fs.f[f];
-        const LaneCol lc(strip, lane, a.g.np);
+        const TileRows tr(a, tile);
+        const Field &fd = a.fs.f[tr.f];
+        const LaneCol lc(tr.strip, lane, a.g.np);
+        const int r0 = tr.lo(0), r1 = tr.hi(0);
         FeatIn pre;
-        if (hi[0] > lo[0]) feat_load(pre, lo[0], nt, fd, a.g, lc.col, lc.cw, lc.ce);
-        for (int srow = lo[0]; srow < hi[0] && !*s_fail; ++srow) {
+        if (r1 > r0) feat_load(pre, r0, nt, fd, a.g, lc.col, lc.cw, lc.ce);
+        for (int srow = r0; srow < r1 && !*s_fail; ++srow) {
             const int b = srow & (kNBuf - 1);
             if ((used >> b) & 1u) wt.wait(bars.xempty(1, b), ((pph >> b) & 1u) ^ 1u);
             used |= 1u << b;
@@ -562,7 +565,7 @@ __device__ void feature_agent(const FusedArgs &a, const Bars &bars, uint8_t *sme
             feat_store(pre, fd, a.g, smem + xbuf(1, b), lane);
             fence_async_smem();
             mbar_arrive(bars.xfull(1, b));
-            if (srow + 1 < hi[0]) feat_load(pre, srow + 1, nt, fd, a.g, lc.col, lc.cw, lc.ce);
+            if (srow + 1 < r1) feat_load(pre, srow + 1, nt, fd, a.g, lc.col, lc.cw, lc.ce);
         }
     }
 }
@@ -575,12 +578,13 @@ __device__ void output_agent(const FusedArgs &a, const Bars &bars, uint8_t *smem
     float *prev = reinterpret_cast<float *>(smem + kOffPrev) + lane;  // [column][lane]
     for (int j = 0; j < kDepth4; ++j) prev[j * kLanes] = 0.f;
     for (int tile = blockIdx.x; tile < a.ntiles && !*s_fail; tile += gridDim.x) {
-        int lo[5], hi[5], strip, f;
-        tile_rows(a, tile, lo, hi, strip, f);
+        const TileRows tr(a, tile);
+        const int f = tr.f;
         const Field &fd = a.fs.f[f];
-        const LaneCol lc(strip, lane, np);
-        for (int r = lo[3] - 1; r <= hi[3] && !*s_fail; ++r) {
-            const bool emit = r >= lo[4] && r < hi[4] && lc.out;
+        const LaneCol lc(tr.strip, lane, np);
+        const int r_end = tr.hi(3), o_lo = tr.lo(4), o_hi = tr.hi(4);
+        for (int r = tr.lo(3) - 1; r <= r_end && !*s_fail; ++r) {
+            const bool emit = r >= o_lo && r < o_hi && lc.out;
             float hout = 0.f;
             if (emit && a.h_out) hout = fd.h[(size_t)r * fd.pitch + lc.col];
             const int j = ring<kDepth4>(r);
@@ -591,7 +595,7 @@ __device__ void output_agent(const FusedArgs &a, const Bars &bars, uint8_t *smem
             pin(yv);
             const float sum = __uint_as_float(yv), acc = __fsub_rn(sum, prev[j * kLanes]);
             prev[j * kLanes] = sum;
-            if (r == hi[3]) {
+            if (r == r_end) {
                 // every MMA of the tile has completed: restart the ring from zero
                 tzero16(tl + acc_col(3));
                 wait_st();
