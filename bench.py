@@ -20,7 +20,8 @@ surrogate: the learned 64-step operator (include/sbs_nn.h) trained here on 512 p
 trajectories at 256 x 512, then a 10,000-step rollout of the same 2048 x 4096 field with a plain
 check every 8 intervals; effective cell-steps/s and the masked relative L-inf error of the final
 thickness against the plain run (rows with sin(theta) >= 0.2; nearer the poles the explicit
-scheme is unstable at this resolution).
+scheme is unstable at this resolution). `surrogate` is the network with GELU activations (the
+default), `surrogate_hswish` the same network, data and schedule with hard-swish.
 foam / spectral: the batched-foam and spectral-contraction workloads, device-resident.
 
 --impl reference: times that CPU restatement alone (the reference is Rust and cannot be
@@ -193,22 +194,18 @@ def launches_per_run(k: int) -> int:
     return total
 
 
-def surrogate_section(sbs, synthetic, h0, c0, torch):
-    """C4: train on 512 plain trajectories at 256 x 512, then the checked 10,000-step rollout."""
-    N = sbs._native
+def surrogate_section(sbs, synthetic, h0, c0, torch, activations=("gelu", "hswish")):
+    """C4: train on 512 plain trajectories at 256 x 512, then the checked 10,000-step rollout, once per
+    activation (GELU, the network's default, and hard-swish) from the same initial weights and data."""
     nt, np_ = h0.shape
     cells = h0.size
     s = sbs.DrainageSurrogate(seed=7)
+    theta0 = s.params
     t0 = time.perf_counter()
     ntraj = 512
     for h, c, visc, rad in synthetic.surrogate_trajectories(ntraj):
         s.add_trajectory(h, c, sbs.field_params(256, 512, viscosity=visc, bubble_radius=rad), pairs=4)
-    t1 = time.perf_counter()
-    iters = 3000
-    losses = s.train(ntraj - 32, iters, batch=8, lr=2e-3, seed=5)
-    torch.cuda.synchronize()
-    t2 = time.perf_counter()
-    ev = s.evaluate(ntraj - 32, 32, mode="fused")
+    data_s = time.perf_counter() - t0
     p = sbs.field_params(nt, np_, bubble_radius=0.025)
 
     def fresh():
@@ -229,47 +226,60 @@ def surrogate_section(sbs, synthetic, h0, c0, torch):
     torch.cuda.synchronize()
     plain_s = time.perf_counter() - ta
     h_ref = ref.thickness_array()
-    # fused forward pass alone (one 64-pass interval)
-    sim = fresh()
-    for _ in range(3):
-        s.advance(sim, mode="fused")
-    reps = 20
-    torch.cuda.synchronize()
-    ta = time.perf_counter()
-    for _ in range(reps):
-        s.advance(sim, mode="fused")
-    torch.cuda.synchronize()
-    fused_ms = (time.perf_counter() - ta) / reps * 1e3
-    # the checked rollout: 156 intervals (9,984 passes) + 16 plain passes = 10,000 steps
-    sim = fresh()
-    torch.cuda.synchronize()
-    ta = time.perf_counter()
-    st = s.rollout(sim, STEPS_PER_RUN // 64 * 64, check_every=8, tol=1e-3, mode="fused")
-    sim.run(STEPS_PER_RUN % 64)
-    torch.cuda.synchronize()
-    roll_s = time.perf_counter() - ta
-    h_sur = sim.thickness_array()
-    err = sbs.masked_error(h_sur, h_ref)
+    ref.close()
     err_id = sbs.masked_error(h0, h_ref)
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     tf_peak = float(peaks.get("bf16_tflops", 1900.0))
     flop_cell = 2 * 9 * (16 * 32 + 32 * 32 * 2 + 32 * 1)  # useful multiply-adds x 2 per cell and interval
-    tflops = flop_cell * cells / (fused_ms * 1e-3) / 1e12
-    rate = cells * STEPS_PER_RUN / roll_s
     plain_rate = cells * STEPS_PER_RUN / plain_s
-    out = {"value": rate, "unit": "cell-steps/s", "speedup_vs_plain": rate / plain_rate,
-           "plain_value": plain_rate, "masked_rel_linf_vs_plain": err, "identity_rel_linf_vs_plain": err_id,
-           "tol": 1e-3, "stats": st, "fused_ms_per_interval": fused_ms,
-           "fused_interval_cell_steps_per_s": cells * 64 / (fused_ms * 1e-3),
-           "tensor": {"bound": "tensor", "achieved": tflops, "peak": tf_peak, "unit": "TFLOP/s",
-                      "frac": tflops / tf_peak, "flop_per_cell": flop_cell, "peak_kind": "measured bf16 burst"},
-           "train": {"trajectories": ntraj, "grid": "256 x 512", "pairs_per_trajectory": 4, "iters": iters,
-                     "batch": 8, "data_s": t1 - t0, "train_s": t2 - t1, "loss_first": float(losses[:10].mean()),
-                     "loss_last": float(losses[-50:].mean())},
-           "heldout_256": ev}
+    iters = 3000
+    results = {}
+    for act in activations:
+        s.activation = act
+        s.params = theta0  # same start for every activation (also resets the optimiser state)
+        t1 = time.perf_counter()
+        losses = s.train(ntraj - 32, iters, batch=8, lr=2e-3, seed=5)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        ev = s.evaluate(ntraj - 32, 32, mode="fused")
+        # fused forward pass alone (one 64-pass interval)
+        sim = fresh()
+        for _ in range(3):
+            s.advance(sim, mode="fused")
+        reps = 20
+        torch.cuda.synchronize()
+        ta = time.perf_counter()
+        for _ in range(reps):
+            s.advance(sim, mode="fused")
+        torch.cuda.synchronize()
+        fused_ms = (time.perf_counter() - ta) / reps * 1e3
+        sim.close()
+        # the checked rollout: 156 intervals (9,984 passes) + 16 plain passes = 10,000 steps
+        sim = fresh()
+        torch.cuda.synchronize()
+        ta = time.perf_counter()
+        st = s.rollout(sim, STEPS_PER_RUN // 64 * 64, check_every=8, tol=1e-3, mode="fused")
+        sim.run(STEPS_PER_RUN % 64)
+        torch.cuda.synchronize()
+        roll_s = time.perf_counter() - ta
+        err = sbs.masked_error(sim.thickness_array(), h_ref)
+        sim.close()
+        tflops = flop_cell * cells / (fused_ms * 1e-3) / 1e12
+        rate = cells * STEPS_PER_RUN / roll_s
+        results[act] = {
+            "activation": act, "value": rate, "unit": "cell-steps/s", "speedup_vs_plain": rate / plain_rate,
+            "plain_value": plain_rate, "masked_rel_linf_vs_plain": err, "identity_rel_linf_vs_plain": err_id,
+            "tol": 1e-3, "stats": st, "fused_ms_per_interval": fused_ms,
+            "fused_interval_cell_steps_per_s": cells * 64 / (fused_ms * 1e-3),
+            "tensor": {"bound": "tensor", "achieved": tflops, "peak": tf_peak, "unit": "TFLOP/s",
+                       "frac": tflops / tf_peak, "flop_per_cell": flop_cell, "peak_kind": "measured bf16 burst"},
+            "train": {"trajectories": ntraj, "grid": "256 x 512", "pairs_per_trajectory": 4, "iters": iters,
+                      "batch": 8, "data_s": data_s, "train_s": t2 - t1, "loss_first": float(losses[:10].mean()),
+                      "loss_last": float(losses[-50:].mean())},
+            "heldout_256": ev}
     s.close()
-    return out
+    return results
 
 
 def foam_section(sbs, synthetic, torch):
@@ -488,7 +498,8 @@ def main():
             "cpu_semantics": {"value": cpu_sem_rate, "unit": "cell-steps/s", "storage": "f32x2 (16 B/cell-step)",
                               "frac_hbm": BYTES_PER_CELL_STEP * cells * 2000 / (cpu_sem_ms / 1e3) / 1e9 / peak},
             "cpu_baseline": base,
-            "surrogate": surrogate,
+            "surrogate": surrogate and surrogate["gelu"],
+            "surrogate_hswish": surrogate and surrogate["hswish"],
             "foam": foam,
             "spectral": spectral,
         }

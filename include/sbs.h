@@ -414,9 +414,14 @@ int sbs_surrogate_destroy(sbs_surrogate *s);
 /* FP32 parameter vector, n = SBS_NN_PARAMS, host memory. */
 int sbs_surrogate_set_params(sbs_surrogate *s, const float *params, size_t n);
 int sbs_surrogate_get_params(sbs_surrogate *s, float *params, size_t n);
+/* Activation of the network: SBS_NN_ACT_GELU (default) or SBS_NN_ACT_HSWISH
+ * (sbs_nn.h). Weights trained with one do not fit the other; set it before
+ * training. */
+int sbs_surrogate_set_activation(sbs_surrogate *s, int activation);
+int sbs_surrogate_get_activation(const sbs_surrogate *s, int *out);
 /* Features of nf <= 16 fields: h, c [nf][nt][np] (nt = p[k].grid_height, np =
- * p[k].grid_width, the same for every field), x out [nf][nt][np][8] (BF16
- * values as f32). mem applies to h, c and x. */
+ * p[k].grid_width, the same for every field), x out [nf][nt][np][SBS_NN_NF]
+ * (BF16 values as f32). mem applies to h, c and x. */
 int sbs_surrogate_features(sbs_surrogate *s, uint32_t nf, const float *h, const float *c,
                            const sbs_drainage_params *p, float *x, int mem);
 /* Network output y [nf][nt][np] (mode SBS_NN_LAYERED or SBS_NN_FUSED). */

@@ -52,14 +52,26 @@
  * then b[oc], tap = (dy + 1) * 3 + (dx + 1) with dy the row (theta) offset and
  * dx the column (phi) offset of the input cell read for an output cell.
  *
- * Activation (after every layer but the last): hard-swish,
- *   act(x) = x * s(x),  s(x) = sat(x / 6 + 1/2),  sat() clamping to [0, 1],
- * a smooth-enough relative of GELU / swish that costs two FP32 operations (the
- * saturation is a free modifier of the fused multiply-add on the GPU).  In FP32,
- * bit for bit:
- *   r = fma(x, SBS_NN_HS_SLOPE, 0.5);  s = sat(r) (NaN -> 0);  act = x * s
+ * Activation (after every layer but the last), chosen per network
+ * (sbs_surrogate_set_activation):
+ *
+ * SBS_NN_ACT_GELU (default): gelu(x) = x * phi(x), phi(x) = 0.5 + t p(t^2),
+ * t = clamp(x, -3, 3), p(u) = Q0 + Q1 u + Q2 u^2 + Q3 u^3 + Q4 u^4.  The Qk are a
+ * least-squares fit of the normal CDF minus 1/2 on [0, 3] under the constraint
+ * phi(3) = 1, so phi is 0 / 1 (to float rounding) beyond -3 / 3 (max
+ * |phi - normal CDF| = 1.35e-3, max |gelu - x * normal CDF| = 4.0e-3).  In FP32:
+ *   p = fma(fma(fma(fma(Q4, u, Q3), u, Q2), u, Q1), u, Q0); phi = fma(t, p, 0.5)
  * and the derivative
- *   act'(x) = (0 < r < 1) ? fma(x, SBS_NN_HS_SLOPE, s) : s.
+ *   dp = fma(fma(fma(Q4x4, u, Q3x3), u, Q2x2), u, Q1)
+ *   dphi = |x| < 3 ? fma(u + u, dp, p) : 0;  gelu'(x) = fma(x, dphi, phi).
+ *
+ * SBS_NN_ACT_HSWISH: hard-swish, hswish(x) = x * s(x), s(x) = sat(x / 6 + 1/2),
+ * sat() clamping to [0, 1]: two FP32 operations (the saturation is a modifier of
+ * the fused multiply-add on the GPU) against eleven for the GELU polynomial.  In
+ * FP32:
+ *   r = fma(x, SBS_NN_HS_SLOPE, 0.5);  s = sat(r) (NaN -> 0);  hswish = x * s
+ * and the derivative
+ *   hswish'(x) = (0 < r < 1) ? fma(x, SBS_NN_HS_SLOPE, s) : s.
  */
 #pragma once
 
@@ -88,4 +100,15 @@
 #define SBS_NN_MASK_SIN 0.2
 #define SBS_NN_MU_REF 0.044
 
+#define SBS_NN_ACT_GELU 0
+#define SBS_NN_ACT_HSWISH 1
+
+#define SBS_NN_Q0 0.39817786f
+#define SBS_NN_Q1 (-0.064430825f)
+#define SBS_NN_Q2 0.0083782589f
+#define SBS_NN_Q3 (-0.00064844202f)
+#define SBS_NN_Q4 2.1710333e-05f
+#define SBS_NN_Q2X2 0.016756518f
+#define SBS_NN_Q3X3 (-0.0019453261f)
+#define SBS_NN_Q4X4 8.6841333e-05f
 #define SBS_NN_HS_SLOPE 0.16666667f /* float(1 / 6) */

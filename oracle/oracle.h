@@ -163,19 +163,22 @@ void orc_spectral_rgb(const float *t_nm, const float *cos_i, const float *n_film
 void orc_nn_features(const float *h, const float *c, const orc_wgsl_params *p, float *x);
 /* kout of one field (include/sbs_nn.h) */
 float orc_nn_kout(const orc_wgsl_params *p);
-/* forward: y (nb*nt*np) from x (nb*nt*np*16) with the FP32 parameter vector (BF16-rounded inside) */
-void orc_nn_forward(const float *params, uint32_t nb, uint32_t nt, uint32_t np, const float *x, float *y);
+/* forward: y (nb*nt*np) from x (nb*nt*np*16) with the FP32 parameter vector (BF16-rounded inside);
+ * act = SBS_NN_ACT_GELU or SBS_NN_ACT_HSWISH */
+void orc_nn_forward(const float *params, uint32_t nb, uint32_t nt, uint32_t np, const float *x, float *y, int act);
 /* masked mean-square loss of y against target over rows with sin(theta) >= SBS_NN_MASK_SIN and its
  * gradient (SBS_NN_PARAMS floats). Returns the loss. */
 double orc_nn_loss_grad(const float *params, uint32_t nb, uint32_t nt, uint32_t np, const float *x,
-                        const float *target, float *grad);
+                        const float *target, float *grad, int act);
 /* h_out = surrogate update of h given the network output y (include/sbs_nn.h "Map") */
 void orc_nn_apply(const float *h, const float *y, uint32_t nt, uint32_t np, float kout, float *h_out);
 /* 1: drop every BF16 / float rounding (all-double network), for finite-difference checks */
 void orc_nn_set_exact(int exact);
-/* the hard-swish activation and its derivative in the FP32 form of include/sbs_nn.h */
-float orc_nn_act(float x);
-float orc_nn_act_grad(float x);
+/* the activations and their derivatives in the FP32 form of include/sbs_nn.h */
+float orc_nn_gelu(float x);
+float orc_nn_gelu_grad(float x);
+float orc_nn_hswish(float x);
+float orc_nn_hswish_grad(float x);
 
 #ifdef __cplusplus
 }

@@ -104,12 +104,14 @@ _SIGS = {
     "orc_spectral_rgb": ([_P, _P, _P, _SZ, _P, _U32, _P, _P], None),
     "orc_nn_features": ([_P, _P, C.POINTER(OrcWgslParams), _P], None),
     "orc_nn_kout": ([C.POINTER(OrcWgslParams)], _F),
-    "orc_nn_forward": ([_P, _U32, _U32, _U32, _P, _P], None),
-    "orc_nn_loss_grad": ([_P, _U32, _U32, _U32, _P, _P, _P], _D),
+    "orc_nn_forward": ([_P, _U32, _U32, _U32, _P, _P, _I], None),
+    "orc_nn_loss_grad": ([_P, _U32, _U32, _U32, _P, _P, _P, _I], _D),
     "orc_nn_apply": ([_P, _P, _U32, _U32, _F, _P], None),
-    "orc_nn_act": ([_F], _F),
+    "orc_nn_gelu": ([_F], _F),
+    "orc_nn_gelu_grad": ([_F], _F),
+    "orc_nn_hswish": ([_F], _F),
+    "orc_nn_hswish_grad": ([_F], _F),
     "orc_nn_set_exact": ([_I], None),
-    "orc_nn_act_grad": ([_F], _F),
 }
 
 
@@ -365,23 +367,26 @@ def nn_kout(params: OrcWgslParams) -> float:
     return float(lib().orc_nn_kout(C.byref(params)))
 
 
-def nn_forward(theta, x) -> np.ndarray:
+NN_ACT = {"gelu": 0, "hswish": 1}  # SBS_NN_ACT_*
+
+
+def nn_forward(theta, x, act: str = "gelu") -> np.ndarray:
     """Network output y [nb][nt][np] for features x [nb][nt][np][16]."""
     theta = np.ascontiguousarray(theta, dtype=np.float32)
     x = np.ascontiguousarray(x, dtype=np.float32)
     nb, nt, np_ = x.shape[:3]
     y = np.empty((nb, nt, np_), dtype=np.float32)
-    lib().orc_nn_forward(_p(theta), nb, nt, np_, _p(x), _p(y))
+    lib().orc_nn_forward(_p(theta), nb, nt, np_, _p(x), _p(y), NN_ACT[act])
     return y
 
 
-def nn_loss_grad(theta, x, target):
+def nn_loss_grad(theta, x, target, act: str = "gelu"):
     theta = np.ascontiguousarray(theta, dtype=np.float32)
     x = np.ascontiguousarray(x, dtype=np.float32)
     target = np.ascontiguousarray(target, dtype=np.float32)
     nb, nt, np_ = x.shape[:3]
     g = np.empty(NN_PARAMS, dtype=np.float32)
-    loss = lib().orc_nn_loss_grad(_p(theta), nb, nt, np_, _p(x), _p(target), _p(g))
+    loss = lib().orc_nn_loss_grad(_p(theta), nb, nt, np_, _p(x), _p(target), _p(g), NN_ACT[act])
     return float(loss), g
 
 
@@ -397,9 +402,17 @@ def nn_set_exact(exact: bool) -> None:
     lib().orc_nn_set_exact(1 if exact else 0)
 
 
-def nn_act(x: float) -> float:
-    return float(lib().orc_nn_act(float(x)))
+def nn_gelu(x: float) -> float:
+    return float(lib().orc_nn_gelu(float(x)))
 
 
-def nn_act_grad(x: float) -> float:
-    return float(lib().orc_nn_act_grad(float(x)))
+def nn_gelu_grad(x: float) -> float:
+    return float(lib().orc_nn_gelu_grad(float(x)))
+
+
+def nn_hswish(x: float) -> float:
+    return float(lib().orc_nn_hswish(float(x)))
+
+
+def nn_hswish_grad(x: float) -> float:
+    return float(lib().orc_nn_hswish_grad(float(x)))

@@ -41,16 +41,34 @@ int g_exact = 0;
 inline double rb(double v) { return g_exact ? v : (double)bf16r((float)v); }
 inline double rf(double v) { return g_exact ? v : (double)(float)v; }
 
-// hard-swish of include/sbs_nn.h in double (exact mode)
-double act_d(double x) {
+// activations of include/sbs_nn.h in double (exact mode)
+double gelu_d(double x) {
+    const double t = std::fmin(std::fmax(x, -3.0), 3.0), u = t * t;
+    const double p = (((SBS_NN_Q4 * u + SBS_NN_Q3) * u + SBS_NN_Q2) * u + SBS_NN_Q1) * u + SBS_NN_Q0;
+    return x * (0.5 + t * p);
+}
+
+double gelu_grad_d(double x) {
+    const double t = std::fmin(std::fmax(x, -3.0), 3.0), u = t * t;
+    const double p = (((SBS_NN_Q4 * u + SBS_NN_Q3) * u + SBS_NN_Q2) * u + SBS_NN_Q1) * u + SBS_NN_Q0;
+    const double dp = ((4.0 * (double)SBS_NN_Q4 * u + 3.0 * (double)SBS_NN_Q3) * u + 2.0 * (double)SBS_NN_Q2) * u +
+                      (double)SBS_NN_Q1;
+    const double dphi = std::fabs(x) < 3.0 ? p + 2.0 * u * dp : 0.0;
+    return (0.5 + t * p) + x * dphi;
+}
+
+double hswish_d(double x) {
     const double s = std::fmin(std::fmax(x * (double)SBS_NN_HS_SLOPE + 0.5, 0.0), 1.0);
     return x * s;
 }
 
-double act_grad_d(double x) {
+double hswish_grad_d(double x) {
     const double r = x * (double)SBS_NN_HS_SLOPE + 0.5;
     return r <= 0.0 ? 0.0 : (r >= 1.0 ? 1.0 : r + x * (double)SBS_NN_HS_SLOPE);
 }
+
+double act_d(int act, double x) { return act == SBS_NN_ACT_HSWISH ? hswish_d(x) : gelu_d(x); }
+double act_grad_d(int act, double x) { return act == SBS_NN_ACT_HSWISH ? hswish_grad_d(x) : gelu_grad_d(x); }
 
 struct Grid {
     std::vector<float> cp, cg, sg;
@@ -108,16 +126,39 @@ inline uint32_t refl(int64_t i, uint32_t nt) {
     return (uint32_t)i;
 }
 
+// the activations and their derivatives in the FP32 operation order of include/sbs_nn.h
+float gelu_f(float x) {
+    const float t = std::fmin(std::fmax(x, -3.f), 3.f);
+    const float u = t * t;
+    const float p = std::fma(std::fma(std::fma(std::fma(SBS_NN_Q4, u, SBS_NN_Q3), u, SBS_NN_Q2), u, SBS_NN_Q1),
+                             u, SBS_NN_Q0);
+    const float phi = std::fma(t, p, 0.5f);
+    return x * phi;
+}
+
+float gelu_grad_f(float x) {
+    const float t = std::fmin(std::fmax(x, -3.f), 3.f);
+    const float u = t * t;
+    const float p = std::fma(std::fma(std::fma(std::fma(SBS_NN_Q4, u, SBS_NN_Q3), u, SBS_NN_Q2), u, SBS_NN_Q1),
+                             u, SBS_NN_Q0);
+    const float phi = std::fma(t, p, 0.5f);
+    const float dp = std::fma(std::fma(std::fma(SBS_NN_Q4X4, u, SBS_NN_Q3X3), u, SBS_NN_Q2X2), u, SBS_NN_Q1);
+    const float dphi = std::fabs(x) < 3.f ? std::fma(u + u, dp, p) : 0.f;
+    return std::fma(x, dphi, phi);
+}
+
 // sat() of include/sbs_nn.h: clamp to [0, 1], NaN -> 0
 inline float sat01(float r) { return r > 0.f ? (r < 1.f ? r : 1.f) : 0.f; }
 
-// hard-swish and its derivative in the FP32 operation order of include/sbs_nn.h
-float act_f(float x) { return x * sat01(std::fma(x, SBS_NN_HS_SLOPE, 0.5f)); }
+float hswish_f(float x) { return x * sat01(std::fma(x, SBS_NN_HS_SLOPE, 0.5f)); }
 
-float act_grad_f(float x) {
+float hswish_grad_f(float x) {
     const float r = std::fma(x, SBS_NN_HS_SLOPE, 0.5f), s = sat01(r);
     return (r > 0.f && r < 1.f) ? std::fma(x, SBS_NN_HS_SLOPE, s) : s;
 }
+
+float act_f(int act, float x) { return act == SBS_NN_ACT_HSWISH ? hswish_f(x) : gelu_f(x); }
+float act_grad_f(int act, float x) { return act == SBS_NN_ACT_HSWISH ? hswish_grad_f(x) : gelu_grad_f(x); }
 
 struct Layer {
     int ci, co;
@@ -168,7 +209,7 @@ struct Fwd {
     std::vector<double> x, y[4], a[3];
 };
 
-void forward(const std::vector<Layer> &L, const float *x, uint32_t nb, uint32_t nt, uint32_t np, Fwd &F) {
+void forward(const std::vector<Layer> &L, const float *x, uint32_t nb, uint32_t nt, uint32_t np, int act, Fwd &F) {
     F.x.assign(x, x + (size_t)nb * nt * np * SBS_NN_NF);
     const double *in = F.x.data();
     for (int l = 0; l < 4; ++l) {
@@ -176,7 +217,7 @@ void forward(const std::vector<Layer> &L, const float *x, uint32_t nb, uint32_t 
         if (l < 3) {
             F.a[l].resize(F.y[l].size());
             for (size_t k = 0; k < F.y[l].size(); ++k)
-                F.a[l][k] = g_exact ? act_d(F.y[l][k]) : (double)bf16r(act_f((float)F.y[l][k]));
+                F.a[l][k] = g_exact ? act_d(act, F.y[l][k]) : (double)bf16r(act_f(act, (float)F.y[l][k]));
             in = F.a[l].data();
         }
     }
@@ -232,8 +273,10 @@ extern "C" {
 
 void orc_nn_set_exact(int exact) { g_exact = exact ? 1 : 0; }
 
-float orc_nn_act(float x) { return act_f(x); }
-float orc_nn_act_grad(float x) { return act_grad_f(x); }
+float orc_nn_gelu(float x) { return gelu_f(x); }
+float orc_nn_gelu_grad(float x) { return gelu_grad_f(x); }
+float orc_nn_hswish(float x) { return hswish_f(x); }
+float orc_nn_hswish_grad(float x) { return hswish_grad_f(x); }
 
 float orc_nn_kout(const orc_wgsl_params *p) { return field_consts(p).kout; }
 
@@ -267,18 +310,18 @@ void orc_nn_features(const float *h, const float *c, const orc_wgsl_params *p, f
     }
 }
 
-void orc_nn_forward(const float *params, uint32_t nb, uint32_t nt, uint32_t np, const float *x, float *y) {
+void orc_nn_forward(const float *params, uint32_t nb, uint32_t nt, uint32_t np, const float *x, float *y, int act) {
     const std::vector<Layer> L = layers_from(params);
     Fwd F;
-    forward(L, x, nb, nt, np, F);
+    forward(L, x, nb, nt, np, act, F);
     for (size_t k = 0; k < F.y[3].size(); ++k) y[k] = (float)F.y[3][k];
 }
 
 double orc_nn_loss_grad(const float *params, uint32_t nb, uint32_t nt, uint32_t np, const float *x,
-                        const float *target, float *grad) {
+                        const float *target, float *grad, int act) {
     const std::vector<Layer> L = layers_from(params);
     Fwd F;
-    forward(L, x, nb, nt, np, F);
+    forward(L, x, nb, nt, np, act, F);
     const Grid g = make_grid(nt, np);
     const size_t cells = (size_t)nb * nt * np;
     size_t nmask = 0;
@@ -306,7 +349,7 @@ double orc_nn_loss_grad(const float *params, uint32_t nb, uint32_t nt, uint32_t 
         const std::vector<double> &yl = F.y[l - 1];
         gy.assign(dx.size(), 0.0);
         for (size_t k = 0; k < dx.size(); ++k)
-            gy[k] = g_exact ? dx[k] * act_grad_d(yl[k]) : (double)bf16r((float)dx[k] * act_grad_f((float)yl[k]));
+            gy[k] = g_exact ? dx[k] * act_grad_d(act, yl[k]) : (double)bf16r((float)dx[k] * act_grad_f(act, (float)yl[k]));
     }
     return loss;
 }

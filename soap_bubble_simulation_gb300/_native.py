@@ -35,6 +35,8 @@ LOOKUP_TEXEL = 1
 NN_LAYERED = 0
 NN_FUSED = 1
 NN_PARAMS = 23425
+NN_ACT_GELU = 0
+NN_ACT_HSWISH = 1
 NN_STEPS = 64
 
 _ERR_NAMES = {
@@ -195,6 +197,8 @@ SIGNATURES: dict[str, list] = {
     "sbs_surrogate_destroy": [_P],
     "sbs_surrogate_set_params": [_P, _P, _SZ],
     "sbs_surrogate_get_params": [_P, _P, _SZ],
+    "sbs_surrogate_set_activation": [_P, _I],
+    "sbs_surrogate_get_activation": [_P, _P],
     "sbs_surrogate_features": [_P, _U32, _P, _P, _P, _P, _I],
     "sbs_surrogate_forward": [_P, _U32, _P, _P, _P, _P, _I, _I],
     "sbs_surrogate_loss_grad": [_P, _U32, _P, _P, _P, _P, _DP, _P],

@@ -1,6 +1,7 @@
-// Shared device pieces of the drainage surrogate (include/sbs_nn.h): the FP32 hard-swish and its
-// derivative in the exact operation order of the definition, BF16 packing, and the argument
-// structs of the kernels in nn_kernels.cu / nn_fused.cu.
+// Shared device pieces of the drainage surrogate (include/sbs_nn.h): the FP32 activations (GELU
+// polynomial and hard-swish) and their derivatives in the exact operation order of the
+// definition, BF16 packing, and the argument structs of the kernels in nn_kernels.cu /
+// nn_fused.cu.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -16,6 +17,44 @@ typedef __nv_bfloat16 bf16;
 constexpr int kTileCols = 128;  // output columns per tile of the layered kernels
 constexpr int kMaxFields = 16;  // fields per batched launch
 
+__device__ __forceinline__ float phi_poly(float t, float u, float *p_out) {
+    const float p =
+        __fmaf_rn(__fmaf_rn(__fmaf_rn(__fmaf_rn(SBS_NN_Q4, u, SBS_NN_Q3), u, SBS_NN_Q2), u, SBS_NN_Q1), u, SBS_NN_Q0);
+    *p_out = p;
+    return __fmaf_rn(t, p, 0.5f);
+}
+
+__device__ __forceinline__ float gelu(float x) {
+    const float t = fminf(fmaxf(x, -3.f), 3.f);
+    const float u = __fmul_rn(t, t);
+    float p;
+    const float phi = phi_poly(t, u, &p);
+    return __fmul_rn(x, phi);
+}
+
+__device__ __forceinline__ float gelu_grad(float x) {
+    const float t = fminf(fmaxf(x, -3.f), 3.f);
+    const float u = __fmul_rn(t, t);
+    float p;
+    const float phi = phi_poly(t, u, &p);
+    const float dp = __fmaf_rn(__fmaf_rn(__fmaf_rn(SBS_NN_Q4X4, u, SBS_NN_Q3X3), u, SBS_NN_Q2X2), u, SBS_NN_Q1);
+    const float dphi = fabsf(x) < 3.f ? __fmaf_rn(__fadd_rn(u, u), dp, p) : 0.f;
+    return __fmaf_rn(x, dphi, phi);
+}
+
+// Two GELUs with packed FP32x2 arithmetic: the same IEEE round-to-nearest operations as gelu(),
+// so the results are bitwise those of two gelu() calls.
+__device__ __forceinline__ float2 gelu2(float2 x) {
+    const float2 t = make_float2(fminf(fmaxf(x.x, -3.f), 3.f), fminf(fmaxf(x.y, -3.f), 3.f));
+    const float2 u = __fmul2_rn(t, t);
+    float2 p = __ffma2_rn(make_float2(SBS_NN_Q4, SBS_NN_Q4), u, make_float2(SBS_NN_Q3, SBS_NN_Q3));
+    p = __ffma2_rn(p, u, make_float2(SBS_NN_Q2, SBS_NN_Q2));
+    p = __ffma2_rn(p, u, make_float2(SBS_NN_Q1, SBS_NN_Q1));
+    p = __ffma2_rn(p, u, make_float2(SBS_NN_Q0, SBS_NN_Q0));
+    const float2 phi = __ffma2_rn(t, p, make_float2(0.5f, 0.5f));
+    return __fmul2_rn(x, phi);
+}
+
 // sat(fma(a, b, c)) in one instruction: round-to-nearest FMA, then clamp to [0, 1] (NaN -> +0).
 __device__ __forceinline__ float fma_sat(float a, float b, float c) {
     float r;
@@ -23,20 +62,26 @@ __device__ __forceinline__ float fma_sat(float a, float b, float c) {
     return r;
 }
 
-// Hard-swish of include/sbs_nn.h: x * sat(fma(x, 1/6, 0.5)).
-__device__ __forceinline__ float act(float x) { return __fmul_rn(x, fma_sat(x, SBS_NN_HS_SLOPE, 0.5f)); }
+// Hard-swish: x * sat(fma(x, 1/6, 0.5)).
+__device__ __forceinline__ float hswish(float x) { return __fmul_rn(x, fma_sat(x, SBS_NN_HS_SLOPE, 0.5f)); }
 
-__device__ __forceinline__ float act_grad(float x) {
+__device__ __forceinline__ float hswish_grad(float x) {
     const float r = __fmaf_rn(x, SBS_NN_HS_SLOPE, 0.5f);
     const float s = __saturatef(r);
     return (r > 0.f && r < 1.f) ? __fmaf_rn(x, SBS_NN_HS_SLOPE, s) : s;
 }
 
-// Two activations: the saturating FMAs are scalar (there is no saturating FP32x2 FMA), the product
-// is one packed FP32x2 multiply; bitwise the results of two act() calls.
-__device__ __forceinline__ float2 act2(float2 x) {
+// Two hard-swishes: the saturating FMAs are scalar (there is no saturating FP32x2 FMA), the
+// product is one packed FP32x2 multiply; bitwise the results of two hswish() calls.
+__device__ __forceinline__ float2 hswish2(float2 x) {
     const float2 s = make_float2(fma_sat(x.x, SBS_NN_HS_SLOPE, 0.5f), fma_sat(x.y, SBS_NN_HS_SLOPE, 0.5f));
     return __fmul2_rn(x, s);
+}
+
+// The network's activation (SBS_NN_ACT_*), chosen by a value that is uniform over the launch.
+__device__ __forceinline__ float act(int kind, float x) { return kind == SBS_NN_ACT_HSWISH ? hswish(x) : gelu(x); }
+__device__ __forceinline__ float act_grad(int kind, float x) {
+    return kind == SBS_NN_ACT_HSWISH ? hswish_grad(x) : gelu_grad(x);
 }
 
 __device__ __forceinline__ uint32_t pack2(float lo, float hi) {

@@ -6,8 +6,8 @@
 // 4 on each side are the halo the four layers consume) times a block of theta rows of one field.
 // The block runs nine agents that only talk through mbarriers: four MMA warps (one per layer:
 // for each input row, wait for the row and for the accumulator slot it starts, issue, commit),
-// three epilogue warpgroups (warpgroup l-1 reads layer l's finished row from TMEM, zeroes and
-// releases the slot at once, then adds the bias, applies the activation and writes the row into
+// three epilogue warpgroups (warpgroup l-1 reads layer l's finished row from TMEM, restarts the
+// slot from the bias at once, then applies the activation and writes the row into
 // one of four input buffers of layer l+1), a feature warpgroup (the input rows of layer 1) and an
 // output warpgroup (layer 4's rows: y and the thickness update). Every ring (activation buffers:
 // full / empty; accumulator rows: full / empty) is balanced per tile, so each waiter is at most
@@ -61,6 +61,7 @@ const float *theta_of(sbs_surrogate *s);
 void **fused_slot(sbs_surrogate *s);
 int *fused_dirty_flag(sbs_surrogate *s);
 int sms_of(sbs_surrogate *s);
+int act_of(sbs_surrogate *s);
 
 namespace {
 
@@ -206,6 +207,7 @@ struct FusedArgs {
     float *h_out;          // field 0 only, or null
     size_t pitch_out;
     int nf, nstrips, nrb, rows_per_block, ntiles;
+    int act;  // SBS_NN_ACT_*
     unsigned *err;
 };
 
@@ -483,6 +485,24 @@ __device__ void mma_agent(const int L, const FusedArgs &a, const Bars &bars, uin
     }
 }
 
+// A finished row's 32 activations (slot values already include the bias) as four BF16 planes.
+template <int ACT>
+__device__ __forceinline__ void store_row(const uint32_t *v, uint8_t *dst) {
+#pragma unroll
+    for (int pl = 0; pl < 4; ++pl) {
+        uint4 o;
+        uint32_t *ow = reinterpret_cast<uint32_t *>(&o);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int c = pl * 8 + 2 * e;
+            const float2 y = make_float2(__uint_as_float(v[c]), __uint_as_float(v[c + 1]));
+            const float2 gy = ACT == SBS_NN_ACT_HSWISH ? hswish2(y) : gelu2(y);
+            ow[e] = pack2(gy.x, gy.y);
+        }
+        *reinterpret_cast<uint4 *>(dst + pl * kPlane) = o;
+    }
+}
+
 // One code copy serves the three warpgroups (L is a runtime value): the epilogue is the largest
 // code of the kernel, and three instantiations cost instruction-cache misses.
 __device__ void epi_agent(const int L, const FusedArgs &a, const Bars &bars, uint8_t *smem, uint32_t tl, int lane,
@@ -513,18 +533,10 @@ __device__ void epi_agent(const int L, const FusedArgs &a, const Bars &bars, uin
                 used |= 1u << bx;
                 pph ^= 1u << bx;
                 uint8_t *dst = smem + xbuf(L + 1, bx) + (lane + 1) * 16;
-#pragma unroll
-                for (int pl = 0; pl < 4; ++pl) {
-                    uint4 o;
-                    uint32_t *ow = reinterpret_cast<uint32_t *>(&o);
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        const int c = pl * 8 + 2 * e;
-                        const float2 gy = act2(make_float2(__uint_as_float(v[c]), __uint_as_float(v[c + 1])));
-                        ow[e] = pack2(gy.x, gy.y);
-                    }
-                    *reinterpret_cast<uint4 *>(dst + pl * kPlane) = o;
-                }
+                if (a.act == SBS_NN_ACT_HSWISH)
+                    store_row<SBS_NN_ACT_HSWISH>(v, dst);
+                else
+                    store_row<SBS_NN_ACT_GELU>(v, dst);
                 fence_async_smem();
                 mbar_arrive(bars.xfull(L + 1, bx));
             }
@@ -799,6 +811,7 @@ int fused_forward(sbs_surrogate *s, const Fields &fields, int nf, const GridTab 
     a.pitch_out = pitch_out;
     a.nf = nf;
     a.nstrips = (g.np + kOut - 1) / kOut;
+    a.act = act_of(s);
     a.err = st->err;
     // rows per block: the smallest block count whose tile count fills the grid evenly (>= 16 rows)
     const int sms = std::max(1, sms_of(s));

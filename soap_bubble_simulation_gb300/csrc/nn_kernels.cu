@@ -98,6 +98,7 @@ struct ConvArgs {
     float *yout;
     bf16 *aout;
     int nt, np, tiles_x;
+    int act;  // SBS_NN_ACT_*
 };
 
 template <int CIN, bool BWD>
@@ -222,11 +223,11 @@ __global__ void __launch_bounds__(128) conv_kernel(ConvArgs a) {
                 if (!BWD) {
                     const float y0 = __fadd_rn(v0, a.bias[n]), y1 = __fadd_rn(v1, a.bias[n + 1]);
                     *(float2 *)(a.yout + cell * 32 + n) = make_float2(y0, y1);
-                    *(uint32_t *)(a.aout + cell * 32 + n) = pack2(act(y0), act(y1));
+                    *(uint32_t *)(a.aout + cell * 32 + n) = pack2(act(a.act, y0), act(a.act, y1));
                 } else {
                     const float2 yp = *(const float2 *)(a.yprev + cell * 32 + n);
                     *(uint32_t *)(a.aout + cell * 32 + n) =
-                        pack2(__fmul_rn(v0, act_grad(yp.x)), __fmul_rn(v1, act_grad(yp.y)));
+                        pack2(__fmul_rn(v0, act_grad(a.act, yp.x)), __fmul_rn(v1, act_grad(a.act, yp.y)));
                 }
             }
         }
@@ -468,6 +469,7 @@ struct Dgrad4Args {
     bf16 *g3;
     GridTab g;
     size_t cells;
+    int act;  // SBS_NN_ACT_*
 };
 
 __global__ void dgrad4_kernel(Dgrad4Args a) {
@@ -487,7 +489,7 @@ __global__ void dgrad4_kernel(Dgrad4Args a) {
         if (i == 1 && dy == -1) s = __fmaf_rn(a.g4[fb + q], a.w4[t * 32 + ic], s);
         if (i == nt - 2 && dy == 1) s = __fmaf_rn(a.g4[fb + (size_t)(nt - 1) * np + q], a.w4[t * 32 + ic], s);
     }
-    a.g3[c * 32 + ic] = __float2bfloat16_rn(__fmul_rn(s, act_grad(a.y3[c * 32 + ic])));
+    a.g3[c * 32 + ic] = __float2bfloat16_rn(__fmul_rn(s, act_grad(a.act, a.y3[c * 32 + ic])));
 }
 
 // sum of partial rows (fixed order) scattered into the canonical parameter layout
@@ -646,6 +648,7 @@ cudaError_t conv_forward(int layer, const bf16 *in, const Packed &p, float *y, b
     c.nt = nt;
     c.np = np;
     c.tiles_x = (np + kTileCols - 1) / kTileCols;
+    c.act = p.act;
     if (layer == 1) {
         c.w = p.wf1;
         c.bias = p.b;
@@ -663,6 +666,7 @@ cudaError_t conv_backward_data(int layer, const bf16 *g, const Packed &p, const 
     c.w = layer == 2 ? p.wb2 : p.wb3;
     c.yprev = yprev;
     c.aout = gprev;
+    c.act = p.act;
     c.nt = nt;
     c.np = np;
     c.tiles_x = (np + kTileCols - 1) / kTileCols;
@@ -743,6 +747,7 @@ cudaError_t output_backward(const float *g4, const bf16 *a3, const float *y3, co
     d.g3 = g3;
     d.g = g;
     d.cells = cells;
+    d.act = p.act;
     dgrad4_kernel<<<(unsigned)((cells + 7) / 8), 256, 0, st>>>(d);
     return cudaGetLastError();
 }

@@ -17,6 +17,7 @@ struct Packed {
     bf16 *wb3;  // [32][288] layer 3 transpose
     float *w4;  // [9][32]   layer 4, BF16-rounded values in FP32
     float *b;   // [97]      b1 | b2 | b3 | b4
+    int act;    // SBS_NN_ACT_* of the network
 };
 
 cudaError_t features(const Fields &fs, int nf, const GridTab &g, bf16 *x, cudaStream_t st);

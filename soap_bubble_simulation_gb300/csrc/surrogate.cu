@@ -121,6 +121,7 @@ const float *theta_of(sbs_surrogate *s) { return s->theta; }
 void **fused_slot(sbs_surrogate *s) { return &s->fused_w; }
 int *fused_dirty_flag(sbs_surrogate *s) { return &s->fused_dirty; }
 int sms_of(sbs_surrogate *s) { return s->sms; }
+int act_of(sbs_surrogate *s) { return s->pk.act; }
 }  // namespace nn
 }  // namespace sbs
 
@@ -410,6 +411,23 @@ int sbs_surrogate_set_params(sbs_surrogate *s, const float *params, size_t n) {
     int rc = repack(s);
     if (rc) return rc;
     SBS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return SBS_OK;
+}
+
+int sbs_surrogate_set_activation(sbs_surrogate *s, int activation) {
+    clear_error();
+    CHECK_S(s);
+    SBS_CHECK_ARG(activation == SBS_NN_ACT_GELU || activation == SBS_NN_ACT_HSWISH, "unknown activation %d",
+                  activation);
+    s->pk.act = activation;
+    return SBS_OK;
+}
+
+int sbs_surrogate_get_activation(const sbs_surrogate *s, int *out) {
+    clear_error();
+    CHECK_S(s);
+    SBS_CHECK_ARG(out != nullptr, "out is null");
+    *out = s->pk.act;
     return SBS_OK;
 }
 

@@ -6,7 +6,7 @@ Cases: `wgsl` (GPUDrainageSimulator semantics, h + surfactant), `cpu` (DrainageS
 semantics, compensated f32x2), `cpu32` (plain f32), `spectral-tc` / `spectral-fp32` (81-wavelength
 spectral colour of --points seeded points, tensor-core or FP32 contraction), `surrogate-fused` /
 `surrogate-layered` (--steps 64-pass surrogate intervals of the field, untrained seeded weights:
-the same kernels and shapes as a trained network), `foam` (the 4096-bubble foam batch, --steps
+the same kernels and shapes as a trained network; --activation gelu or hswish), `foam` (the 4096-bubble foam batch, --steps
 steps with the default tiles). The field is the seeded smooth-mode field of
 the 2048-resolution workload, built at the requested resolution. Steps launch one kernel each
 (graph replay for runs of 8 or more).
@@ -32,6 +32,7 @@ def main(argv=None) -> None:
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--blocking", type=int, default=-1, help="WGSL steps per launch (default: library choice)")
     p.add_argument("--bubbles", type=int, default=4096, help="foam case: number of bubbles")
+    p.add_argument("--activation", default="gelu", choices=["gelu", "hswish"], help="surrogate cases: activation")
     a = p.parse_args(argv)
     if a.case.startswith("spectral"):
         from .interference import spectral_rgb
@@ -59,7 +60,7 @@ def main(argv=None) -> None:
     if a.case.startswith("surrogate"):
         from .surrogate import DrainageSurrogate, field_params
 
-        s = DrainageSurrogate(seed=7)
+        s = DrainageSurrogate(seed=7, activation=a.activation)
         sim = GPUDrainageSimulator(None, 550e-9, 2 * a.res, a.res)
         sim.update_params(field_params(a.res, 2 * a.res, bubble_radius=0.025))
         sim.set_thickness_array(h)
@@ -68,7 +69,7 @@ def main(argv=None) -> None:
             s.advance(sim, mode="fused" if a.case == "surrogate-fused" else "layered")
         s.close()
         sim.close()
-        print(f"ran {a.steps} surrogate intervals ({a.case}) at resolution {a.res}")
+        print(f"ran {a.steps} surrogate intervals ({a.case}, {a.activation}) at resolution {a.res}")
         return
     if a.case == "wgsl":
         sim = GPUDrainageSimulator(None, 550e-9, 2 * a.res, a.res)

@@ -1,7 +1,8 @@
 """Drainage surrogate: a 4-layer convolutional neural operator that advances a GPUDrainageSimulator
 film (drainage.wgsl:72-202, Marangoni off) by SURROGATE_STEPS = 64 passes in one forward pass.
 
-The network, its input features and its parameter layout are fixed by include/sbs_nn.h. It is
+The network, its input features and its parameter layout are fixed by include/sbs_nn.h; the
+activation is GELU (the default, ``activation="gelu"``) or hard-swish (``"hswish"``). It is
 trained here on trajectories of the plain GPU solver by the library's own tensor-core forward and
 backward kernels, and it runs either layer by layer (``mode="layered"``) or as one fused tcgen05
 kernel (``mode="fused"``). ``rollout`` lets the plain solver check every K-th interval and take
@@ -20,6 +21,7 @@ from .drainage import DrainageParams, GPUDrainageSimulator
 SURROGATE_STEPS = N.NN_STEPS
 NUM_PARAMS = N.NN_PARAMS
 _MODES = {"layered": N.NN_LAYERED, "fused": N.NN_FUSED}
+ACTIVATIONS = {"gelu": N.NN_ACT_GELU, "hswish": N.NN_ACT_HSWISH}
 
 
 class SurrogateEval(C.Structure):
@@ -70,9 +72,10 @@ def _mode(mode: str) -> int:
 
 
 class DrainageSurrogate:
-    def __init__(self, seed: int = 0):
+    def __init__(self, seed: int = 0, activation: str = "gelu"):
         self._h = C.c_void_p()
         N.call("sbs_surrogate_create", C.c_uint64(seed), C.byref(self._h))
+        self.activation = activation
 
     def close(self):
         if self._h:
@@ -98,6 +101,19 @@ class DrainageSurrogate:
         if theta.size != NUM_PARAMS:
             raise ValueError(f"expected {NUM_PARAMS} parameters")
         N.call("sbs_surrogate_set_params", self._h, N.ptr(theta), theta.size)
+
+    @property
+    def activation(self) -> str:
+        out = C.c_int()
+        N.call("sbs_surrogate_get_activation", self._h, C.byref(out))
+        return {v: k for k, v in ACTIVATIONS.items()}[out.value]
+
+    @activation.setter
+    def activation(self, name: str) -> None:
+        """Weights trained with one activation do not fit the other: set it before training."""
+        if name not in ACTIVATIONS:
+            raise ValueError(f"activation must be one of {sorted(ACTIVATIONS)}")
+        N.call("sbs_surrogate_set_activation", self._h, ACTIVATIONS[name])
 
     # ------------------------------------------------------------------ network
     def features(self, h, c, params) -> np.ndarray:

@@ -5,8 +5,9 @@ max |y| at every cell and 5e-4 in RMS (FP32 tensor-core accumulation order vs do
 activation that lands within an FP32 rounding of a BF16 rounding boundary flips by one BF16 ulp,
 2^-8 of itself - about 6e-5 of all activations, hundreds per 256 x 512 field - and the flip
 propagates through the later layers, so the worst cell grows with the grid while the RMS stays
-near 5e-5; the RMS bar catches any systematic error); gradients within 3e-2 relative L-inf per layer (the per-layer BF16 gradients
-amplify those flips).
+near 5e-5; the RMS bar catches any systematic error); gradients within 3e-2 relative L-inf per
+layer (the per-layer BF16 gradients amplify those flips). Every network test runs with both
+activations (GELU, hard-swish).
 """
 import numpy as np
 import pytest
@@ -47,10 +48,23 @@ def check_y(y, want):
     assert err <= 1e-2 and rms <= 5e-4, (err, rms)
 
 
-@pytest.fixture(scope="module")
-def net(sbs):
-    s = sbs.DrainageSurrogate(seed=11)
+@pytest.fixture(scope="module", params=["gelu", "hswish"])
+def net(sbs, request):
+    s = sbs.DrainageSurrogate(seed=11, activation=request.param)
     yield s
+    s.close()
+
+
+def test_activation_setting(sbs):
+    s = sbs.DrainageSurrogate(seed=1)
+    assert s.activation == "gelu"
+    s.activation = "hswish"
+    assert s.activation == "hswish"
+    with pytest.raises(ValueError):
+        s.activation = "relu"
+    with pytest.raises(sbs.SbsError):
+        sbs._native.call("sbs_surrogate_set_activation", s._h, 7)
+    assert s.activation == "hswish"
     s.close()
 
 
@@ -72,7 +86,7 @@ def test_forward_matches_oracle(sbs, orc, net, nt, np_, nf):
     theta = net.params
     y = net.forward(h, c, ps, mode="layered")
     x = np.stack([orc.nn_features(h[b], c[b], orc_params(orc, ps[b])) for b in range(nf)])
-    want = orc.nn_forward(theta, x)
+    want = orc.nn_forward(theta, x, net.activation)
     check_y(y, want)
 
 
@@ -83,15 +97,15 @@ def test_gradients_match_oracle(sbs, orc, net):
     target = np.random.default_rng(9).standard_normal((nf, nt, np_)).astype(np.float32)
     loss, grad = net.loss_grad(h, c, ps, target)
     x = np.stack([orc.nn_features(h[b], c[b], orc_params(orc, ps[b])) for b in range(nf)])
-    loss_o, grad_o = orc.nn_loss_grad(net.params, x, target)
+    loss_o, grad_o = orc.nn_loss_grad(net.params, x, target, net.activation)
     assert abs(loss - loss_o) <= 1e-3 * loss_o
     for name, a, b in LAYERS:
         e = np.abs(grad[a:b] - grad_o[a:b]).max() / np.abs(grad_o[a:b]).max()
         assert e <= 3e-2, (name, e)
 
 
-def trained_surrogate(sbs, ntraj=24, nt=48, np_=96, iters=300):
-    s = sbs.DrainageSurrogate(seed=3)
+def trained_surrogate(sbs, ntraj=24, nt=48, np_=96, iters=300, activation="gelu"):
+    s = sbs.DrainageSurrogate(seed=3, activation=activation)
     g = np.random.default_rng(0)
     from soap_bubble_simulation_gb300 import synthetic as S
 
@@ -104,8 +118,9 @@ def trained_surrogate(sbs, ntraj=24, nt=48, np_=96, iters=300):
     return s, losses
 
 
-def test_training_beats_identity(sbs):
-    s, losses = trained_surrogate(sbs)
+@pytest.mark.parametrize("activation", ["gelu", "hswish"])
+def test_training_beats_identity(sbs, activation):
+    s, losses = trained_surrogate(sbs, activation=activation)
     assert np.isfinite(losses).all()
     assert losses[-20:].mean() < 0.2 * losses[:5].mean()
     ev = s.evaluate(20, 4, mode="layered")
@@ -149,7 +164,7 @@ def test_fused_forward_matches_oracle(sbs, orc, net, nt, np_, nf):
     ps = params_list(sbs, nf, nt, np_, seed=nt + 8)
     y = net.forward(h, c, ps, mode="fused")
     x = np.stack([orc.nn_features(h[b], c[b], orc_params(orc, ps[b])) for b in range(nf)])
-    want = orc.nn_forward(net.params, x)
+    want = orc.nn_forward(net.params, x, net.activation)
     check_y(y, want)
     check_y(y, net.forward(h, c, ps, mode="layered"))
 

@@ -1,25 +1,41 @@
 """The surrogate oracle (include/sbs_nn.h restated on the CPU) pinned by analytic checks: the
-hard-swish activation against its closed form, the finite-difference features against closed-form derivatives,
-and the backward pass against central finite differences of the forward pass (exact mode)."""
+GELU polynomial against x * normal CDF, hard-swish against its closed form, the finite-difference
+features against closed-form derivatives, and the backward pass against central finite
+differences of the forward pass (exact mode), for both activations."""
+import math
 
 import numpy as np
 import pytest
+from scipy.special import erf
 
 S2 = 1e-5
 
 
+def test_gelu_polynomial_and_derivative(orc):
+    xs = np.linspace(-6, 6, 241)
+    g = np.array([orc.nn_gelu(v) for v in xs])
+    gt = xs * 0.5 * (1 + erf(xs / math.sqrt(2)))
+    assert np.abs(g - gt).max() < 4.1e-3
+    assert abs(orc.nn_gelu(-3.5)) < 1e-6 and abs(orc.nn_gelu(3.5) - 3.5) < 1e-6
+    pts = np.concatenate([np.linspace(-5, -3.05, 9), np.linspace(-2.95, 2.95, 31), np.linspace(3.05, 5, 9)])
+    fd = np.array([(orc.nn_gelu(v + 1e-2) - orc.nn_gelu(v - 1e-2)) / 2e-2 for v in pts])
+    gd = np.array([orc.nn_gelu_grad(v) for v in pts])
+    assert np.abs(fd - gd).max() < 2e-4
+
+
 def test_hardswish_and_derivative(orc):
     xs = np.linspace(-6, 6, 241)
-    a = np.array([orc.nn_act(v) for v in xs])
+    a = np.array([orc.nn_hswish(v) for v in xs])
     want = xs * np.clip(xs / 6 + 0.5, 0, 1)
     assert np.abs(a - want).max() <= 1e-6 * np.abs(xs).max()
-    assert orc.nn_act(-3.5) == 0.0 and orc.nn_act(3.5) == 3.5 and orc.nn_act(float("nan")) != orc.nn_act(float("nan"))
+    assert orc.nn_hswish(-3.5) == 0.0 and orc.nn_hswish(3.5) == 3.5
+    assert math.isnan(orc.nn_hswish(float("nan")))
     # away from the kinks at +-3 the derivative matches central differences
     pts = np.concatenate([np.linspace(-5, -3.05, 9), np.linspace(-2.95, 2.95, 31), np.linspace(3.05, 5, 9)])
-    fd = np.array([(orc.nn_act(v + 1e-2) - orc.nn_act(v - 1e-2)) / 2e-2 for v in pts])
-    gd = np.array([orc.nn_act_grad(v) for v in pts])
+    fd = np.array([(orc.nn_hswish(v + 1e-2) - orc.nn_hswish(v - 1e-2)) / 2e-2 for v in pts])
+    gd = np.array([orc.nn_hswish_grad(v) for v in pts])
     assert np.abs(fd - gd).max() < 2e-4
-    assert orc.nn_act_grad(-4.0) == 0.0 and orc.nn_act_grad(4.0) == 1.0 and orc.nn_act_grad(0.0) == 0.5
+    assert orc.nn_hswish_grad(-4.0) == 0.0 and orc.nn_hswish_grad(4.0) == 1.0 and orc.nn_hswish_grad(0.0) == 0.5
 
 
 def _params(orc, nt, np_, **kw):
@@ -79,15 +95,16 @@ def test_features_are_finite_for_nonfinite_input(orc):
     assert np.isfinite(x).all() and np.abs(x).max() <= 1e4
 
 
+@pytest.mark.parametrize("act", ["gelu", "hswish"])
 @pytest.mark.parametrize("nb,nt,np_", [(2, 6, 8), (1, 9, 12)])
-def test_backward_matches_finite_differences(orc, nb, nt, np_):
+def test_backward_matches_finite_differences(orc, nb, nt, np_, act):
     g = np.random.default_rng(nb * 100 + nt)
     theta = (0.08 * g.standard_normal(orc.NN_PARAMS)).astype(np.float32)
     x = g.standard_normal((nb, nt, np_, 16)).astype(np.float32)
     target = g.standard_normal((nb, nt, np_)).astype(np.float32)
     orc.nn_set_exact(True)
     try:
-        loss, grad = orc.nn_loss_grad(theta, x, target)
+        loss, grad = orc.nn_loss_grad(theta, x, target, act)
         # parameters in every layer: weights at the reflected (dy = -1 / +1) and periodic taps, biases
         idx = np.concatenate([g.integers(0, 4608, 6), [4608, 4639], g.integers(4640, 13856, 6), [13856],
                               g.integers(13888, 23104, 6), [23104], g.integers(23136, 23424, 6), [23424]])
@@ -96,7 +113,7 @@ def test_backward_matches_finite_differences(orc, nb, nt, np_):
             tp, tm = theta.copy(), theta.copy()
             tp[k] += eps
             tm[k] -= eps
-            fd = (orc.nn_loss_grad(tp, x, target)[0] - orc.nn_loss_grad(tm, x, target)[0]) / (2 * eps)
+            fd = (orc.nn_loss_grad(tp, x, target, act)[0] - orc.nn_loss_grad(tm, x, target, act)[0]) / (2 * eps)
             # the step itself is float32-rounded: use the exact difference of the stored values
             fd *= 2 * eps / (float(tp[k]) - float(tm[k]))
             assert abs(fd - grad[k]) <= 1e-4 * max(1.0, abs(fd)) + 1e-6, (k, fd, grad[k])
