@@ -15,7 +15,8 @@ roofline: the dominant kernel, the temporally blocked step (wtb_wgsl_kernel, 4 s
 launch), at 16 algorithmic bytes per cell-step (read h, Gamma; write h, Gamma) times the steps
 of a launch, against the measured copy bandwidth; `traffic` is its ncu DRAM bytes per launch.
 cpu_baseline: the oracle's f64 restatement of DrainageSimulator::step (drainage.rs:298-392) on
-all host cores, on a bounded sample of the same field (about --cpu-seconds of work).
+all host cores, on a bounded sample of the same field (about --cpu-seconds of work);
+cpu_baseline_single_thread: the same on one core (the reference's CPU path is single-threaded).
 surrogate: the learned 64-step operator (include/sbs_nn.h) trained here on 512 plain-solver
 trajectories at 256 x 512, then a 10,000-step rollout of the same 2048 x 4096 field with a plain
 check every 8 intervals; effective cell-steps/s and the masked relative L-inf error of the final
@@ -57,7 +58,7 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU baseline sample length")
+    p.add_argument("--cpu-seconds", type=float, default=20.0, help="target CPU baseline sample length")
     p.add_argument("--skip-aux", action="store_true",
                    help="plain path only (no surrogate / foam / spectral / CPU baseline), e.g. for an ncu launch list")
     return p.parse_args()
@@ -311,6 +312,10 @@ def spectral_section(sbs, synthetic, torch):
     wl = synthetic.WAVELENGTHS_81.astype(np.float32)
     cmf = synthetic.spectral_cmf().astype(np.float32)
     dt, dc, dn = (torch.from_numpy(x).cuda() for x in (t, c, nf))
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    tf_peak = float(peaks.get("bf16_tflops", 1900.0))
     out = {}
     res = {}
     for mode, name in ((N.SPECTRAL_TC_BF16, "tc_bf16"), (N.SPECTRAL_FP32, "fp32")):
@@ -329,7 +334,16 @@ def spectral_section(sbs, synthetic, torch):
             run()
         torch.cuda.synchronize()
         ms = (time.perf_counter() - ta) / reps * 1e3
-        out[name] = {"value": n / (ms * 1e-3), "unit": "points/s", "ms": ms}
+        # roofline fractions: HBM at 24 B per point (t, cos, n in; RGB out), the contraction's 486
+        # useful FLOP per point on the tensor pipe; the bound is the FP32 / SFU work of the 81 Airy
+        # terms per point (ncu: FMA pipe ~64 % of active cycles, profiles/spectral_tc_c3.md)
+        gbs = 24.0 * n / (ms * 1e-3) / 1e9
+        tfl = 2.0 * 81 * 3 * n / (ms * 1e-3) / 1e12
+        out[name] = {"value": n / (ms * 1e-3), "unit": "points/s", "ms": ms,
+                     "hbm": {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak},
+                     "tensor": {"achieved": tfl, "peak": tf_peak, "unit": "TFLOP/s", "frac": tfl / tf_peak,
+                                "pipe": "tcgen05 BF16" if name == "tc_bf16" else "none (FP32 FMA contraction)"},
+                     "bound": "FP32/SFU: spectrum generation (81 Airy terms per point)"}
         res[name] = o[:262144].cpu().numpy()
     # precision on a 262,144-point subset against the FP64 oracle
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -468,9 +482,11 @@ def main():
         foam = foam_section(sbs, synthetic, torch)
         spectral = spectral_section(sbs, synthetic, torch)
 
-    base = None
+    base = base1 = None
     if rank == 0 and world == 1 and not args.skip_aux:
         base = cpu_baseline(h0, args.cpu_seconds, os.cpu_count() or 1)
+        # the reference's own CPU path is single-threaded: the same restatement on one core
+        base1 = cpu_baseline(h0, min(args.cpu_seconds, 8.0), 1)
 
     if rank == 0:
         line = {
@@ -498,6 +514,7 @@ def main():
             "cpu_semantics": {"value": cpu_sem_rate, "unit": "cell-steps/s", "storage": "f32x2 (16 B/cell-step)",
                               "frac_hbm": BYTES_PER_CELL_STEP * cells * 2000 / (cpu_sem_ms / 1e3) / 1e9 / peak},
             "cpu_baseline": base,
+            "cpu_baseline_single_thread": base1,
             "surrogate": surrogate and surrogate["gelu"],
             "surrogate_hswish": surrogate and surrogate["hswish"],
             "foam": foam,

@@ -22,6 +22,8 @@
 
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "cell.cuh"
@@ -34,6 +36,12 @@ constexpr int kTileM = 128;
 constexpr int kNPad = 16;         // MMA N (channels 0..2 used)
 constexpr int kMaxLambda = 128;   // K padded to a multiple of 16, at most 128
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz: bound on every mbarrier wait
+
+// The BF16 CMF^T tile (B operand) passed by value in the kernel parameters: no per-call device
+// buffer, no upload.
+struct BTile {
+    uint4 v[kNPad * kMaxLambda * 2 / 16];
+};
 
 struct SpecConsts {
     float invl[kMaxLambda];     // 1 / lambda (nm^-1), zero beyond nl
@@ -144,7 +152,7 @@ template <int KPAD, int NBUF>
 __global__ void __launch_bounds__(kTileM) spectral_tc_kernel(const float *__restrict__ t_nm,
                                                             const float *__restrict__ cos_i,
                                                             const float *__restrict__ n_film, size_t n,
-                                                            const uint8_t *__restrict__ b_tile, const SpecConsts c,
+                                                            const BTile b_tile, const SpecConsts c,
                                                             float *__restrict__ rgb, unsigned *err) {
     constexpr uint32_t SBO = (KPAD / 8) * 128;
     constexpr uint32_t A_BYTES = kTileM * KPAD * 2;
@@ -171,8 +179,7 @@ __global__ void __launch_bounds__(kTileM) spectral_tc_kernel(const float *__rest
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         *s_fail = 0;
     }
-    for (uint32_t i = tid * 16; i < B_BYTES; i += kTileM * 16)
-        *reinterpret_cast<uint4 *>(sB + i) = *reinterpret_cast<const uint4 *>(b_tile + i);
+    for (uint32_t i = tid; i < B_BYTES / 16; i += kTileM) reinterpret_cast<uint4 *>(sB)[i] = b_tile.v[i];
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -292,7 +299,7 @@ __global__ void __launch_bounds__(128) spectral_fp32_kernel(const float *__restr
 #endif
 
 template <int KPAD>
-cudaError_t launch_tc(const float *t, const float *ci, const float *nf, size_t n, const uint8_t *btile,
+cudaError_t launch_tc(const float *t, const float *ci, const float *nf, size_t n, const BTile &btile,
                       const SpecConsts &c, float *rgb, unsigned *err, cudaStream_t s) {
     constexpr int NBUF = SBS_SPECTRAL_NBUF;
     const size_t smem = NBUF * (size_t)kTileM * KPAD * 2 + (size_t)kNPad * KPAD * 2 + 16 + 64;
@@ -319,6 +326,35 @@ cudaError_t launch_tc(const float *t, const float *ci, const float *nf, size_t n
 
 using namespace sbs;
 
+namespace {
+
+// A per-device memory pool whose release threshold keeps freed memory for reuse.
+int keep_pool(cudaMemPool_t *out) {
+    static std::mutex mu;
+    static std::map<int, cudaMemPool_t> pools;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return set_error(SBS_E_CUDA, "cudaGetDevice failed");
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = pools.find(dev);
+    if (it != pools.end()) {
+        *out = it->second;
+        return SBS_OK;
+    }
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) return set_error(SBS_E_CUDA, "cudaMemPoolCreate failed");
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    pools[dev] = pool;
+    *out = pool;
+    return SBS_OK;
+}
+
+}  // namespace
+
 extern "C" int sbs_spectral_rgb(const float *t_nm, const float *cos_i, const float *n_film, size_t n,
                                 const float *wl_nm, uint32_t nl, const float *cmf, int mode, float *rgb, int mem,
                                 void *stream) {
@@ -342,28 +378,35 @@ extern "C" int sbs_spectral_rgb(const float *t_nm, const float *cos_i, const flo
     }
     const int kpad = nl <= 32 ? 32 : (nl <= 64 ? 64 : (nl <= 96 ? 96 : 128));
     // B tile: CMF^T (16 x kpad) in BF16, K-major core matrices, channels 3..15 zero
-    const size_t b_bytes = (size_t)kNPad * kpad * 2;
-    std::vector<uint8_t> btile(b_bytes, 0);
+    BTile bt;
+    std::memset(&bt, 0, sizeof(bt));
+    uint8_t *btile = reinterpret_cast<uint8_t *>(bt.v);
     const uint32_t sbo = (uint32_t)(kpad / 8) * 128u;
     for (int ch = 0; ch < 3; ++ch)
         for (uint32_t l = 0; l < nl; ++l) {
             const __nv_bfloat16 v = __float2bfloat16_rn(cmf[3 * l + ch]);
-            std::memcpy(btile.data() + tile_off(ch, (int)l, sbo), &v, 2);
+            std::memcpy(btile + tile_off(ch, (int)l, sbo), &v, 2);
         }
 
+    // scratch: the timeout flag, plus staging buffers for host inputs. Device-memory calls take the
+    // flag from a pool that keeps its memory (the default pool returns it to the system at every
+    // synchronisation, and mapping it again costs more than this kernel's launch).
     const size_t in_bytes = 3 * n * sizeof(float), out_bytes = 3 * n * sizeof(float);
-    size_t scratch = b_bytes + 256;
-    if (mem == SBS_MEM_HOST) scratch += in_bytes + out_bytes;
     char *base = nullptr;
-    SBS_CUDA_TRY(cudaMallocAsync((void **)&base, scratch, s));
-    uint8_t *d_b = reinterpret_cast<uint8_t *>(base);
-    unsigned *d_err = reinterpret_cast<unsigned *>(base + b_bytes);
+    if (mem == SBS_MEM_HOST) {
+        SBS_CUDA_TRY(cudaMallocAsync((void **)&base, 256 + in_bytes + out_bytes, s));
+    } else {
+        cudaMemPool_t pool = nullptr;
+        rc = keep_pool(&pool);
+        if (rc) return rc;
+        SBS_CUDA_TRY(cudaMallocFromPoolAsync((void **)&base, 256, pool, s));
+    }
+    unsigned *d_err = reinterpret_cast<unsigned *>(base);
     const float *dt = t_nm, *dc = cos_i, *dn = n_film;
     float *dout = rgb;
-    cudaError_t e = cudaMemcpyAsync(d_b, btile.data(), b_bytes, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(d_err, 0, sizeof(unsigned), s);
+    cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(unsigned), s);
     if (e == cudaSuccess && mem == SBS_MEM_HOST) {
-        float *in = reinterpret_cast<float *>(base + b_bytes + 256);
+        float *in = reinterpret_cast<float *>(base + 256);
         e = cudaMemcpyAsync(in, t_nm, n * sizeof(float), cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) e = cudaMemcpyAsync(in + n, cos_i, n * sizeof(float), cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) e = cudaMemcpyAsync(in + 2 * n, n_film, n * sizeof(float), cudaMemcpyHostToDevice, s);
@@ -385,13 +428,13 @@ extern "C" int sbs_spectral_rgb(const float *t_nm, const float *cos_i, const flo
                 spectral_fp32_kernel<128><<<g, 128, 0, s>>>(dt, dc, dn, n, c, dout);
             e = cudaGetLastError();
         } else if (kpad == 32) {
-            e = launch_tc<32>(dt, dc, dn, n, d_b, c, dout, d_err, s);
+            e = launch_tc<32>(dt, dc, dn, n, bt, c, dout, d_err, s);
         } else if (kpad == 64) {
-            e = launch_tc<64>(dt, dc, dn, n, d_b, c, dout, d_err, s);
+            e = launch_tc<64>(dt, dc, dn, n, bt, c, dout, d_err, s);
         } else if (kpad == 96) {
-            e = launch_tc<96>(dt, dc, dn, n, d_b, c, dout, d_err, s);
+            e = launch_tc<96>(dt, dc, dn, n, bt, c, dout, d_err, s);
         } else {
-            e = launch_tc<128>(dt, dc, dn, n, d_b, c, dout, d_err, s);
+            e = launch_tc<128>(dt, dc, dn, n, bt, c, dout, d_err, s);
         }
     }
     unsigned herr = 0;
