@@ -24,6 +24,8 @@ thickness against the plain run (rows with sin(theta) >= 0.2; nearer the poles t
 scheme is unstable at this resolution). `surrogate` is the network with GELU activations (the
 default), `surrogate_hswish` the same network, data and schedule with hard-swish.
 foam / spectral: the batched-foam and spectral-contraction workloads, device-resident.
+c0: the small configuration's latency-bound calls (1000 steps at resolution 128 in both
+semantics, the colour LUTs, colours at 10,242 icosphere vertices), host in and host out.
 
 --impl reference: times that CPU restatement alone (the reference is Rust and cannot be
 built here), same metric and config.
@@ -305,6 +307,53 @@ def foam_section(sbs, synthetic, torch):
             "algorithmic_gbs": cells * 1000 * 16 / (ms * 1e-3) / 1e9}
 
 
+def c0_section(sbs, synthetic, torch):
+    """C0, latency-bound: 1000 steps at resolution 128 (128 x 256 cells) in both semantics, the
+    256 x 64 colour LUT over 0-1000 nm, the RGBA8 LUT and colours at the 10,242 subdivision-5
+    icosphere vertices, each timed through the public call (host in, host out)."""
+
+    def best(fn, reps=5):
+        fn()
+        ts = []
+        for _ in range(reps):
+            ta = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - ta)
+        return min(ts)
+
+    cfg = sbs.SimulationConfig()
+    cfg.resolution = 128
+    h = synthetic.bubble_c0(128, seed=0)
+    cpu = sbs.DrainageSimulator(cfg)
+
+    def run_cpu():
+        cpu.set_thickness_array(h)
+        cpu.step_n(cfg.dt, 1000)
+
+    t_cpu = best(run_cpu)
+    gpu = sbs.GPUDrainageSimulator(None, 500e-9, 256, 128)
+
+    def run_gpu():
+        gpu.set_thickness_array(h.astype(np.float32))
+        gpu.run(1000)
+
+    t_gpu = best(run_gpu)
+    calc = sbs.InterferenceCalculator(1.33)
+    lut = calc.color_lookup_2d_array(0.0, 1000.0, 256, 64)
+    t_lut = best(lambda: calc.color_lookup_2d_array(0.0, 1000.0, 256, 64))
+    t_rgba = best(lambda: sbs.generate_interference_lut(1.33, 1.0))
+    xyz = synthetic.icosphere(5)
+    t_vert = best(lambda: cpu.vertex_colors(xyz, lut, 0.0, 1000.0))
+    cells = 128 * 256
+    cpu.close()
+    gpu.close()
+    return {"drainage_cpu_semantics": {"ms_per_1000_steps": t_cpu * 1e3, "cell_steps_per_s": cells * 1000 / t_cpu},
+            "drainage_wgsl_semantics": {"ms_per_1000_steps": t_gpu * 1e3, "cell_steps_per_s": cells * 1000 / t_gpu},
+            "lut_256x64_f64": {"ms": t_lut * 1e3, "points_per_s": 256 * 64 / t_lut},
+            "lut_rgba8_64x256": {"ms": t_rgba * 1e3, "texels_per_s": 256 * 64 / t_rgba},
+            "vertex_colors": {"vertices": int(len(xyz)), "ms": t_vert * 1e3, "points_per_s": len(xyz) / t_vert}}
+
+
 def spectral_section(sbs, synthetic, torch):
     N = sbs._native
     n = 8_388_608
@@ -476,8 +525,9 @@ def main():
     cpu_sem_ms = a_ev.elapsed_time(b_ev)
     cpu_sem_rate = cells * 2000 / (cpu_sem_ms / 1e3)
 
-    surrogate = foam = spectral = None
+    surrogate = foam = spectral = small = None
     if not args.skip_aux:
+        small = c0_section(sbs, synthetic, torch)
         surrogate = surrogate_section(sbs, synthetic, h0, c0, torch)
         foam = foam_section(sbs, synthetic, torch)
         spectral = spectral_section(sbs, synthetic, torch)
@@ -519,6 +569,7 @@ def main():
             "surrogate_hswish": surrogate and surrogate["hswish"],
             "foam": foam,
             "spectral": spectral,
+            "c0": small,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -5,6 +5,9 @@
 #include <cstdio>
 #include <cstring>
 
+#include <map>
+#include <mutex>
+
 #include "sbs_internal.h"
 
 namespace sbs {
@@ -32,6 +35,34 @@ int require_device() {
     }
     if (n <= 0) return set_error(SBS_E_CUDA, "no CUDA device visible");
     return SBS_OK;
+}
+
+cudaError_t scratch_alloc(void **p, size_t bytes, cudaStream_t s) {
+    constexpr size_t kPooled = (size_t)64 << 20;
+    if (bytes > kPooled) return cudaMallocAsync(p, bytes, s);
+    static std::mutex mu;
+    static std::map<int, cudaMemPool_t> pools;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    cudaMemPool_t pool = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = pools.find(dev);
+        if (it != pools.end()) {
+            pool = it->second;
+        } else {
+            cudaMemPoolProps props{};
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            if ((e = cudaMemPoolCreate(&pool, &props)) != cudaSuccess) return e;
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            pools[dev] = pool;
+        }
+    }
+    return cudaMallocFromPoolAsync(p, bytes, pool, s);
 }
 
 }  // namespace sbs

@@ -377,7 +377,7 @@ int sbs_interference_color_batch(double n_film, const double wl[3], const void *
     Scratch scr;
     if (mem == SBS_MEM_HOST) {
         scr.s = s;
-        SBS_CUDA_TRY(cudaMallocAsync(&scr.p, 5 * n * es, s));
+        SBS_CUDA_TRY(scratch_alloc((void **)&scr.p, 5 * n * es, s));
         char *base = (char *)scr.p;
         SBS_CUDA_TRY(cudaMemcpyAsync(base, t_nm, n * es, cudaMemcpyHostToDevice, s));
         SBS_CUDA_TRY(cudaMemcpyAsync(base + n * es, cos_i, n * es, cudaMemcpyHostToDevice, s));
@@ -417,7 +417,7 @@ int sbs_interference_terms_batch(double n_film, double wl_nm, const double *t_nm
     Scratch scr;
     if (mem == SBS_MEM_HOST) {
         scr.s = s;
-        SBS_CUDA_TRY(cudaMallocAsync(&scr.p, 10 * n * sizeof(double), s));
+        SBS_CUDA_TRY(scratch_alloc((void **)&scr.p, 10 * n * sizeof(double), s));
         double *base = (double *)scr.p;
         SBS_CUDA_TRY(cudaMemcpyAsync(base, t_nm, n * sizeof(double), cudaMemcpyHostToDevice, s));
         SBS_CUDA_TRY(cudaMemcpyAsync(base + n, cos_i, n * sizeof(double), cudaMemcpyHostToDevice, s));
@@ -450,7 +450,7 @@ static int path_call(double n_film, const double *a, const double *b, const doub
     Scratch scr;
     if (mem == SBS_MEM_HOST) {
         scr.s = s;
-        SBS_CUDA_TRY(cudaMallocAsync(&scr.p, 4 * n * sizeof(double), s));
+        SBS_CUDA_TRY(scratch_alloc((void **)&scr.p, 4 * n * sizeof(double), s));
         double *base = (double *)scr.p;
         SBS_CUDA_TRY(cudaMemcpyAsync(base, a, n * sizeof(double), cudaMemcpyHostToDevice, s));
         SBS_CUDA_TRY(cudaMemcpyAsync(base + n, b, n * sizeof(double), cudaMemcpyHostToDevice, s));
@@ -501,7 +501,7 @@ int sbs_lut1d_build(double n_film, const double wl[3], double tmin, double tmax,
     Scratch scr;
     if (mem == SBS_MEM_HOST) {
         scr.s = s;
-        SBS_CUDA_TRY(cudaMallocAsync(&scr.p, 3 * (size_t)count * sizeof(double), s));
+        SBS_CUDA_TRY(scratch_alloc((void **)&scr.p, 3 * (size_t)count * sizeof(double), s));
         dout = (double *)scr.p;
     }
     Wl3 w{{wl[0], wl[1], wl[2]}};
@@ -533,7 +533,7 @@ int sbs_lut2d_build(double n_film, const double wl[3], double tmin, double tmax,
     Scratch scr;
     if (mem == SBS_MEM_HOST) {
         scr.s = s;
-        SBS_CUDA_TRY(cudaMallocAsync(&scr.p, 3 * n * sizeof(double), s));
+        SBS_CUDA_TRY(scratch_alloc((void **)&scr.p, 3 * n * sizeof(double), s));
         dout = (double *)scr.p;
     }
     Wl3 w{{wl[0], wl[1], wl[2]}};
@@ -559,7 +559,7 @@ int sbs_interference_lut_rgba8(float n_film, float intensity, uint8_t *out, int 
     Scratch scr;
     if (mem == SBS_MEM_HOST) {
         scr.s = s;
-        SBS_CUDA_TRY(cudaMallocAsync(&scr.p, 4 * n, s));
+        SBS_CUDA_TRY(scratch_alloc((void **)&scr.p, 4 * n, s));
         dout = (uchar4 *)scr.p;
     } else {
         SBS_CHECK_ARG(((uintptr_t)out & 3) == 0, "device output must be 4-byte aligned");
@@ -589,7 +589,7 @@ int sbs_schlick_rgb_batch(float n_film, const float wl[3], const float *t_nm, co
     Scratch scr;
     if (mem == SBS_MEM_HOST) {
         scr.s = s;
-        SBS_CUDA_TRY(cudaMallocAsync(&scr.p, 5 * n * sizeof(float), s));
+        SBS_CUDA_TRY(scratch_alloc((void **)&scr.p, 5 * n * sizeof(float), s));
         float *base = (float *)scr.p;
         SBS_CUDA_TRY(cudaMemcpyAsync(base, t_nm, n * sizeof(float), cudaMemcpyHostToDevice, s));
         SBS_CUDA_TRY(cudaMemcpyAsync(base + n, cos_i, n * sizeof(float), cudaMemcpyHostToDevice, s));
@@ -628,7 +628,7 @@ int sbs_lut_rgba8_lookup_batch(const uint8_t *lut, uint32_t W, uint32_t H, float
     Scratch scr;
     if (mem == SBS_MEM_HOST) {
         scr.s = s;
-        SBS_CUDA_TRY(cudaMallocAsync(&scr.p, 5 * n * sizeof(float) + lut_bytes + 16, s));
+        SBS_CUDA_TRY(scratch_alloc((void **)&scr.p, 5 * n * sizeof(float) + lut_bytes + 16, s));
         float *base = (float *)scr.p;
         dt = base;
         dc = base + n;
@@ -670,7 +670,7 @@ int sbs_lut2d_lookup_batch(const double *lut, uint32_t T, uint32_t A, double tmi
     Scratch scr;
     if (mem == SBS_MEM_HOST) {
         scr.s = s;
-        SBS_CUDA_TRY(cudaMallocAsync(&scr.p, (5 * n + lut_n) * sizeof(double), s));
+        SBS_CUDA_TRY(scratch_alloc((void **)&scr.p, (5 * n + lut_n) * sizeof(double), s));
         double *base = (double *)scr.p;
         SBS_CUDA_TRY(cudaMemcpyAsync(base, t_nm, n * sizeof(double), cudaMemcpyHostToDevice, s));
         SBS_CUDA_TRY(cudaMemcpyAsync(base + n, cos_i, n * sizeof(double), cudaMemcpyHostToDevice, s));

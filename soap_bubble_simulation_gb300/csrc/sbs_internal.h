@@ -35,6 +35,12 @@ void clear_error();
 // Makes sure a CUDA device exists and the runtime is usable; fails with SBS_E_CUDA otherwise.
 int require_device();
 
+// Stream-ordered scratch for one call (release it with cudaFreeAsync on the same stream). Blocks of
+// up to 64 MB come from a per-device pool that keeps freed memory for the next call (the default
+// pool returns it to the system at every synchronisation, and mapping it again costs ~100 us);
+// larger blocks come from the default pool.
+cudaError_t scratch_alloc(void **p, size_t bytes, cudaStream_t s);
+
 // WGSL-semantics passes (params.dt each) enqueued on the handle's stream without a final
 // synchronisation (sbs_gpu_drainage_run minus the wait).
 int drainage_run_async(sbs_drainage *h, uint32_t passes);

@@ -22,8 +22,6 @@
 
 #include <cmath>
 #include <cstring>
-#include <map>
-#include <mutex>
 #include <vector>
 
 #include "cell.cuh"
@@ -326,34 +324,7 @@ cudaError_t launch_tc(const float *t, const float *ci, const float *nf, size_t n
 
 using namespace sbs;
 
-namespace {
 
-// A per-device memory pool whose release threshold keeps freed memory for reuse.
-int keep_pool(cudaMemPool_t *out) {
-    static std::mutex mu;
-    static std::map<int, cudaMemPool_t> pools;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return set_error(SBS_E_CUDA, "cudaGetDevice failed");
-    std::lock_guard<std::mutex> lock(mu);
-    auto it = pools.find(dev);
-    if (it != pools.end()) {
-        *out = it->second;
-        return SBS_OK;
-    }
-    cudaMemPoolProps props{};
-    props.allocType = cudaMemAllocationTypePinned;
-    props.location.type = cudaMemLocationTypeDevice;
-    props.location.id = dev;
-    cudaMemPool_t pool = nullptr;
-    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) return set_error(SBS_E_CUDA, "cudaMemPoolCreate failed");
-    uint64_t keep = UINT64_MAX;
-    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
-    pools[dev] = pool;
-    *out = pool;
-    return SBS_OK;
-}
-
-}  // namespace
 
 extern "C" int sbs_spectral_rgb(const float *t_nm, const float *cos_i, const float *n_film, size_t n,
                                 const float *wl_nm, uint32_t nl, const float *cmf, int mode, float *rgb, int mem,
@@ -388,19 +359,10 @@ extern "C" int sbs_spectral_rgb(const float *t_nm, const float *cos_i, const flo
             std::memcpy(btile + tile_off(ch, (int)l, sbo), &v, 2);
         }
 
-    // scratch: the timeout flag, plus staging buffers for host inputs. Device-memory calls take the
-    // flag from a pool that keeps its memory (the default pool returns it to the system at every
-    // synchronisation, and mapping it again costs more than this kernel's launch).
+    // scratch: the timeout flag, plus staging buffers for host inputs
     const size_t in_bytes = 3 * n * sizeof(float), out_bytes = 3 * n * sizeof(float);
     char *base = nullptr;
-    if (mem == SBS_MEM_HOST) {
-        SBS_CUDA_TRY(cudaMallocAsync((void **)&base, 256 + in_bytes + out_bytes, s));
-    } else {
-        cudaMemPool_t pool = nullptr;
-        rc = keep_pool(&pool);
-        if (rc) return rc;
-        SBS_CUDA_TRY(cudaMallocFromPoolAsync((void **)&base, 256, pool, s));
-    }
+    SBS_CUDA_TRY(scratch_alloc((void **)&base, 256 + (mem == SBS_MEM_HOST ? in_bytes + out_bytes : 0), s));
     unsigned *d_err = reinterpret_cast<unsigned *>(base);
     const float *dt = t_nm, *dc = cos_i, *dn = n_film;
     float *dout = rgb;

@@ -35,7 +35,7 @@ extern "C" int sbs_film_volume_device(const float *h, uint32_t num_theta, uint32
     // scratch: weights, per-block partials, arrival counter, result
     const size_t bytes = sizeof(double) * (size_t)nt + sizeof(double) * 3 * nb + sizeof(ReduceOut) + 16;
     char *scratch = nullptr;
-    SBS_CUDA_TRY(cudaMallocAsync((void **)&scratch, bytes, s));
+    SBS_CUDA_TRY(scratch_alloc((void **)&scratch, bytes, s));
     double *w = (double *)scratch;
     double *partials = w + nt;
     ReduceOut *res = (ReduceOut *)(partials + 3 * nb);
