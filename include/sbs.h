@@ -394,6 +394,58 @@ int sbs_foam_stream(const sbs_foam *f, void **out);
 int sbs_spectral_rgb(const float *t_nm, const float *cos_i, const float *n_film, size_t n, const float *wl_nm,
                      uint32_t nl, const float *cmf, int mode, float *rgb, int mem, void *stream);
 
+/* ------------------------------------------------------------------ */
+/* Headless film shading: the bubble fragment shader as a CUDA kernel  */
+/* ------------------------------------------------------------------ */
+/* The renderer's per-bubble uniform, field for field (pipeline.rs:23-67,
+ * 128 bytes; the same #[repr(C)] layout the renderer uploads). */
+typedef struct sbs_bubble_uniform {
+    float refractive_index, base_thickness_nm, time, interference_intensity;
+    float base_alpha, edge_alpha, background_r, background_g, background_b;
+    float film_time, swirl_intensity, drainage_speed, pattern_scale;
+    float position_x, position_y, position_z;
+    uint32_t edge_smoothing_mode; /* 0 linear, 1 smoothstep, 2 power 1.5 */
+    uint32_t branched_flow_enabled;
+    float branched_flow_intensity, branched_flow_scale, branched_flow_sharpness;
+    float light_dir_x, light_dir_y, light_dir_z;
+    uint32_t patch_enabled;
+    float patch_center_u, patch_center_v, patch_half_size;
+    uint32_t padding[4];
+} sbs_bubble_uniform;
+
+#define SBS_LUT_ANGLES 64       /* generate_interference_lut rows (cos theta 0..1) */
+#define SBS_LUT_THICKNESSES 256 /* columns (0..2000 nm) */
+#define SBS_BRANCHED_W 512      /* branched-flow texture (bubble.wgsl:59-60), u32 value * 256 */
+#define SBS_BRANCHED_H 256
+
+/* BubbleUniform::default() (pipeline.rs:69-111). */
+int sbs_bubble_uniform_default(sbs_bubble_uniform *out);
+
+/* Colour and alpha of n fragments (fs_main, bubble.wgsl:486-545): unit-sphere
+ * normals and world positions [n][3] in, straight-alpha rgba [n][4] out (the
+ * fragment output before blending). The thickness is the procedural film of
+ * get_film_thickness (:200-229: drainage term, 4-octave simplex FBM, swirl
+ * noise, gravity ripple), the colour the LUT of generate_interference_lut
+ * ([64 angle][256 thickness][4] RGBA8) sampled bilinearly at texel centres
+ * with clamp-to-edge (pipeline.rs:350-359), black film below 30 nm. branched
+ * is the 512 x 256 branched-flow texture or null (then the term is off, as
+ * when branched_flow_enabled = 0). mem applies to every array. */
+int sbs_shade_fragments(const sbs_bubble_uniform *u, const float camera_pos[3], const uint8_t *lut,
+                        const uint32_t *branched, size_t n, const float *normal, const float *world_pos, float *rgba,
+                        int mem, void *stream);
+/* One headless frame (the reference's headless renderer, render/headless.rs):
+ * every pixel of a width x height target casts a ray through view_proj
+ * (column-major 4 x 4, wgpu clip space, depth 0..1) from camera_pos; where it
+ * meets the sphere of `radius` around the uniform's position the front
+ * surface is shaded as in sbs_shade_fragments and alpha-blended over the
+ * background (BlendState::ALPHA_BLENDING over a clear of the background colour
+ * with alpha 1; the source clamped to 0..1 as for a unorm target). Outputs,
+ * either may be null: rgba8 [height][width][4] sRGB-encoded as an
+ * Rgba8UnormSrgb target stores it, linear [height][width][4] f32. */
+int sbs_shade_frame(const sbs_bubble_uniform *u, const float view_proj[16], const float camera_pos[3], float radius,
+                    const uint8_t *lut, const uint32_t *branched, uint32_t width, uint32_t height, uint8_t *rgba8,
+                    float *linear, int mem, void *stream);
+
 
 /* ------------------------------------------------------------------ */
 /* Drainage surrogate: conv neural operator over SBS_NN_STEPS passes   */

@@ -16,7 +16,7 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
-SOURCES = ["drainage.cpp", "interference.cpp", "surrogate.cpp"]
+SOURCES = ["drainage.cpp", "interference.cpp", "surrogate.cpp", "shade.cpp"]
 CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
 
 
@@ -30,7 +30,8 @@ def _stale(lib: str, deps: list[str]) -> bool:
 def build(force: bool = False) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     srcs = [os.path.join(HERE, s) for s in SOURCES]
-    deps = srcs + [os.path.join(HERE, "oracle.h"), os.path.join(HERE, "..", "include", "sbs_nn.h"), __file__]
+    deps = srcs + [os.path.join(HERE, "oracle.h"), os.path.join(HERE, "..", "include", "sbs_nn.h"),
+            os.path.join(HERE, "..", "include", "sbs.h"), __file__]
     if not force and not _stale(LIB, deps):
         return LIB
     cxx = os.environ.get("CXX", "g++")

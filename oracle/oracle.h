@@ -28,6 +28,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include "../include/sbs.h" /* interface types only (sbs_bubble_uniform, texture sizes) */
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -179,6 +181,20 @@ float orc_nn_gelu(float x);
 float orc_nn_gelu_grad(float x);
 float orc_nn_hswish(float x);
 float orc_nn_hswish_grad(float x);
+
+/* ------------------------------------------------------------------ */
+/* Bubble fragment shader (bubble.wgsl) and headless frame             */
+/* ------------------------------------------------------------------ */
+/* simplex_noise_3d (bubble.wgsl:113-180) and get_film_thickness (:203-229) */
+float orc_simplex3(float x, float y, float z);
+float orc_film_thickness(const sbs_bubble_uniform *u, float nx, float ny, float nz);
+/* fs_main (:486-545) for n fragments: normal, wpos [n][3] -> rgba [n][4] (straight alpha) */
+void orc_shade_fragments(const sbs_bubble_uniform *u, const float cam[3], const uint8_t *lut, const uint32_t *tex,
+                         size_t n, const float *normal, const float *wpos, float *rgba);
+/* one headless frame (render/headless.rs), as sbs_shade_frame; -1 if view_proj is singular */
+int orc_shade_frame(const sbs_bubble_uniform *u, const float view_proj[16], const float cam[3], float radius,
+                    const uint8_t *lut, const uint32_t *tex, uint32_t width, uint32_t height, uint8_t *rgba8,
+                    float *linear);
 
 #ifdef __cplusplus
 }

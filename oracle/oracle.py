@@ -107,6 +107,10 @@ _SIGS = {
     "orc_nn_forward": ([_P, _U32, _U32, _U32, _P, _P, _I], None),
     "orc_nn_loss_grad": ([_P, _U32, _U32, _U32, _P, _P, _P, _I], _D),
     "orc_nn_apply": ([_P, _P, _U32, _U32, _F, _P], None),
+    "orc_simplex3": ([_F, _F, _F], _F),
+    "orc_film_thickness": ([_P, _F, _F, _F], _F),
+    "orc_shade_fragments": ([_P, _P, _P, _P, C.c_size_t, _P, _P, _P], None),
+    "orc_shade_frame": ([_P, _P, _P, _F, _P, _P, _U32, _U32, _P, _P], _I),
     "orc_nn_gelu": ([_F], _F),
     "orc_nn_gelu_grad": ([_F], _F),
     "orc_nn_hswish": ([_F], _F),
@@ -416,3 +420,41 @@ def nn_hswish(x: float) -> float:
 
 def nn_hswish_grad(x: float) -> float:
     return float(lib().orc_nn_hswish_grad(float(x)))
+
+
+# ---------------------------------------------------------------------- bubble fragment shader
+def simplex3(x: float, y: float, z: float) -> float:
+    return float(lib().orc_simplex3(float(x), float(y), float(z)))
+
+
+def film_thickness(uniform, n) -> float:
+    """get_film_thickness for one unit normal; uniform is a ctypes structure laid out as
+    sbs_bubble_uniform."""
+    return float(lib().orc_film_thickness(C.cast(C.byref(uniform), C.c_void_p), float(n[0]), float(n[1]), float(n[2])))
+
+
+def shade_fragments(uniform, camera_pos, lut, normals, world_pos, branched=None) -> np.ndarray:
+    nn = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+    wp = np.ascontiguousarray(world_pos, dtype=np.float32).reshape(-1, 3)
+    cam = np.ascontiguousarray(camera_pos, dtype=np.float32).reshape(3)
+    L = np.ascontiguousarray(lut, dtype=np.uint8)
+    B = None if branched is None else np.ascontiguousarray(branched, dtype=np.uint32)
+    out = np.empty((nn.shape[0], 4), dtype=np.float32)
+    lib().orc_shade_fragments(C.cast(C.byref(uniform), C.c_void_p), _p(cam), _p(L), _p(B) if B is not None else None,
+                              nn.shape[0], _p(nn), _p(wp), _p(out))
+    return out
+
+
+def shade_frame(uniform, view_proj, camera_pos, radius, lut, width, height, branched=None):
+    """(rgba8 [h][w][4], linear [h][w][4]) of one headless frame."""
+    vp = np.ascontiguousarray(view_proj, dtype=np.float32).reshape(16)
+    cam = np.ascontiguousarray(camera_pos, dtype=np.float32).reshape(3)
+    L = np.ascontiguousarray(lut, dtype=np.uint8)
+    B = None if branched is None else np.ascontiguousarray(branched, dtype=np.uint32)
+    rgba8 = np.empty((height, width, 4), dtype=np.uint8)
+    lin = np.empty((height, width, 4), dtype=np.float32)
+    rc = lib().orc_shade_frame(C.cast(C.byref(uniform), C.c_void_p), _p(vp), _p(cam), float(radius), _p(L),
+                               _p(B) if B is not None else None, int(width), int(height), _p(rgba8), _p(lin))
+    if rc != 0:
+        raise ValueError("singular view_proj")
+    return rgba8, lin

@@ -1,7 +1,8 @@
 """GB300-native film-drainage and thin-film-interference path of the soap-bubble simulation.
 
 Drop-in for the reference's `physics::drainage`, `physics::interference` and
-`render::{gpu_drainage, interference_lut}` APIs, computed by hand-written
+`render::{gpu_drainage, interference_lut}` APIs, plus the bubble fragment shader as a headless
+frame (`render_frame`), computed by hand-written
 CUDA kernels for sm_103a behind the C ABI in include/sbs.h (libsbs.so).
 """
 from . import _native
@@ -16,6 +17,7 @@ from .interference import (LUT_ANGLE_SAMPLES, LUT_MAX_THICKNESS_NM, LUT_THICKNES
 from ._native import SbsError
 from .foam import FoamDrainage
 from .surrogate import SURROGATE_STEPS, DrainageSurrogate, field_params, masked_error
+from .shading import BubbleUniform, Camera, render_frame, shade_fragments
 
 __all__ = [
     "BubbleParameters", "ConfigError", "EnvironmentParameters", "FluidParameters", "SimulationConfig",
@@ -24,5 +26,5 @@ __all__ = [
     "FresnelCoefficients", "InterferenceCalculator", "RgbColor", "constants", "generate_interference_lut",
     "generate_interference_lut_array", "lookup_2d", "sample_interference_lut", "schlick_interference_rgb", "spectral_rgb",
     "wavelengths", "SbsError", "FoamDrainage", "SURROGATE_STEPS", "DrainageSurrogate", "field_params",
-    "masked_error",
+    "masked_error", "BubbleUniform", "Camera", "render_frame", "shade_fragments",
 ]

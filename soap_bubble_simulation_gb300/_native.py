@@ -192,6 +192,9 @@ SIGNATURES: dict[str, list] = {
     "sbs_foam_autotune": [_P, _U32, _U32P, _U32P],
     "sbs_foam_stream": [_P, C.POINTER(_P)],
     "sbs_spectral_rgb": [_P, _P, _P, _SZ, _P, _U32, _P, _I, _P, _I, _P],
+    "sbs_bubble_uniform_default": [_P],
+    "sbs_shade_fragments": [_P, _P, _P, _P, _SZ, _P, _P, _P, _I, _P],
+    "sbs_shade_frame": [_P, _P, _P, _F, _P, _P, _U32, _U32, _P, _P, _I, _P],
     "sbs_drainage_vertex_colors": [_P, _P, _SZ, _P, _U32, _U32, _D, _D, _P, _I],
     "sbs_surrogate_create": [C.c_uint64, C.POINTER(_P)],
     "sbs_surrogate_destroy": [_P],
