@@ -26,6 +26,7 @@ default), `surrogate_hswish` the same network, data and schedule with hard-swish
 foam / spectral: the batched-foam and spectral-contraction workloads, device-resident.
 c0: the small configuration's latency-bound calls (1000 steps at resolution 128 in both
 semantics, the colour LUTs, colours at 10,242 icosphere vertices), host in and host out.
+shading: one 3840 x 2160 headless frame of the bubble fragment shader, pixels/s.
 
 --impl reference: times that CPU restatement alone (the reference is Rust and cannot be
 built here), same metric and config.
@@ -354,6 +355,51 @@ def c0_section(sbs, synthetic, torch):
             "vertex_colors": {"vertices": int(len(xyz)), "ms": t_vert * 1e3, "points_per_s": len(xyz) / t_vert}}
 
 
+def shade_section(sbs, torch):
+    """Headless film shading: one 3840 x 2160 frame of the bubble fragment shader (RGBA8 sRGB out),
+    camera at 6 cm so that the bubble covers most of the frame; device-resident (CUDA events) and
+    through the host call (frame copied back)."""
+    from soap_bubble_simulation_gb300 import shading as sh
+
+    N = sbs._native
+    w, h = 3840, 2160
+    u = sh.BubbleUniform.default()
+    u.set_time(2.0)
+    cam = sh.Camera(aspect=w / h, distance=0.06)
+    vp, pos = cam.view_proj(), cam.position().astype(np.float32)
+    lut = torch.from_numpy(sh.default_lut(1.33).copy()).cuda()
+    out8 = torch.empty((h, w, 4), dtype=torch.uint8, device="cuda")
+    st = torch.cuda.current_stream()
+
+    def run():
+        N.call("sbs_shade_frame", ctypes.cast(ctypes.byref(u), ctypes.c_void_p), N.ptr(vp), N.ptr(pos),
+               float(sh.HEADLESS_RADIUS), ctypes.c_void_p(lut.data_ptr()), None, w, h,
+               ctypes.c_void_p(out8.data_ptr()), None, N.MEM_DEVICE, ctypes.c_void_p(st.cuda_stream))
+
+    for _ in range(3):
+        run()
+    reps = 20
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    for _ in range(reps):
+        run()
+    b.record(st)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / reps
+    frame = out8.cpu().numpy()
+    bg = np.array([round(255 * (1.055 * x ** (1 / 2.4) - 0.055)) for x in (0.1, 0.1, 0.15)])
+    cover = float(np.any(frame[..., :3] != bg, axis=-1).mean())
+    sh.render_frame(u, cam, w, h)
+    ta = time.perf_counter()
+    for _ in range(5):
+        sh.render_frame(u, cam, w, h)
+    e2e_ms = (time.perf_counter() - ta) / 5 * 1e3
+    return {"value": w * h / (ms * 1e-3), "unit": "pixels/s", "ms_per_frame": ms, "frame": f"{w} x {h}",
+            "bubble_coverage": cover, "bytes_out_per_pixel": 4,
+            "e2e": {"value": w * h / (e2e_ms * 1e-3), "unit": "pixels/s", "ms_per_frame": e2e_ms,
+                    "d2h_bytes_per_frame": 4 * w * h}}
+
+
 def spectral_section(sbs, synthetic, torch):
     N = sbs._native
     n = 8_388_608
@@ -525,9 +571,10 @@ def main():
     cpu_sem_ms = a_ev.elapsed_time(b_ev)
     cpu_sem_rate = cells * 2000 / (cpu_sem_ms / 1e3)
 
-    surrogate = foam = spectral = small = None
+    surrogate = foam = spectral = small = shade = None
     if not args.skip_aux:
         small = c0_section(sbs, synthetic, torch)
+        shade = shade_section(sbs, torch)
         surrogate = surrogate_section(sbs, synthetic, h0, c0, torch)
         foam = foam_section(sbs, synthetic, torch)
         spectral = spectral_section(sbs, synthetic, torch)
@@ -570,6 +617,7 @@ def main():
             "foam": foam,
             "spectral": spectral,
             "c0": small,
+            "shading": shade,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

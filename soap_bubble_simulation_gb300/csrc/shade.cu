@@ -47,8 +47,23 @@ struct V4 {
 
 __device__ __forceinline__ float dot3(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ float dot4(V4 a, V4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
-// WGSL % on f32 (the values here are integers below 2^24: exact)
-__device__ __forceinline__ float mod289(float x) { return fmodf(x, 289.f); }
+// WGSL % on f32 by 289, i.e. fmodf(x, 289): truncated quotient, result with the sign of x. Every
+// argument here is an integer-valued float; below 2^24 the quotient x * (1/289) truncates to the
+// exact one or one off, the remainder x - 289 q is exact, and one correction step gives fmodf's
+// result bit for bit (copysignf keeps the sign of a zero remainder). Larger magnitudes take fmodf.
+__device__ __forceinline__ float mod289(float x) {
+    if (!(fabsf(x) < 16777216.f)) return fmodf(x, 289.f);
+    const float q = truncf(x * (1.f / 289.f));
+    float r = x - q * 289.f;
+    if (x >= 0.f) {
+        if (r >= 289.f) r -= 289.f;
+        else if (r < 0.f) r += 289.f;
+    } else {
+        if (r <= -289.f) r += 289.f;
+        else if (r > 0.f) r -= 289.f;
+    }
+    return copysignf(r, x);
+}
 // permute (bubble.wgsl:105-107), one component
 __device__ __forceinline__ float permute1(float x) { return mod289((x * 34.f + 1.f) * x); }
 // step(edge, x) = x >= edge

@@ -7,7 +7,8 @@ semantics, compensated f32x2), `cpu32` (plain f32), `spectral-tc` / `spectral-fp
 spectral colour of --points seeded points, tensor-core or FP32 contraction), `surrogate-fused` /
 `surrogate-layered` (--steps 64-pass surrogate intervals of the field, untrained seeded weights:
 the same kernels and shapes as a trained network; --activation gelu or hswish), `foam` (the 4096-bubble foam batch, --steps
-steps with the default tiles). The field is the seeded smooth-mode field of
+steps with the default tiles), `shade` (--steps 3840 x 2160 headless frames of the bubble
+fragment shader). The field is the seeded smooth-mode field of
 the 2048-resolution workload, built at the requested resolution. Steps launch one kernel each
 (graph replay for runs of 8 or more).
 """
@@ -26,7 +27,7 @@ def main(argv=None) -> None:
     p = argparse.ArgumentParser()
     p.add_argument("--case", default="wgsl",
                    choices=["wgsl", "cpu", "cpu32", "spectral-tc", "spectral-fp32", "surrogate-fused", "surrogate-layered",
-                            "foam"])
+                            "foam", "shade"])
     p.add_argument("--points", type=int, default=1 << 20, help="spectral cases: number of points")
     p.add_argument("--res", type=int, default=2048)
     p.add_argument("--steps", type=int, default=20)
@@ -43,6 +44,16 @@ def main(argv=None) -> None:
         for _ in range(a.steps):
             spectral_rgb(t, ci, nf, wl, cmf, mode="tc" if a.case == "spectral-tc" else "fp32")
         print(f"ran {a.steps} spectral evaluations of {a.points} points ({a.case})")
+        return
+    if a.case == "shade":
+        from .shading import BubbleUniform, Camera, render_frame
+
+        u = BubbleUniform.default()
+        u.set_time(2.0)
+        cam = Camera(aspect=16 / 9, distance=0.06)
+        for _ in range(a.steps):
+            render_frame(u, cam, 3840, 2160)
+        print(f"shaded {a.steps} 3840 x 2160 frames")
         return
     if a.case == "foam":
         from .foam import FoamDrainage
