@@ -446,6 +446,36 @@ int sbs_shade_frame(const sbs_bubble_uniform *u, const float view_proj[16], cons
                     const uint8_t *lut, const uint32_t *branched, uint32_t width, uint32_t height, uint8_t *rgba8,
                     float *linear, int mem, void *stream);
 
+/* ------------------------------------------------------------------ */
+/* Caustic intensity map over the drained thickness                    */
+/* ------------------------------------------------------------------ */
+/* CausticParams (caustics.rs:17-52, 64 bytes, the same #[repr(C)] layout). */
+typedef struct sbs_caustic_params {
+    uint32_t grid_width, grid_height;
+    float refractive_index, film_thickness_scale;
+    float light_dir_x, light_dir_y, light_dir_z, light_intensity;
+    float focal_length, caustic_intensity, caustic_sharpness, branch_threshold;
+    float ground_y, bubble_radius, time;
+    uint32_t padding;
+} sbs_caustic_params;
+
+/* CausticParams::default() (caustics.rs:54-76). */
+int sbs_caustic_params_default(sbs_caustic_params *out);
+/* The caustic compute pass (caustics_compute.wgsl:1-126): caustic_map
+ * [grid_height][grid_width] from the thickness field [grid_height][pitch]
+ * (pitch >= grid_width elements; phi wrapped, theta clamped). To map a drainage
+ * handle's field without a copy, pass sbs_drainage_thickness_device's pointer
+ * and pitch with SBS_MEM_DEVICE and the handle's stream
+ * (sbs_drainage_stream); which = 1 there is the buffer the reference binds
+ * (gpu_drainage.rs:478). */
+int sbs_caustics(const sbs_caustic_params *p, const float *thickness, size_t pitch, float *caustic_map, int mem,
+                 void *stream);
+/* The caustic pass over a WGSL-semantics handle's field (which as in
+ * sbs_drainage_thickness_device), on the handle's stream, no copy of the
+ * field; p's grid must equal the handle's. caustic_map per mem (host: the call
+ * returns when the map is there; device: ordered on the handle's stream). */
+int sbs_gpu_drainage_caustics(sbs_drainage *h, const sbs_caustic_params *p, int which, float *caustic_map, int mem);
+
 
 /* ------------------------------------------------------------------ */
 /* Drainage surrogate: conv neural operator over SBS_NN_STEPS passes   */

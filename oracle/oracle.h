@@ -196,6 +196,9 @@ int orc_shade_frame(const sbs_bubble_uniform *u, const float view_proj[16], cons
                     const uint8_t *lut, const uint32_t *tex, uint32_t width, uint32_t height, uint8_t *rgba8,
                     float *linear);
 
+/* caustic compute pass (caustics_compute.wgsl:1-126): out [grid_height][grid_width] */
+void orc_caustics(const sbs_caustic_params *p, const float *h, size_t pitch, float *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -107,6 +107,7 @@ _SIGS = {
     "orc_nn_forward": ([_P, _U32, _U32, _U32, _P, _P, _I], None),
     "orc_nn_loss_grad": ([_P, _U32, _U32, _U32, _P, _P, _P, _I], _D),
     "orc_nn_apply": ([_P, _P, _U32, _U32, _F, _P], None),
+    "orc_caustics": ([_P, _P, C.c_size_t, _P], None),
     "orc_simplex3": ([_F, _F, _F], _F),
     "orc_film_thickness": ([_P, _F, _F, _F], _F),
     "orc_shade_fragments": ([_P, _P, _P, _P, C.c_size_t, _P, _P, _P], None),
@@ -458,3 +459,13 @@ def shade_frame(uniform, view_proj, camera_pos, radius, lut, width, height, bran
     if rc != 0:
         raise ValueError("singular view_proj")
     return rgba8, lin
+
+
+# ---------------------------------------------------------------------- caustics
+def caustics(params, h) -> np.ndarray:
+    """Caustic map of a [grid_height][grid_width] float32 field; params a ctypes structure laid out as
+    sbs_caustic_params."""
+    h = np.ascontiguousarray(h, dtype=np.float32)
+    out = np.empty((params.grid_height, params.grid_width), dtype=np.float32)
+    lib().orc_caustics(C.cast(C.byref(params), C.c_void_p), _p(h), h.shape[1], _p(out))
+    return out

@@ -18,6 +18,7 @@ from ._native import SbsError
 from .foam import FoamDrainage
 from .surrogate import SURROGATE_STEPS, DrainageSurrogate, field_params, masked_error
 from .shading import BubbleUniform, Camera, render_frame, shade_fragments
+from .caustics import CausticParams, caustic_map
 
 __all__ = [
     "BubbleParameters", "ConfigError", "EnvironmentParameters", "FluidParameters", "SimulationConfig",
@@ -26,5 +27,5 @@ __all__ = [
     "FresnelCoefficients", "InterferenceCalculator", "RgbColor", "constants", "generate_interference_lut",
     "generate_interference_lut_array", "lookup_2d", "sample_interference_lut", "schlick_interference_rgb", "spectral_rgb",
     "wavelengths", "SbsError", "FoamDrainage", "SURROGATE_STEPS", "DrainageSurrogate", "field_params",
-    "masked_error", "BubbleUniform", "Camera", "render_frame", "shade_fragments",
+    "masked_error", "BubbleUniform", "Camera", "render_frame", "shade_fragments", "CausticParams", "caustic_map",
 ]

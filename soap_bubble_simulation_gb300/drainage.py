@@ -449,6 +449,19 @@ class GPUDrainageSimulator(_Handle):
         step that is the last pass's input, one pass behind current_thickness_buffer()."""
         return self._device_view("sbs_drainage_thickness_device", 1)
 
+    def caustic_map(self, params=None, which: int = 0) -> np.ndarray:
+        """The caustic compute pass (caustics_compute.wgsl) over this simulator's thickness, on its
+        stream without a copy of the field. which = 1 reads the buffer the reference's caustic
+        renderer binds (current_buffer())."""
+        from .caustics import CausticParams
+
+        nt, np_ = self.grid()
+        p = params if params is not None else CausticParams.default(np_, nt)
+        out = np.empty((nt, np_), dtype=np.float32)
+        N.call("sbs_gpu_drainage_caustics", self.handle, C.cast(C.byref(p), C.c_void_p), int(which), N.ptr(out),
+               N.MEM_HOST)
+        return out
+
     def concentration_buffer(self) -> DeviceField:
         """The reference's concentration_buffer() (gpu_drainage.rs:458-460), same indexing as
         current_buffer()."""
