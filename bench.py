@@ -27,6 +27,7 @@ foam / spectral: the batched-foam and spectral-contraction workloads, device-res
 c0: the small configuration's latency-bound calls (1000 steps at resolution 128 in both
 semantics, the colour LUTs, colours at 10,242 icosphere vertices), host in and host out.
 shading: one 3840 x 2160 headless frame of the bubble fragment shader, pixels/s.
+caustics: the caustic pass over the drained 2048 x 4096 field, on the simulator's device field.
 
 --impl reference: times that CPU restatement alone (the reference is Rust and cannot be
 built here), same metric and config.
@@ -400,6 +401,45 @@ def shade_section(sbs, torch):
                     "d2h_bytes_per_frame": 4 * w * h}}
 
 
+def caustics_section(sbs, synthetic, torch, h0, c0):
+    """The caustic pass over the 2048 x 4096 field after a drainage run, on the simulator's own
+    device field (no copy): 8 algorithmic bytes per cell (read h, write the map)."""
+    from soap_bubble_simulation_gb300.caustics import CausticParams
+
+    N = sbs._native
+    nt, np_ = h0.shape
+    sim = sbs.GPUDrainageSimulator(None, 550e-9, np_, nt)
+    sim.set_thickness_array(h0)
+    sim.set_concentration_array(c0)
+    sim.run(100)
+    p = CausticParams.default(np_, nt)
+    out = torch.empty((nt, np_), device="cuda")
+    st = torch.cuda.ExternalStream(sim.stream())
+
+    def run():
+        N.call("sbs_gpu_drainage_caustics", sim.handle, ctypes.cast(ctypes.byref(p), ctypes.c_void_p), 0,
+               ctypes.c_void_p(out.data_ptr()), N.MEM_DEVICE)
+
+    for _ in range(3):
+        run()
+    reps = 50
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    for _ in range(reps):
+        run()
+    b.record(st)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / reps
+    sim.close()
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    gbs = 8.0 * h0.size / (ms * 1e-3) / 1e9
+    return {"value": h0.size / (ms * 1e-3), "unit": "cells/s", "us_per_map": ms * 1e3, "grid": f"{nt} x {np_}",
+            "hbm": {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                    "bytes_per_cell": 8}}
+
+
 def spectral_section(sbs, synthetic, torch):
     N = sbs._native
     n = 8_388_608
@@ -571,10 +611,11 @@ def main():
     cpu_sem_ms = a_ev.elapsed_time(b_ev)
     cpu_sem_rate = cells * 2000 / (cpu_sem_ms / 1e3)
 
-    surrogate = foam = spectral = small = shade = None
+    surrogate = foam = spectral = small = shade = caus = None
     if not args.skip_aux:
         small = c0_section(sbs, synthetic, torch)
         shade = shade_section(sbs, torch)
+        caus = caustics_section(sbs, synthetic, torch, h0, c0)
         surrogate = surrogate_section(sbs, synthetic, h0, c0, torch)
         foam = foam_section(sbs, synthetic, torch)
         spectral = spectral_section(sbs, synthetic, torch)
@@ -618,6 +659,7 @@ def main():
             "spectral": spectral,
             "c0": small,
             "shading": shade,
+            "caustics": caus,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

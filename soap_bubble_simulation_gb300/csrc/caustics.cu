@@ -3,10 +3,12 @@
 // determinant of the 9-point Hessian of the thickness field (phi wrapped, theta clamped), turned
 // into a focusing x branching x refraction factor, raised to the caustic sharpness and scaled.
 //
-// One thread per cell; a block stages its 32 x 8 cells plus a one-cell halo in shared memory, so
-// the field is read from HBM once and the map written once: 8 bytes per cell, HBM-bound. The
-// arithmetic follows the WGSL in FP32 left to right without contraction; only pow differs from a
-// CPU restatement, by its rounding.
+// One thread per column walks 16 rows with the three rows of the stencil in registers (one new
+// row of three loads per cell, two of them L1 hits), so the field is read from HBM once and the
+// map written once: 8 bytes per cell, HBM-bound. The arithmetic follows the WGSL in FP32 left to
+// right without contraction. pow(x, y) is evaluated as exp2(y log2 x) on the special-function unit,
+// as GPU shader compilers evaluate WGSL pow (x >= 0.01 here); it agrees with a correctly rounded
+// pow to ~6e-7 relative.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -17,30 +19,35 @@
 namespace sbs {
 namespace {
 
-constexpr int kTX = 32, kTY = 8;
+constexpr int kCols = 128;  // threads (columns) per block
+constexpr int kRows = 16;   // rows a thread walks down
 
-__global__ void __launch_bounds__(kTX *kTY) caustics_kernel(sbs_caustic_params p, const float *__restrict__ h,
-                                                            size_t pitch, float *__restrict__ out) {
-    __shared__ float tile[kTY + 2][kTX + 2];
-    const int W = (int)p.grid_width, H = (int)p.grid_height;
-    const int x0 = blockIdx.x * kTX - 1, y0 = blockIdx.y * kTY - 1;
-    const int tid = threadIdx.y * kTX + threadIdx.x;
-    for (int k = tid; k < (kTY + 2) * (kTX + 2); k += kTX * kTY) {
-        const int ty = k / (kTX + 2), tx = k % (kTX + 2);
-        int sx = (x0 + tx) % W;  // sample_thickness: x wrapped, y clamped
-        if (sx < 0) sx += W;
-        const int sy = min(max(y0 + ty, 0), H - 1);
-        tile[ty][tx] = __ldg(h + (size_t)sy * pitch + sx);
-    }
-    __syncthreads();
-    const int x = blockIdx.x * kTX + threadIdx.x, y = blockIdx.y * kTY + threadIdx.y;
-    if (x >= W || y >= H) return;
-    const int cx = threadIdx.x + 1, cy = threadIdx.y + 1;
-    const float center = tile[cy][cx];
-    const float left = tile[cy][cx - 1], right = tile[cy][cx + 1];
-    const float up = tile[cy - 1][cx], down = tile[cy + 1][cx];
-    const float ul = tile[cy - 1][cx - 1], ur = tile[cy - 1][cx + 1];
-    const float dl = tile[cy + 1][cx - 1], dr = tile[cy + 1][cx + 1];
+struct Row {
+    float l, c, r;
+};
+
+// pow(x, y) for x > 0 through the special-function unit: 2^(y log2 x) with the hardware base-2
+// logarithm and exponential (each ~2^-22 relative), i.e. well below 1e-6 relative for the
+// exponents and magnitudes of this pass.
+__device__ __forceinline__ float pow_sfu(float x, float y) {
+    float l, r;
+    asm("lg2.approx.f32 %0, %1;" : "=f"(l) : "f"(x));
+    const float e = y * l;
+    asm("ex2.approx.f32 %0, %1;" : "=f"(r) : "f"(e));
+    return r;
+}
+
+__device__ __forceinline__ Row load_row(const float *__restrict__ h, size_t pitch, int H, int y, int xl, int x,
+                                        int xr) {
+    const float *p = h + (size_t)min(max(y, 0), H - 1) * pitch;  // theta clamped
+    return Row{__ldg(p + xl), __ldg(p + x), __ldg(p + xr)};
+}
+
+// compute_caustic_intensity (caustics_compute.wgsl:87-111) from the 3 x 3 neighbourhood:
+// a = row above (y - 1), b = the cell's row, c = row below (y + 1)
+__device__ __forceinline__ float intensity(const sbs_caustic_params &p, Row a, Row b, Row c) {
+    const float center = b.c, left = b.l, right = b.r, up = a.c, down = c.c;
+    const float ul = a.l, ur = a.r, dl = c.l, dr = c.r;
     // thickness_gradient (h = 1)
     const float gx = (right - left) / 2.0f, gy = (down - up) / 2.0f;
     // thickness_laplacian
@@ -50,16 +57,34 @@ __global__ void __launch_bounds__(kTX *kTY) caustics_kernel(sbs_caustic_params p
     const float d2y = (up + down - 2.0f * center) / 1.0f;
     const float dxy = (dr - dl - ur + ul) / 4.0f;
     const float hdet = d2x * d2y - dxy * dxy;
-    // compute_caustic_intensity
     const float curvature = -lap * p.focal_length;
     const float focusing = 1.0f / fmaxf(fabsf(1.0f - curvature), 0.01f);
     const float branch = hdet < -p.branch_threshold ? 1.5f : 1.0f;
     const float gmag = sqrtf(gx * gx + gy * gy);
     const float refraction = 1.0f + gmag * 0.5f;
     float it = focusing * branch * refraction;
-    it = powf(it, p.caustic_sharpness);
+    it = pow_sfu(it, p.caustic_sharpness);  // it >= 0.01 (the focusing clamp keeps it positive)
     it *= p.caustic_intensity;
-    out[(size_t)y * W + x] = fminf(fmaxf(it, 0.0f), 10.0f);
+    return fminf(fmaxf(it, 0.0f), 10.0f);
+}
+
+// One thread per column, walking kRows rows with the three-row window in registers.
+__global__ void __launch_bounds__(kCols) caustics_kernel(sbs_caustic_params p, const float *__restrict__ h,
+                                                         size_t pitch, float *__restrict__ out) {
+    const int W = (int)p.grid_width, H = (int)p.grid_height;
+    const int x = blockIdx.x * kCols + threadIdx.x;
+    if (x >= W) return;
+    const int xl = x == 0 ? W - 1 : x - 1, xr = x + 1 == W ? 0 : x + 1;  // phi wrapped
+    const int y0 = blockIdx.y * kRows, y1 = min(H, y0 + kRows);
+    Row a = load_row(h, pitch, H, y0 - 1, xl, x, xr);
+    Row b = load_row(h, pitch, H, y0, xl, x, xr);
+#pragma unroll 4
+    for (int y = y0; y < y1; ++y) {
+        const Row c = load_row(h, pitch, H, y + 1, xl, x, xr);
+        out[(size_t)y * W + x] = intensity(p, a, b, c);
+        a = b;
+        b = c;
+    }
 }
 
 }  // namespace
@@ -116,8 +141,8 @@ int sbs_caustics(const sbs_caustic_params *p, const float *thickness, size_t pit
         din = (const float *)base;
         dout = (float *)(base + ((in_b + 255) / 256) * 256);
     }
-    const dim3 grid((unsigned)((W + kTX - 1) / kTX), (unsigned)((H + kTY - 1) / kTY));
-    caustics_kernel<<<grid, dim3(kTX, kTY), 0, s>>>(*p, din, pitch, dout);
+    const dim3 grid((unsigned)((W + kCols - 1) / kCols), (unsigned)((H + kRows - 1) / kRows));
+    caustics_kernel<<<grid, kCols, 0, s>>>(*p, din, pitch, dout);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && mem == SBS_MEM_HOST)
         e = cudaMemcpyAsync(caustic_map, dout, sizeof(float) * W * H, cudaMemcpyDeviceToHost, s);
