@@ -8,7 +8,7 @@ spectral colour of --points seeded points, tensor-core or FP32 contraction), `su
 `surrogate-layered` (--steps 64-pass surrogate intervals of the field, untrained seeded weights:
 the same kernels and shapes as a trained network; --activation gelu or hswish), `foam` (the 4096-bubble foam batch, --steps
 steps with the default tiles), `shade` (--steps 3840 x 2160 headless frames of the bubble
-fragment shader). The field is the seeded smooth-mode field of
+fragment shader), `caustics` (--steps caustic maps of the field after 100 WGSL passes). The field is the seeded smooth-mode field of
 the 2048-resolution workload, built at the requested resolution. Steps launch one kernel each
 (graph replay for runs of 8 or more).
 """
@@ -27,7 +27,7 @@ def main(argv=None) -> None:
     p = argparse.ArgumentParser()
     p.add_argument("--case", default="wgsl",
                    choices=["wgsl", "cpu", "cpu32", "spectral-tc", "spectral-fp32", "surrogate-fused", "surrogate-layered",
-                            "foam", "shade"])
+                            "foam", "shade", "caustics"])
     p.add_argument("--points", type=int, default=1 << 20, help="spectral cases: number of points")
     p.add_argument("--res", type=int, default=2048)
     p.add_argument("--steps", type=int, default=20)
@@ -81,6 +81,16 @@ def main(argv=None) -> None:
         s.close()
         sim.close()
         print(f"ran {a.steps} surrogate intervals ({a.case}, {a.activation}) at resolution {a.res}")
+        return
+    if a.case == "caustics":
+        sim = GPUDrainageSimulator(None, 550e-9, 2 * a.res, a.res)
+        sim.set_thickness_array(h)
+        sim.set_concentration_array(c)
+        sim.run(100)
+        for _ in range(a.steps):
+            sim.caustic_map()
+        sim.close()
+        print(f"ran {a.steps} caustic maps at resolution {a.res}")
         return
     if a.case == "wgsl":
         sim = GPUDrainageSimulator(None, 550e-9, 2 * a.res, a.res)
