@@ -476,6 +476,47 @@ int sbs_caustics(const sbs_caustic_params *p, const float *thickness, size_t pit
  * returns when the map is there; device: ordered on the handle's stream). */
 int sbs_gpu_drainage_caustics(sbs_drainage *h, const sbs_caustic_params *p, int which, float *caustic_map, int mem);
 
+/* ------------------------------------------------------------------ */
+/* Branched flow of light through the film (ray tracing)               */
+/* ------------------------------------------------------------------ */
+/* BranchedFlowParams (branched_flow.rs:43-94, 112 bytes, same layout). */
+typedef struct sbs_branched_params {
+    float entry_point[3], beam_dir[3];
+    uint32_t num_rays, ray_steps;
+    float step_size, bend_strength, spread_angle, intensity_falloff;
+    uint32_t tex_width, tex_height;
+    float time, thickness_scale, base_thickness_nm, swirl_intensity, drainage_speed, pattern_scale;
+    uint32_t num_scatterers;
+    float scatterer_strength, scatterer_radius, particle_weight;
+    uint32_t patch_enabled;
+    float patch_center_u, patch_center_v, patch_half_size;
+} sbs_branched_params;
+
+/* ScattererGPU (branched_flow.rs:19-30). */
+typedef struct sbs_scatterer {
+    float pos_u, pos_v, strength, inv_sigma_sq;
+} sbs_scatterer;
+
+/* BranchedFlowParams::default() (branched_flow.rs:96-134). */
+int sbs_branched_params_default(sbs_branched_params *out);
+/* generate_scatterers (branched_flow.rs:164-226) on the host: num scatterers
+ * at Halton positions with time jitter, in the patch of p when
+ * p->patch_enabled; out holds num entries (num <= 2048). */
+int sbs_branched_scatterers(const sbs_branched_params *p, uint32_t num, float time, sbs_scatterer *out);
+/* One step of BranchedFlowSimulator (branched_flow.rs:575-601): the fade pass
+ * (texture *= 0.85, truncated) when fade != 0, then the kick-drift trace of
+ * p->num_rays rays (branched_flow_compute.wgsl:365-468) depositing into the
+ * u32 texture [tex_height][tex_width] (value * 256, atomic adds). thickness is
+ * the drainage field [height][pitch] (the shader's 128 x 64 grid generalised
+ * to width x height); scatterers holds min(p->num_scatterers, 2048) entries.
+ * acos, atan2 and exp are evaluated by the library's own published
+ * approximations (Abramowitz & Stegun 4.4.46 and 4.4.49; Cody-Waite
+ * reduction + Taylor series), so the texture is reproducible bit for bit. mem
+ * applies to thickness, scatterers and texture. */
+int sbs_branched_flow(const sbs_branched_params *p, const float *thickness, uint32_t width, uint32_t height,
+                      size_t pitch, const sbs_scatterer *scatterers, uint32_t *texture, int fade, int mem,
+                      void *stream);
+
 
 /* ------------------------------------------------------------------ */
 /* Drainage surrogate: conv neural operator over SBS_NN_STEPS passes   */

@@ -199,6 +199,15 @@ int orc_shade_frame(const sbs_bubble_uniform *u, const float view_proj[16], cons
 /* caustic compute pass (caustics_compute.wgsl:1-126): out [grid_height][grid_width] */
 void orc_caustics(const sbs_caustic_params *p, const float *h, size_t pitch, float *out);
 
+/* branched flow (branched_flow_compute.wgsl, branched_flow.rs): the library's acos / atan2 / exp,
+ * scatterer generation, and one fade + trace step into tex (accumulated in place) */
+float orc_acos_as(float x);
+float orc_atan2_as(float y, float x);
+float orc_exp_cw(float x);
+void orc_branched_scatterers(const sbs_branched_params *p, uint32_t num, float time, sbs_scatterer *out);
+void orc_branched_flow(const sbs_branched_params *p, const float *th, uint32_t w, uint32_t h, size_t pitch,
+                       const sbs_scatterer *sc, uint32_t *tex, int fade);
+
 #ifdef __cplusplus
 }
 #endif

@@ -107,6 +107,11 @@ _SIGS = {
     "orc_nn_forward": ([_P, _U32, _U32, _U32, _P, _P, _I], None),
     "orc_nn_loss_grad": ([_P, _U32, _U32, _U32, _P, _P, _P, _I], _D),
     "orc_nn_apply": ([_P, _P, _U32, _U32, _F, _P], None),
+    "orc_acos_as": ([_F], _F),
+    "orc_atan2_as": ([_F, _F], _F),
+    "orc_exp_cw": ([_F], _F),
+    "orc_branched_scatterers": ([_P, _U32, _F, _P], None),
+    "orc_branched_flow": ([_P, _P, _U32, _U32, C.c_size_t, _P, _P, _I], None),
     "orc_caustics": ([_P, _P, C.c_size_t, _P], None),
     "orc_simplex3": ([_F, _F, _F], _F),
     "orc_film_thickness": ([_P, _F, _F, _F], _F),
@@ -469,3 +474,33 @@ def caustics(params, h) -> np.ndarray:
     out = np.empty((params.grid_height, params.grid_width), dtype=np.float32)
     lib().orc_caustics(C.cast(C.byref(params), C.c_void_p), _p(h), h.shape[1], _p(out))
     return out
+
+
+# ---------------------------------------------------------------------- branched flow
+def acos_as(x: float) -> float:
+    return float(lib().orc_acos_as(float(x)))
+
+
+def atan2_as(y: float, x: float) -> float:
+    return float(lib().orc_atan2_as(float(y), float(x)))
+
+
+def exp_cw(x: float) -> float:
+    return float(lib().orc_exp_cw(float(x)))
+
+
+def branched_scatterers(params, num: int, time: float) -> np.ndarray:
+    """[num][4] float32 (pos_u, pos_v, strength, inv_sigma_sq); params laid out as sbs_branched_params."""
+    out = np.empty((num, 4), dtype=np.float32)
+    lib().orc_branched_scatterers(C.cast(C.byref(params), C.c_void_p), int(num), float(time), _p(out))
+    return out
+
+
+def branched_flow(params, thickness, scatterers, texture, fade: bool) -> np.ndarray:
+    """One fade + trace step; returns the updated [tex_height][tex_width] u32 texture."""
+    th = np.ascontiguousarray(thickness, dtype=np.float32)
+    sc = np.ascontiguousarray(scatterers, dtype=np.float32).reshape(-1, 4)
+    tex = np.array(texture, dtype=np.uint32, copy=True)
+    lib().orc_branched_flow(C.cast(C.byref(params), C.c_void_p), _p(th), th.shape[1], th.shape[0], th.shape[1],
+                            _p(sc), _p(tex), 1 if fade else 0)
+    return tex

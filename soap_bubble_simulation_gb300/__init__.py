@@ -19,6 +19,7 @@ from .foam import FoamDrainage
 from .surrogate import SURROGATE_STEPS, DrainageSurrogate, field_params, masked_error
 from .shading import BubbleUniform, Camera, render_frame, shade_fragments
 from .caustics import CausticParams, caustic_map
+from .branched import BranchedFlowParams, BranchedFlowSimulator, branched_flow_step, generate_scatterers
 
 __all__ = [
     "BubbleParameters", "ConfigError", "EnvironmentParameters", "FluidParameters", "SimulationConfig",
@@ -28,4 +29,5 @@ __all__ = [
     "generate_interference_lut_array", "lookup_2d", "sample_interference_lut", "schlick_interference_rgb", "spectral_rgb",
     "wavelengths", "SbsError", "FoamDrainage", "SURROGATE_STEPS", "DrainageSurrogate", "field_params",
     "masked_error", "BubbleUniform", "Camera", "render_frame", "shade_fragments", "CausticParams", "caustic_map",
+    "BranchedFlowParams", "BranchedFlowSimulator", "branched_flow_step", "generate_scatterers",
 ]

@@ -198,6 +198,9 @@ SIGNATURES: dict[str, list] = {
     "sbs_caustic_params_default": [_P],
     "sbs_caustics": [_P, _P, _SZ, _P, _I, _P],
     "sbs_gpu_drainage_caustics": [_P, _P, _I, _P, _I],
+    "sbs_branched_params_default": [_P],
+    "sbs_branched_scatterers": [_P, _U32, _F, _P],
+    "sbs_branched_flow": [_P, _P, _U32, _U32, _SZ, _P, _P, _I, _I, _P],
     "sbs_drainage_vertex_colors": [_P, _P, _SZ, _P, _U32, _U32, _D, _D, _P, _I],
     "sbs_surrogate_create": [C.c_uint64, C.POINTER(_P)],
     "sbs_surrogate_destroy": [_P],
