@@ -28,6 +28,7 @@ c0: the small configuration's latency-bound calls (1000 steps at resolution 128 
 semantics, the colour LUTs, colours at 10,242 icosphere vertices), host in and host out.
 shading: one 3840 x 2160 headless frame of the bubble fragment shader, pixels/s.
 caustics: the caustic pass over the drained 2048 x 4096 field, on the simulator's device field.
+branched_flow: one step of the branched-flow ray tracer at the reference's defaults.
 
 --impl reference: times that CPU restatement alone (the reference is Rust and cannot be
 built here), same metric and config.
@@ -440,6 +441,48 @@ def caustics_section(sbs, synthetic, torch, h0, c0):
                     "bytes_per_cell": 8}}
 
 
+def branched_section(sbs, synthetic, torch):
+    """Branched flow: one step of the reference's defaults (32,768 rays x 400 kick-drift steps, 800
+    scatterers, 512 x 256 texture; patch off so that every step deposits) over a 128 x 64 film,
+    device-resident (CUDA events) and through the host call."""
+    from soap_bubble_simulation_gb300 import branched as br
+
+    N = sbs._native
+    p = br.BranchedFlowParams.default()
+    p.patch_enabled = 0
+    th = (synthetic.smooth_modes(64, 128, seed=3) * 2e4).astype(np.float32)
+    sc = br.generate_scatterers(p, time=1.5)
+    dth, dsc = torch.from_numpy(th).cuda(), torch.from_numpy(sc).cuda()
+    dtex = torch.zeros((p.tex_height, p.tex_width), dtype=torch.int32, device="cuda")
+    st = torch.cuda.current_stream()
+
+    def run():
+        N.call("sbs_branched_flow", ctypes.cast(ctypes.byref(p), ctypes.c_void_p), ctypes.c_void_p(dth.data_ptr()),
+               128, 64, 128, ctypes.c_void_p(dsc.data_ptr()), ctypes.c_void_p(dtex.data_ptr()), 1, N.MEM_DEVICE,
+               ctypes.c_void_p(st.cuda_stream))
+
+    for _ in range(2):
+        run()
+    reps = 10
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    for _ in range(reps):
+        run()
+    b.record(st)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / reps
+    tex = np.zeros((p.tex_height, p.tex_width), np.uint32)
+    br.branched_flow_step(p, th, sc, tex)
+    ta = time.perf_counter()
+    for _ in range(3):
+        tex = br.branched_flow_step(p, th, sc, tex)
+    e2e_ms = (time.perf_counter() - ta) / 3 * 1e3
+    steps = p.num_rays * p.ray_steps
+    return {"value": steps / (ms * 1e-3), "unit": "ray-steps/s", "ms_per_step": ms, "rays": int(p.num_rays),
+            "steps_per_ray": int(p.ray_steps), "scatterers": int(p.num_scatterers),
+            "e2e": {"value": steps / (e2e_ms * 1e-3), "unit": "ray-steps/s", "ms_per_step": e2e_ms}}
+
+
 def spectral_section(sbs, synthetic, torch):
     N = sbs._native
     n = 8_388_608
@@ -611,11 +654,12 @@ def main():
     cpu_sem_ms = a_ev.elapsed_time(b_ev)
     cpu_sem_rate = cells * 2000 / (cpu_sem_ms / 1e3)
 
-    surrogate = foam = spectral = small = shade = caus = None
+    surrogate = foam = spectral = small = shade = caus = bflow = None
     if not args.skip_aux:
         small = c0_section(sbs, synthetic, torch)
         shade = shade_section(sbs, torch)
         caus = caustics_section(sbs, synthetic, torch, h0, c0)
+        bflow = branched_section(sbs, synthetic, torch)
         surrogate = surrogate_section(sbs, synthetic, h0, c0, torch)
         foam = foam_section(sbs, synthetic, torch)
         spectral = spectral_section(sbs, synthetic, torch)
@@ -660,6 +704,7 @@ def main():
             "c0": small,
             "shading": shade,
             "caustics": caus,
+            "branched_flow": bflow,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
