@@ -517,6 +517,64 @@ int sbs_branched_flow(const sbs_branched_params *p, const float *thickness, uint
                       size_t pitch, const sbs_scatterer *scatterers, uint32_t *texture, int fade, int mem,
                       void *stream);
 
+/* ------------------------------------------------------------------ */
+/* Foam cluster dynamics (FoamSimulator)                               */
+/* ------------------------------------------------------------------ */
+/* FoamSimulator's physics fields (foam_dynamics.rs:11-34), 48 bytes. */
+typedef struct sbs_foam_physics {
+    float surface_tension, viscosity, density;
+    float gravity[3];
+    float van_der_waals_strength, repulsion_stiffness, damping;
+    uint32_t coalescence_enabled;
+    float coalescence_threshold;
+    uint32_t padding;
+} sbs_foam_physics;
+
+/* BubbleConnection (foam.rs:90-105), 40 bytes; bubble_a < bubble_b are bubble ids. */
+typedef struct sbs_bubble_connection {
+    uint32_t bubble_a, bubble_b;
+    float contact_point[3], contact_normal[3];
+    float wall_curvature_radius, wall_thickness_nm;
+} sbs_bubble_connection;
+
+typedef struct sbs_foam_sim sbs_foam_sim;
+
+/* FoamSimulator::new's defaults (foam_dynamics.rs:38-53). */
+int sbs_foam_physics_default(sbs_foam_physics *out);
+/* A cluster of n bubbles in the order of BubbleCluster::bubbles() (ids 0..n-1, at rest):
+ * position [n][3] and radius [n] in metres, thickness_nm [n] (null: 500 nm, Bubble::new). The
+ * state lives on the GPU. */
+int sbs_foam_sim_create(uint32_t n, const float *position, const float *radius, const float *thickness_nm,
+                        const sbs_foam_physics *p, sbs_foam_sim **out);
+int sbs_foam_sim_destroy(sbs_foam_sim *s);
+int sbs_foam_sim_set_physics(sbs_foam_sim *s, const sbs_foam_physics *p);
+/* `steps` FoamSimulator::step(dt) calls (foam_dynamics.rs:172-211): forces over all pairs in the
+ * reference's accumulation order, semi-implicit Euler with damping and the 0.1 m/s speed clamp,
+ * update_connections, and with coalescence_enabled the merge of the first connection whose
+ * Weber number exceeds the threshold. Pairs farther apart than 3 (r_a + r_b) contribute exact
+ * zeros in the reference; they are skipped through a neighbour list sorted by bubble order, so
+ * the sums are the reference's f32 sums. Returns when the steps are done. */
+int sbs_foam_sim_step(sbs_foam_sim *s, float dt, uint32_t steps);
+/* bubble_count() and connection_count() (either pointer may be null). */
+int sbs_foam_sim_counts(sbs_foam_sim *s, uint32_t *bubbles, uint32_t *connections);
+/* The bubbles in cluster order: position and velocity [n][3], radius, thickness_nm [n], ids [n];
+ * any pointer may be null; n = the current bubble count. */
+int sbs_foam_sim_get_state(sbs_foam_sim *s, float *position, float *velocity, float *radius, float *thickness_nm,
+                           uint32_t *ids, int mem);
+/* Overwrites the listed fields of the current bubbles (null = keep), as the reference's public
+ * Bubble fields allow; the count stays. */
+int sbs_foam_sim_set_state(sbs_foam_sim *s, const float *position, const float *velocity, const float *radius,
+                           const float *thickness_nm, int mem);
+/* compute_forces (foam_dynamics.rs:62-94) on the current state: forces [n][3]. */
+int sbs_foam_sim_forces(sbs_foam_sim *s, float *forces, int mem);
+/* The cluster's connections() after the last step (foam.rs:304-307), in its order; writes
+ * min(count, capacity) records to out (host memory) and the full count to *count. */
+int sbs_foam_sim_connections(sbs_foam_sim *s, sbs_bubble_connection *out, uint32_t capacity, uint32_t *count);
+/* Couples the cluster to a batched drainage foam with the same bubble count: bubble i's
+ * thickness_nm becomes the area-weighted (sin theta) mean of batch bubble i's current thickness
+ * field, in nm. */
+int sbs_foam_sim_couple_thickness(sbs_foam_sim *s, sbs_foam *batch);
+
 
 /* ------------------------------------------------------------------ */
 /* Drainage surrogate: conv neural operator over SBS_NN_STEPS passes   */

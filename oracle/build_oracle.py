@@ -16,7 +16,8 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
-SOURCES = ["drainage.cpp", "interference.cpp", "surrogate.cpp", "shade.cpp", "caustics.cpp", "branched.cpp"]
+SOURCES = ["drainage.cpp", "interference.cpp", "surrogate.cpp", "shade.cpp", "caustics.cpp", "branched.cpp",
+           "foam_dynamics.cpp"]
 CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
 
 

@@ -208,6 +208,18 @@ void orc_branched_scatterers(const sbs_branched_params *p, uint32_t num, float t
 void orc_branched_flow(const sbs_branched_params *p, const float *th, uint32_t w, uint32_t h, size_t pitch,
                        const sbs_scatterer *sc, uint32_t *tex, int fade);
 
+/* foam cluster dynamics (foam_dynamics.rs, foam.rs), the reference's O(n^2) loops: forces [n][3]
+ * of compute_forces; `steps` FoamSimulator::step calls on arrays in cluster order (updated in place,
+ * the new count returned), the final connections() into conn (up to cap, *nconn = count) */
+float orc_pow15(float x);
+void orc_foam_forces(const sbs_foam_physics *p, uint32_t n, const float *pos, const float *vel, const float *radius,
+                     const float *thick, float *out);
+void orc_foam_forces_subset(const sbs_foam_physics *p, uint32_t n, const float *pos, const float *vel,
+                            const float *radius, const float *thick, const uint32_t *idx, uint32_t m, float *out);
+uint32_t orc_foam_step(const sbs_foam_physics *p, float dt, uint32_t steps, uint32_t n, float *pos, float *vel,
+                       float *radius, float *thick, uint32_t *ids, uint32_t *next_id, sbs_bubble_connection *conn,
+                       uint32_t cap, uint32_t *nconn);
+
 #ifdef __cplusplus
 }
 #endif

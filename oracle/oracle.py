@@ -112,6 +112,10 @@ _SIGS = {
     "orc_exp_cw": ([_F], _F),
     "orc_branched_scatterers": ([_P, _U32, _F, _P], None),
     "orc_branched_flow": ([_P, _P, _U32, _U32, C.c_size_t, _P, _P, _I], None),
+    "orc_pow15": ([_F], _F),
+    "orc_foam_forces": ([_P, _U32, _P, _P, _P, _P, _P], None),
+    "orc_foam_forces_subset": ([_P, _U32, _P, _P, _P, _P, _P, _U32, _P], None),
+    "orc_foam_step": ([_P, _F, _U32, _U32, _P, _P, _P, _P, _P, _P, _P, _U32, _P], _U32),
     "orc_caustics": ([_P, _P, C.c_size_t, _P], None),
     "orc_simplex3": ([_F, _F, _F], _F),
     "orc_film_thickness": ([_P, _F, _F, _F], _F),
@@ -504,3 +508,65 @@ def branched_flow(params, thickness, scatterers, texture, fade: bool) -> np.ndar
     lib().orc_branched_flow(C.cast(C.byref(params), C.c_void_p), _p(th), th.shape[1], th.shape[0], th.shape[1],
                             _p(sc), _p(tex), 1 if fade else 0)
     return tex
+
+
+# ---------------------------------------------------------------------- foam cluster dynamics
+def foam_forces(physics, position, radius, velocity=None, thickness_nm=None) -> np.ndarray:
+    """compute_forces (foam_dynamics.rs:62-94): [n][3] float32; physics laid out as sbs_foam_physics."""
+    pos = np.ascontiguousarray(position, dtype=np.float32).reshape(-1, 3)
+    n = pos.shape[0]
+    r = np.ascontiguousarray(radius, dtype=np.float32).reshape(n)
+    v = None if velocity is None else np.ascontiguousarray(velocity, dtype=np.float32).reshape(n, 3)
+    t = None if thickness_nm is None else np.ascontiguousarray(thickness_nm, dtype=np.float32).reshape(n)
+    out = np.empty((n, 3), dtype=np.float32)
+    lib().orc_foam_forces(C.cast(C.byref(physics), C.c_void_p), n, _p(pos), None if v is None else _p(v), _p(r),
+                          None if t is None else _p(t), _p(out))
+    return out
+
+
+def foam_forces_subset(physics, position, radius, idx, velocity=None, thickness_nm=None) -> np.ndarray:
+    """The forces on the bubbles idx alone, in compute_forces' accumulation order: [len(idx)][3]."""
+    pos = np.ascontiguousarray(position, dtype=np.float32).reshape(-1, 3)
+    n = pos.shape[0]
+    r = np.ascontiguousarray(radius, dtype=np.float32).reshape(n)
+    v = None if velocity is None else np.ascontiguousarray(velocity, dtype=np.float32).reshape(n, 3)
+    t = None if thickness_nm is None else np.ascontiguousarray(thickness_nm, dtype=np.float32).reshape(n)
+    ix = np.ascontiguousarray(idx, dtype=np.uint32)
+    out = np.empty((ix.size, 3), dtype=np.float32)
+    lib().orc_foam_forces_subset(C.cast(C.byref(physics), C.c_void_p), n, _p(pos), None if v is None else _p(v), _p(r),
+                                 None if t is None else _p(t), _p(ix), ix.size, _p(out))
+    return out
+
+
+def pow15(x: float) -> float:
+    return float(lib().orc_pow15(float(x)))
+
+
+def foam_step(physics, dt: float, steps: int, position, radius, velocity=None, thickness_nm=None, ids=None,
+              next_id=None):
+    """`steps` FoamSimulator::step calls on the cluster (arrays in cluster order). Returns a dict with
+    position, velocity [m][3], radius, thickness_nm [m], ids [m], next_id and connections: a structured
+    array of (bubble_a, bubble_b, contact_point[3], contact_normal[3], wall_curvature_radius,
+    wall_thickness_nm) in the reference's order."""
+    pos = np.array(position, dtype=np.float32, copy=True).reshape(-1, 3)
+    n = pos.shape[0]
+    r = np.array(radius, dtype=np.float32, copy=True).reshape(n)
+    v = np.zeros((n, 3), np.float32) if velocity is None else np.array(velocity, np.float32, copy=True).reshape(n, 3)
+    t = np.full(n, 500.0, np.float32) if thickness_nm is None else np.array(thickness_nm, np.float32,
+                                                                              copy=True).reshape(n)
+    i = np.arange(n, dtype=np.uint32) if ids is None else np.array(ids, dtype=np.uint32, copy=True).reshape(n)
+    nid = C.c_uint32(n if next_id is None else int(next_id))
+    cap = 64 * n + 64
+    conn = np.zeros(cap, dtype=FOAM_CONNECTION)
+    nconn = C.c_uint32(0)
+    m = lib().orc_foam_step(C.cast(C.byref(physics), C.c_void_p), float(dt), int(steps), n, _p(pos), _p(v), _p(r),
+                            _p(t), _p(i), C.byref(nid), conn.ctypes.data, cap, C.byref(nconn))
+    if nconn.value > cap:
+        raise RuntimeError("connection buffer too small")
+    return dict(position=pos[:m], velocity=v[:m], radius=r[:m], thickness_nm=t[:m], ids=i[:m], next_id=nid.value,
+                connections=conn[:nconn.value].copy())
+
+
+FOAM_CONNECTION = np.dtype([("bubble_a", np.uint32), ("bubble_b", np.uint32), ("contact_point", np.float32, 3),
+                            ("contact_normal", np.float32, 3), ("wall_curvature_radius", np.float32),
+                            ("wall_thickness_nm", np.float32)])

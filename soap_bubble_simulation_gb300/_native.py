@@ -201,6 +201,17 @@ SIGNATURES: dict[str, list] = {
     "sbs_branched_params_default": [_P],
     "sbs_branched_scatterers": [_P, _U32, _F, _P],
     "sbs_branched_flow": [_P, _P, _U32, _U32, _SZ, _P, _P, _I, _I, _P],
+    "sbs_foam_physics_default": [_P],
+    "sbs_foam_sim_create": [_U32, _P, _P, _P, _P, C.POINTER(_P)],
+    "sbs_foam_sim_destroy": [_P],
+    "sbs_foam_sim_set_physics": [_P, _P],
+    "sbs_foam_sim_step": [_P, _F, _U32],
+    "sbs_foam_sim_counts": [_P, _P, _P],
+    "sbs_foam_sim_get_state": [_P, _P, _P, _P, _P, _P, _I],
+    "sbs_foam_sim_set_state": [_P, _P, _P, _P, _P, _I],
+    "sbs_foam_sim_forces": [_P, _P, _I],
+    "sbs_foam_sim_connections": [_P, _P, _U32, _P],
+    "sbs_foam_sim_couple_thickness": [_P, _P],
     "sbs_drainage_vertex_colors": [_P, _P, _SZ, _P, _U32, _U32, _D, _D, _P, _I],
     "sbs_surrogate_create": [C.c_uint64, C.POINTER(_P)],
     "sbs_surrogate_destroy": [_P],

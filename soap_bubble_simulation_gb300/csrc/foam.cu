@@ -519,3 +519,53 @@ int sbs_foam_stream(const sbs_foam *f, void **out) {
 }
 
 }  // extern "C"
+
+namespace sbs {
+namespace {
+
+// One block per bubble: sum of h sin(theta_i) and of sin(theta_i) over the grid (theta_i =
+// i pi / (nt - 1)), in double.
+__global__ void __launch_bounds__(256) mean_thickness_kernel(const FoamBubble *bub, int parity, float *out) {
+    __shared__ double s_h[8], s_w[8];
+    const FoamBubble B = bub[blockIdx.x];
+    const float *h = B.h[parity];
+    double sh = 0.0, sw = 0.0;
+    const double dth = 3.14159265358979323846 / (double)(B.nt - 1);
+    for (int r = threadIdx.x >> 5; r < B.nt; r += 8) {
+        const double w = sin(r * dth);
+        double row = 0.0;
+        for (int c = threadIdx.x & 31; c < B.np; c += 32) row += (double)h[(size_t)r * B.pitch + c];
+        sh += row * w;
+        sw += w * ((B.np - (threadIdx.x & 31) + 31) / 32);
+    }
+    for (int o = 16; o; o >>= 1) {
+        sh += __shfl_xor_sync(0xffffffffu, sh, o);
+        sw += __shfl_xor_sync(0xffffffffu, sw, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s_h[threadIdx.x >> 5] = sh;
+        s_w[threadIdx.x >> 5] = sw;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int k = 0; k < 8; ++k) {
+            a += s_h[k];
+            b += s_w[k];
+        }
+        out[blockIdx.x] = b > 0.0 ? (float)(a / b * 1e9) : 0.0f;
+    }
+}
+
+}  // namespace
+
+int foam_mean_thickness_nm(sbs_foam *f, float *out, uint32_t cap, uint32_t *nb) {
+    *nb = (uint32_t)f->nb;
+    if ((uint32_t)f->nb > cap) return SBS_OK;
+    mean_thickness_kernel<<<f->nb, 256, 0, f->stream>>>(f->d_bubbles, f->cur, out);
+    SBS_CUDA_TRY(cudaGetLastError());
+    SBS_CUDA_TRY(cudaStreamSynchronize(f->stream));
+    return SBS_OK;
+}
+
+}  // namespace sbs

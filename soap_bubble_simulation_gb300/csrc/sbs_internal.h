@@ -45,6 +45,11 @@ cudaError_t scratch_alloc(void **p, size_t bytes, cudaStream_t s);
 // synchronisation (sbs_gpu_drainage_run minus the wait).
 int drainage_run_async(sbs_drainage *h, uint32_t passes);
 
+// Area-weighted (sin theta) mean of each bubble's current thickness field of a batched foam, in
+// nm, into out[cap] (device memory); *nb = the batch's bubble count (out is written only when
+// nb <= cap). Returns when the values are there.
+int foam_mean_thickness_nm(sbs_foam *f, float *out, uint32_t cap, uint32_t *nb);
+
 // ---------------------------------------------------------------------------
 // Drainage kernels
 // ---------------------------------------------------------------------------
