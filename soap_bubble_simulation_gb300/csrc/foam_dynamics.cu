@@ -268,7 +268,8 @@ __global__ void list_scatter_kernel(ListArgs a) {
     a.bitems[a.bstart[a.bkey[k]] + a.brank[k]] = k;
 }
 
-// Counts each bubble's candidates; the largest count of a 32-bubble group sets its column length.
+// Counts each bubble's candidates; the largest count of a 32-bubble group, rounded up to a multiple
+// of 32, sets its column length.
 __global__ void list_count_kernel(ListArgs a) {
     Ctl *c = a.ctl;
     if (!c->go) return;
@@ -301,7 +302,9 @@ __global__ void list_count_kernel(ListArgs a) {
     }
     uint32_t g = m;
     for (int o = 16; o; o >>= 1) g = max(g, __shfl_xor_sync(0xffffffffu, g, o));
-    if ((threadIdx.x & 31) == 0 && k < ((n + 31) & ~31u)) a.gcap[k >> 5] = g;
+    // columns padded to whole 32-entry blocks: a group then owns exactly its share of the
+    // connection-bit words (word (t / 32) * 32 + lane of the group's block)
+    if ((threadIdx.x & 31) == 0 && k < ((n + 31) & ~31u)) a.gcap[k >> 5] = (g + 31) & ~31u;
 }
 
 // One warp per bubble: collects the candidates again, sorts them by index and writes the column.
