@@ -29,6 +29,8 @@ semantics, the colour LUTs, colours at 10,242 icosphere vertices), host in and h
 shading: one 3840 x 2160 headless frame of the bubble fragment shader, pixels/s.
 caustics: the caustic pass over the drained 2048 x 4096 field, on the simulator's device field.
 branched_flow: one step of the branched-flow ray tracer at the reference's defaults.
+foam_dynamics: FoamSimulator::step over a 1,048,576-bubble FCC foam (and 4,096 bubbles beside the
+oracle's all-pairs loops on one host core), bubble-steps/s.
 
 --impl reference: times that CPU restatement alone (the reference is Rust and cannot be
 built here), same metric and config.
@@ -483,6 +485,55 @@ def branched_section(sbs, synthetic, torch):
             "e2e": {"value": steps / (e2e_ms * 1e-3), "unit": "ray-steps/s", "ms_per_step": e2e_ms}}
 
 
+def foam_dynamics_section(sbs, cpu_seconds: float):
+    """Foam cluster dynamics (FoamSimulator::step): a face-centred cubic foam of 1,048,576 bubbles
+    (FoamGenerator::generate_fcc's layout, spacing 5 cm, radii 1.5-3 cm, jitter 0.1, seeded),
+    dt = 1 ms, 40 steps timed in one call (the neighbour list is rebuilt about every 40 steps, so
+    the rebuilds are included at their rate); e2e adds the per-frame read-back of every bubble's
+    position, velocity, radius and thickness. The same at 4,096 bubbles next to the oracle's
+    restatement of the reference's all-pairs loops on one host core (the reference is
+    single-threaded), timed on a bounded number of steps."""
+    from soap_bubble_simulation_gb300 import foam_dynamics as fd
+
+    out = {}
+    for n, k in ((1_048_576, 40), (4096, 200)):
+        pos, rad = fd.fcc_foam(n, seed=0)
+        sim = fd.FoamSimulator(pos, rad)
+        sim.step(1e-3, 3)
+        t0 = time.perf_counter()
+        sim.step(1e-3, k)
+        ms = (time.perf_counter() - t0) / k * 1e3
+        reps = 5 if n > 10000 else 50
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            sim.step(1e-3)
+            sim.bubbles()
+        e2e_ms = (time.perf_counter() - t0) / reps * 1e3
+        out[n] = {"bubbles": n, "ms_per_step": ms, "value": n / (ms * 1e-3), "unit": "bubble-steps/s",
+                  "connections": sim.connection_count(),
+                  "e2e": {"value": n / (e2e_ms * 1e-3), "unit": "bubble-steps/s", "ms_per_step": e2e_ms,
+                          "d2h_bytes_per_step": n * 36}}
+        sim.close()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+
+    pos, rad = fd.fcc_foam(4096, seed=0)
+    phys = fd.FoamPhysics.default()
+    r = orc.foam_step(phys, 1e-3, 1, pos, rad)
+    steps, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < cpu_seconds:
+        r = orc.foam_step(phys, 1e-3, 1, r["position"], r["radius"], velocity=r["velocity"], ids=r["ids"],
+                          next_id=r["next_id"])
+        steps += 1
+    cpu_ms = (time.perf_counter() - t0) / steps * 1e3
+    big, small = out[1_048_576], out[4096]
+    return {"value": big["value"], "unit": "bubble-steps/s", "ms_per_step": big["ms_per_step"],
+            "bubbles": big["bubbles"], "connections": big["connections"], "e2e": big["e2e"],
+            "small": small,
+            "cpu_baseline": {"value": 4096 / (cpu_ms * 1e-3), "unit": "bubble-steps/s", "cores": 1, "kind": "port",
+                             "sample": f"4,096 bubbles, {steps} steps of the all-pairs loops", "ms_per_step": cpu_ms}}
+
+
 def spectral_section(sbs, synthetic, torch):
     N = sbs._native
     n = 8_388_608
@@ -654,7 +705,7 @@ def main():
     cpu_sem_ms = a_ev.elapsed_time(b_ev)
     cpu_sem_rate = cells * 2000 / (cpu_sem_ms / 1e3)
 
-    surrogate = foam = spectral = small = shade = caus = bflow = None
+    surrogate = foam = spectral = small = shade = caus = bflow = fdyn = None
     if not args.skip_aux:
         small = c0_section(sbs, synthetic, torch)
         shade = shade_section(sbs, torch)
@@ -663,6 +714,8 @@ def main():
         surrogate = surrogate_section(sbs, synthetic, h0, c0, torch)
         foam = foam_section(sbs, synthetic, torch)
         spectral = spectral_section(sbs, synthetic, torch)
+        if rank == 0 and world == 1:
+            fdyn = foam_dynamics_section(sbs, min(args.cpu_seconds, 10.0))
 
     base = base1 = None
     if rank == 0 and world == 1 and not args.skip_aux:
@@ -705,6 +758,7 @@ def main():
             "shading": shade,
             "caustics": caus,
             "branched_flow": bflow,
+            "foam_dynamics": fdyn,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

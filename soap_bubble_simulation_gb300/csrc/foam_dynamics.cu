@@ -44,7 +44,6 @@ namespace {
 constexpr float kPi = 3.14159265358979323846f;
 constexpr float kMaxSpeed = 0.1f;   // foam_dynamics.rs:194
 constexpr int kMaxCand = 2048;      // neighbour-list entries per bubble (the shared-memory sort buffer)
-constexpr int kFillWarps = 4;       // warps per block of the list fill
 constexpr int kThreads = 256;
 constexpr uint32_t kNone = 0xffffffffu;
 constexpr unsigned long long kNoPair = ~0ull;
@@ -62,7 +61,7 @@ struct Ctl {
     uint32_t nconn;         // connection count after the last step (before its merge)
     unsigned long long coal_key;  // first connection (i << 32 | j) whose Weber number is over the threshold
     uint32_t merged_a, merged_b;  // ids merged by the last step, kNone if none
-    float inv_cell, skin, pad0, pad2;
+    float inv_cell, skin, cell, rmax;
     uint32_t list_total, dense_bubble, dense_count, pad1;
 };
 
@@ -94,10 +93,14 @@ __host__ __device__ __forceinline__ float pow15(float x) {
 __device__ __forceinline__ void pair_force(const Phys &P, float4 a, float4 b, float &fx, float &fy, float &fz) {
     fx = fy = fz = 0.0f;
     const float dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
-    const float distance = len3(dx, dy, dz);
-    if (distance < 1e-6f) return;
+    const float d2 = dx * dx + dy * dy + dz * dz;
     const float sum_radii = a.w + b.w;
     const float three = sum_radii * 3.0f;
+    // far pairs leave before the square root: with d2 above three^2 (1 + 2^-20) the rounded root
+    // is at least `three`, the range where no term applies
+    if (d2 > three * three * 1.00000095f) return;
+    const float distance = sqrtf(d2);
+    if (distance < 1e-6f) return;
     if (!(distance < three)) return;  // exact zero: no term applies (adhesion ends at 1.2 sum)
     const float ux = dx / distance, uy = dy / distance, uz = dz / distance;
     if (distance > sum_radii) {
@@ -123,15 +126,22 @@ __device__ __forceinline__ void pair_force(const Phys &P, float4 a, float4 b, fl
     }
 }
 
+constexpr float kCellLim = 1048574.0f;  // cell coordinates are clamped to +-(2^20 - 2)
+
 __device__ __forceinline__ int3 cell_of(float4 p, float inv_cell) {
-    const float lim = 1.0e9f;
-    return make_int3((int)floorf(fminf(fmaxf(p.x * inv_cell, -lim), lim)),
-                     (int)floorf(fminf(fmaxf(p.y * inv_cell, -lim), lim)),
-                     (int)floorf(fminf(fmaxf(p.z * inv_cell, -lim), lim)));
+    return make_int3((int)floorf(fminf(fmaxf(p.x * inv_cell, -kCellLim), kCellLim)),
+                     (int)floorf(fminf(fmaxf(p.y * inv_cell, -kCellLim), kCellLim)),
+                     (int)floorf(fminf(fmaxf(p.z * inv_cell, -kCellLim), kCellLim)));
 }
 
 __device__ __forceinline__ uint32_t cell_hash(int x, int y, int z, uint32_t mask) {
     return ((uint32_t)x * 73856093u ^ (uint32_t)y * 19349663u ^ (uint32_t)z * 83492791u) & mask;
+}
+
+// 21 bits a coordinate: distinct for every cell of the clamped range and its neighbours.
+__device__ __forceinline__ unsigned long long cell_key(int x, int y, int z) {
+    return ((unsigned long long)(uint32_t)(x + (1 << 20)) << 42) |
+           ((unsigned long long)(uint32_t)(y + (1 << 20)) << 21) | (unsigned long long)(uint32_t)(z + (1 << 20));
 }
 
 // A pair is listed when |p_j - p_k| < 3 (r_k + r_j) + skin.
@@ -146,11 +156,15 @@ struct ListArgs {
     int npar;
     const float4 *pr;
     float4 *p0;             // positions at the build
-    int4 *cellc;            // cell of each bubble
-    uint32_t *bcount, *bstart, *bitems, *bkey, *brank;
+    int4 *cellc;            // cell of each bubble (w: its slot in bucket order)
+    uint32_t *bcount, *bstart, *bkey, *brank;
+    uint32_t *bitems;       // bubbles in bucket order
+    float4 *spr;            // their positions and radii, in bucket order
+    unsigned long long *skey;  // their cell keys, in bucket order
     uint32_t mask;          // hash buckets - 1
     uint32_t *cnt;          // list length per bubble
-    uint32_t *gcap;         // entries per column of each 32-bubble group
+    uint32_t *split;        // entries j < k of each list (the sorted list's lower part)
+    uint32_t *gcap;         // largest list length of each 32-bubble group
     uint32_t *goff;         // group offsets (ngroups + 1)
     uint32_t *nbr;          // interleaved lists
     size_t nbr_cap;
@@ -178,8 +192,12 @@ __global__ void __launch_bounds__(1024) list_begin_kernel(ListArgs a, int forced
         m = threadIdx.x < (blockDim.x >> 5) ? s_max[threadIdx.x] : 0.0f;
         for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
         if (threadIdx.x == 0) {
-            const float cell = (6.0f * m + skin) * 1.0001f + 1e-12f;
+            // cells of half the largest candidate range 6 r_max + skin: the 5 x 5 x 5 cells around a
+            // bubble's own hold all its candidates
+            const float cell = (6.0f * m + skin) * 0.5001f + 1e-12f;
             c->inv_cell = 1.0f / cell;
+            c->cell = cell;
+            c->rmax = m;
             c->skin = skin;
             c->need_rebuild = 0;
             c->go = 1;
@@ -196,14 +214,16 @@ __global__ void list_bin_kernel(ListArgs a) {
     const int3 q = cell_of(p, c->inv_cell);
     const uint32_t h = cell_hash(q.x, q.y, q.z, a.mask);
     a.p0[k] = p;
-    a.cellc[k] = make_int4(q.x, q.y, q.z, 0);
     a.bkey[k] = h;
     a.brank[k] = atomicAdd(a.bcount + h, 1u);
+    a.cellc[k] = make_int4(q.x, q.y, q.z, 0);
 }
 
 // Exclusive scan of `count` values with one block, tile by tile (4 values a thread).
-// mode 0: hash buckets (count given); mode 1: group capacities x 32 (count = ceil(n / 32)), with
-// the capacity check of the list.
+// mode 0: hash buckets (count given); mode 1: the entries of each 32-bubble group, 32 columns of its
+// largest count rounded up to a multiple of 32 (count = ceil(n / 32)), with the capacity check of
+// the list. (Whole 32-entry blocks per column: a group then owns exactly its share of the
+// connection-bit words, word (t / 32) * 32 + lane of the group's block.)
 __global__ void __launch_bounds__(1024) scan_kernel(const uint32_t *in, uint32_t *out, uint32_t count, int mode,
                                                     ListArgs a) {
     __shared__ uint32_t s_w[32];
@@ -220,7 +240,7 @@ __global__ void __launch_bounds__(1024) scan_kernel(const uint32_t *in, uint32_t
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const uint32_t i = i0 + q;
-            v[q] = i < count ? (mode == 1 ? in[i] * 32u : in[i]) : 0u;
+            v[q] = i < count ? (mode == 1 ? ((in[i] + 31u) & ~31u) * 32u : in[i]) : 0u;
             sum += v[q];
         }
         uint32_t x = sum;  // inclusive warp scan
@@ -260,89 +280,136 @@ __global__ void __launch_bounds__(1024) scan_kernel(const uint32_t *in, uint32_t
     }
 }
 
+// Bucket order: the bubbles of each bucket contiguous, with copies of their positions and cell
+// keys, so the candidate walks read contiguous memory.
 __global__ void list_scatter_kernel(ListArgs a) {
     const Ctl *c = a.ctl;
     if (!c->go) return;
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= c->n[a.npar]) return;
-    a.bitems[a.bstart[a.bkey[k]] + a.brank[k]] = k;
-}
-
-// Counts each bubble's candidates; the largest count of a 32-bubble group, rounded up to a multiple
-// of 32, sets its column length.
-__global__ void list_count_kernel(ListArgs a) {
-    Ctl *c = a.ctl;
-    if (!c->go) return;
-    const uint32_t n = c->n[a.npar];
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t m = 0;
-    if (k < n) {
-        const float4 p = a.pr[k];
-        const int4 q = a.cellc[k];
-        const float skin = c->skin;
-        for (int dz = -1; dz <= 1; ++dz)
-            for (int dy = -1; dy <= 1; ++dy)
-                for (int dx = -1; dx <= 1; ++dx) {
-                    const int x = q.x + dx, y = q.y + dy, z = q.z + dz;
-                    const uint32_t h = cell_hash(x, y, z, a.mask);
-                    const uint32_t s = a.bstart[h], e = s + a.bcount[h];
-                    for (uint32_t i = s; i < e; ++i) {
-                        const uint32_t j = a.bitems[i];
-                        if (j == k) continue;
-                        const int4 qj = a.cellc[j];
-                        if (qj.x != x || qj.y != y || qj.z != z) continue;
-                        m += candidate(p, a.pr[j], skin);
-                    }
-                }
-        a.cnt[k] = m;
-        if (m > (uint32_t)kMaxCand && atomicCAS(&c->fault, kFaultNone, kFaultDense) == kFaultNone) {
-            c->dense_bubble = k;
-            c->dense_count = m;
-        }
-    }
-    uint32_t g = m;
-    for (int o = 16; o; o >>= 1) g = max(g, __shfl_xor_sync(0xffffffffu, g, o));
-    // columns padded to whole 32-entry blocks: a group then owns exactly its share of the
-    // connection-bit words (word (t / 32) * 32 + lane of the group's block)
-    if ((threadIdx.x & 31) == 0 && k < ((n + 31) & ~31u)) a.gcap[k >> 5] = (g + 31) & ~31u;
-}
-
-// One warp per bubble: collects the candidates again, sorts them by index and writes the column.
-__global__ void __launch_bounds__(kFillWarps * 32) list_fill_kernel(ListArgs a) {
-    __shared__ uint32_t s_buf[kFillWarps][kMaxCand];
-    const Ctl *c = a.ctl;
-    if (!c->go || c->fault != kFaultNone) return;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const uint32_t k = blockIdx.x * kFillWarps + w;
-    if (k >= c->n[a.npar]) return;
-    uint32_t *buf = s_buf[w];
-    const float4 p = a.pr[k];
+    const uint32_t slot = a.bstart[a.bkey[k]] + a.brank[k];
     const int4 q = a.cellc[k];
-    const float skin = c->skin;
-    const uint32_t mk = a.cnt[k];  // the count pass's length (<= kMaxCand: the pass faults above it)
-    uint32_t m = 0;
-    for (int dz = -1; dz <= 1; ++dz)
-        for (int dy = -1; dy <= 1; ++dy)
-            for (int dx = -1; dx <= 1; ++dx) {
-                const int x = q.x + dx, y = q.y + dy, z = q.z + dz;
+    a.bitems[slot] = k;
+    a.spr[slot] = a.pr[k];
+    a.skey[slot] = cell_key(q.x, q.y, q.z);
+    a.cellc[k].w = (int)slot;
+}
+
+// The candidate walk of one warp for bubble k: the 5 x 5 x 5 cells around its own whose box comes
+// within its largest candidate range 3 (r_k + r_max) + skin (with a margin of 1 % of a cell for
+// the rounding of the cell coordinates), each bucket's slots 32 at a time; visit(i, ok) gets every
+// slot with ok = the slot holds a candidate of k (a bubble of that very cell, not k, within
+// 3 (r_k + r_j) + skin).
+template <class Visit>
+__device__ __forceinline__ void walk(const ListArgs &a, const Ctl *c, float4 p, int4 q, int lane, Visit &&visit) {
+    const float skin = c->skin, cs = c->cell;
+    const float reach = (p.w + c->rmax) * 3.0f + skin + 0.01f * cs;
+    const float reach2 = reach * reach;
+    for (int dz = -2; dz <= 2; ++dz) {
+        const int z = q.z + dz;
+        const float gz = fmaxf(fmaxf(z * cs - p.z, p.z - (z + 1) * cs), 0.0f);
+        for (int dy = -2; dy <= 2; ++dy) {
+            const int y = q.y + dy;
+            const float gy = fmaxf(fmaxf(y * cs - p.y, p.y - (y + 1) * cs), 0.0f);
+            for (int dx = -2; dx <= 2; ++dx) {
+                const int x = q.x + dx;
+                const float gx = fmaxf(fmaxf(x * cs - p.x, p.x - (x + 1) * cs), 0.0f);
+                if (gx * gx + gy * gy + gz * gz > reach2) continue;
                 const uint32_t h = cell_hash(x, y, z, a.mask);
+                const unsigned long long key = cell_key(x, y, z);
                 const uint32_t s = a.bstart[h], e = s + a.bcount[h];
                 for (uint32_t b0 = s; b0 < e; b0 += 32) {
                     const uint32_t i = b0 + lane;
-                    bool ok = false;
-                    uint32_t j = 0;
-                    if (i < e) {
-                        j = a.bitems[i];
-                        const int4 qj = a.cellc[j];
-                        ok = j != k && qj.x == x && qj.y == y && qj.z == z && candidate(p, a.pr[j], skin);
-                    }
-                    const uint32_t bal = __ballot_sync(0xffffffffu, ok);
-                    const uint32_t slot = m + __popc(bal & ((1u << lane) - 1u));
-                    if (ok && slot < mk) buf[slot] = j;
-                    m += __popc(bal);
+                    const bool ok = i < e && i != (uint32_t)q.w && a.skey[i] == key && candidate(p, a.spr[i], skin);
+                    visit(i, ok);
                 }
             }
-    m = min(m, mk);  // equal: both passes make the same decisions
+        }
+    }
+}
+
+// Bitonic sort of 32 R values held R per lane (element r * 32 + lane in v[r]), ascending: strides of
+// 32 and more compare within a lane's registers, smaller ones across lanes by shuffles.
+template <int R>
+__device__ __forceinline__ void warp_sort(uint32_t (&v)[R], int lane) {
+#pragma unroll
+    for (int size = 2; size <= 32 * R; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            if (stride >= 32) {
+                const int rs = stride >> 5;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const int o = r ^ rs;
+                    if (o > r) {
+                        const bool up = ((r * 32) & size) == 0;
+                        const uint32_t x = v[r], y = v[o];
+                        v[r] = up ? min(x, y) : max(x, y);
+                        v[o] = up ? max(x, y) : min(x, y);
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const uint32_t y = __shfl_xor_sync(0xffffffffu, v[r], stride);
+                    const bool up = (((r * 32) + lane) & size) == 0;
+                    const bool low = (lane & stride) == 0;
+                    v[r] = (low == up) ? min(v[r], y) : max(v[r], y);
+                }
+            }
+        }
+    }
+}
+
+// Sorts buf[0..m) (m <= 32 R, padded with kNone) in registers and writes it to the column; returns
+// the number of entries below k.
+template <int R>
+__device__ __forceinline__ uint32_t sort_write(const uint32_t *buf, uint32_t m, uint32_t k, uint32_t *col, int lane) {
+    uint32_t v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const uint32_t e = r * 32 + lane;
+        v[r] = e < m ? buf[e] : kNone;
+    }
+    warp_sort<R>(v, lane);
+    uint32_t below = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const uint32_t e = r * 32 + lane;
+        if (e < m) {
+            col[(size_t)e * 32] = v[r];
+            below += v[r] < k;
+        }
+    }
+    return below;
+}
+
+constexpr int kListWarps = 4;
+
+// Counts each bubble's candidates (a warp per bubble); the groups' largest counts size the list.
+__global__ void __launch_bounds__(kListWarps * 32) list_count_kernel(ListArgs a) {
+    Ctl *c = a.ctl;
+    if (!c->go) return;
+    const uint32_t n = c->n[a.npar];
+    const int lane = threadIdx.x & 31;
+    for (uint32_t k = blockIdx.x * kListWarps + (threadIdx.x >> 5); k < n; k += gridDim.x * kListWarps) {
+        const float4 p = a.pr[k];
+        const int4 q = a.cellc[k];
+        uint32_t m = 0;
+        walk(a, c, p, q, lane, [&](uint32_t, bool ok) { m += __popc(__ballot_sync(0xffffffffu, ok)); });
+        if (lane == 0) {
+            a.cnt[k] = m;
+            atomicMax(a.gcap + (k >> 5), m);
+            if (m > (uint32_t)kMaxCand && atomicCAS(&c->fault, kFaultNone, kFaultDense) == kFaultNone) {
+                c->dense_bubble = k;
+                c->dense_count = m;
+            }
+        }
+    }
+}
+
+// Lists longer than 1024 (rare): bitonic sort in shared memory.
+__device__ __noinline__ uint32_t sort_smem(uint32_t *buf, uint32_t m, uint32_t k, uint32_t *col, int lane) {
     uint32_t P = 1;
     while (P < m) P <<= 1;
     for (uint32_t t = m + lane; t < P; t += 32) buf[t] = kNone;
@@ -361,8 +428,50 @@ __global__ void __launch_bounds__(kFillWarps * 32) list_fill_kernel(ListArgs a) 
             }
             __syncwarp();
         }
-    uint32_t *col = a.nbr + a.goff[k >> 5] + (k & 31);
-    for (uint32_t t = lane; t < m; t += 32) col[(size_t)t * 32] = buf[t];
+    uint32_t below = 0;
+    for (uint32_t t = lane; t < m; t += 32) {
+        col[(size_t)t * 32] = buf[t];
+        below += buf[t] < k;
+    }
+    return below;
+}
+
+// A warp per bubble: collects the candidates again into shared memory, sorts them by index in
+// registers (bitonic; in shared memory beyond 1024) and writes the bubble's column and the length
+// of its lower part.
+__global__ void __launch_bounds__(kListWarps * 32, 4) list_fill_kernel(ListArgs a) {
+    __shared__ uint32_t s_buf[kListWarps][kMaxCand];
+    const Ctl *c = a.ctl;
+    if (!c->go || c->fault != kFaultNone) return;
+    const uint32_t n = c->n[a.npar];
+    const int lane = threadIdx.x & 31;
+    uint32_t *buf = s_buf[threadIdx.x >> 5];
+    for (uint32_t k = blockIdx.x * kListWarps + (threadIdx.x >> 5); k < n; k += gridDim.x * kListWarps) {
+        const float4 p = a.pr[k];
+        const int4 q = a.cellc[k];
+        const uint32_t mk = a.cnt[k];  // the count pass's length (<= kMaxCand: the pass faults above it)
+        uint32_t m = 0;
+        walk(a, c, p, q, lane, [&](uint32_t i, bool ok) {
+            const uint32_t bal = __ballot_sync(0xffffffffu, ok);
+            const uint32_t slot = m + __popc(bal & ((1u << lane) - 1u));
+            if (ok && slot < mk) buf[slot] = a.bitems[i];
+            m += __popc(bal);
+        });
+        m = min(m, mk);  // equal: both passes make the same decisions
+        __syncwarp();
+        uint32_t *col = a.nbr + a.goff[k >> 5] + (k & 31);
+        uint32_t below;
+        if (m <= 32) below = sort_write<1>(buf, m, k, col, lane);
+        else if (m <= 64) below = sort_write<2>(buf, m, k, col, lane);
+        else if (m <= 128) below = sort_write<4>(buf, m, k, col, lane);
+        else if (m <= 256) below = sort_write<8>(buf, m, k, col, lane);
+        else if (m <= 512) below = sort_write<16>(buf, m, k, col, lane);
+        else if (m <= 1024) below = sort_write<32>(buf, m, k, col, lane);
+        else below = sort_smem(buf, m, k, col, lane);
+        for (int o = 16; o; o >>= 1) below += __shfl_xor_sync(0xffffffffu, below, o);
+        if (lane == 0) a.split[k] = below;
+        __syncwarp();
+    }
 }
 
 // ----------------------------------------------------------------------------- the step
@@ -376,7 +485,7 @@ struct DynArgs {
     float4 *pr_out, *vt_out;
     uint32_t *id_out;
     float *force_out;  // forces-only mode: [n][3]
-    const uint32_t *cnt, *goff, *nbr;
+    const uint32_t *cnt, *split, *goff, *nbr;
     uint32_t *cflag;   // connection bits, one per list entry
     const float4 *p0;
     float flag_sq;     // squared displacement from p0 beyond which the next step rebuilds (< 0: always)
@@ -384,7 +493,7 @@ struct DynArgs {
 
 // compute_forces + the integration of step (foam_dynamics.rs:62-94, 172-202); with force_out set,
 // only the forces of the current state.
-__global__ void __launch_bounds__(kThreads) forces_kernel(DynArgs a) {
+__global__ void __launch_bounds__(kThreads, 5) forces_kernel(DynArgs a) {
     Ctl *c = a.ctl;
     if (c->fault != kFaultNone) return;
     const uint32_t n = c->n[a.npar];
@@ -419,29 +528,32 @@ __global__ void __launch_bounds__(kThreads) forces_kernel(DynArgs a) {
         by = ny * net;
         bz = nz * net;
     }
+    // one loop over the sorted list (no divergence between the two halves): entries t < split
+    // are j < k, whose pair force is evaluated with j first and enters negated; the buoyancy
+    // enters before the first j > k; the next entry's position is fetched one iteration ahead
     float fx = 0.0f, fy = 0.0f, fz = 0.0f;
-    const uint32_t m = a.cnt[k];
+    const uint32_t m = a.cnt[k], split = a.split[k];
     const uint32_t *col = a.nbr + a.goff[k >> 5] + (k & 31);
-    uint32_t t = 0;
-    for (; t < m; ++t) {  // j < k: the force on k is minus the force on j
-        const uint32_t j = __ldg(col + (size_t)t * 32);
-        if (j > k) break;
+    float4 next = m ? a.pr_in[__ldg(col)] : me;
+    for (uint32_t t = 0; t < m; ++t) {
+        const float4 o = next;
+        if (t + 1 < m) next = a.pr_in[__ldg(col + (size_t)(t + 1) * 32)];
+        if (t == split) {
+            fx = fx + bx;
+            fy = fy + by;
+            fz = fz + bz;
+        }
+        const bool lower = t < split;
         float gx, gy, gz;
-        pair_force(P, a.pr_in[j], me, gx, gy, gz);
-        fx = fx + (-gx);
-        fy = fy + (-gy);
-        fz = fz + (-gz);
+        pair_force(P, lower ? o : me, lower ? me : o, gx, gy, gz);
+        fx = fx + (lower ? -gx : gx);
+        fy = fy + (lower ? -gy : gy);
+        fz = fz + (lower ? -gz : gz);
     }
-    fx = fx + bx;
-    fy = fy + by;
-    fz = fz + bz;
-    for (; t < m; ++t) {
-        const uint32_t j = __ldg(col + (size_t)t * 32);
-        float gx, gy, gz;
-        pair_force(P, me, a.pr_in[j], gx, gy, gz);
-        fx = fx + gx;
-        fy = fy + gy;
-        fz = fz + gz;
+    if (split == m) {
+        fx = fx + bx;
+        fy = fy + by;
+        fz = fz + bz;
     }
     // compute_drag (foam_dynamics.rs:163-167)
     const float drag_coeff = 6.0f * kPi * P.viscosity * me.w;
@@ -468,17 +580,25 @@ __global__ void __launch_bounds__(kThreads) forces_kernel(DynArgs a) {
         vy = vy * s;
         vz = vz * s;
     }
-    a.pr_out[k] = make_float4(me.x + vx * a.dt, me.y + vy * a.dt, me.z + vz * a.dt, me.w);
+    const float4 np_ = make_float4(me.x + vx * a.dt, me.y + vy * a.dt, me.z + vz * a.dt, me.w);
+    a.pr_out[k] = np_;
     a.vt_out[k] = make_float4(vx, vy, vz, mv.w);
     a.id_out[k] = a.id_in[k];
+    // the neighbour list's displacement check on the new position (see connections_kernel)
+    const float4 q0 = a.p0[k];
+    const float ddx = np_.x - q0.x, ddy = np_.y - q0.y, ddz = np_.z - q0.z;
+    if (ddx * ddx + ddy * ddy + ddz * ddz > a.flag_sq) atomicOr(&c->need_rebuild, 1u);
 }
 
 // update_connections (foam.rs:322-364) on the new positions: a bit per list entry j > i; with
 // coalescence, the first connection in the reference's order whose Weber number exceeds the
-// threshold (foam_dynamics.rs:218-232); and the displacement check of the neighbour list. The list
-// holds every pair within range while no bubble has moved skin / 2 since its build; this pass
-// flags a rebuild once some bubble is within one step's travel (v_max |dt|) of 0.45 skin, so the
-// positions of the next step, which this pass and the next force pass read, are still covered.
+// threshold (foam_dynamics.rs:218-232). The connections are observable only after a call, so
+// without coalescence this pass runs on a call's last step alone.
+//
+// The neighbour list holds every pair within range while no bubble has moved skin / 2 since its
+// build. The force pass flags a rebuild once a new position is within one step's travel
+// (v_max |dt|) of 0.45 skin, so the positions of the next step, which this pass and the next force
+// pass read, are still covered.
 __global__ void __launch_bounds__(kThreads) connections_kernel(DynArgs a) {
     Ctl *c = a.ctl;
     if (c->fault != kFaultNone) return;
@@ -489,19 +609,16 @@ __global__ void __launch_bounds__(kThreads) connections_kernel(DynArgs a) {
         const Phys &P = a.P;
         const float4 me = a.pr_out[i];
         const float4 mv = a.vt_out[i];
-        const float4 q0 = a.p0[i];
-        const float ddx = me.x - q0.x, ddy = me.y - q0.y, ddz = me.z - q0.z;
-        if (ddx * ddx + ddy * ddy + ddz * ddz > a.flag_sq) atomicOr(&c->need_rebuild, 1u);
-        const uint32_t m = a.cnt[i];
+        const uint32_t m = a.cnt[i], t0 = a.split[i];
         const size_t g0 = a.goff[i >> 5];
         const uint32_t *col = a.nbr + g0 + (i & 31);
         uint32_t *fcol = a.cflag + (g0 >> 5) + (i & 31);
         const float threshold = -me.w * 0.3f;
         bool want = P.coalescence != 0;
         uint32_t word = 0;
-        for (uint32_t t = 0; t < m; ++t) {
+        for (uint32_t t = t0; t < m; ++t) {  // the entries j > i
             const uint32_t j = __ldg(col + (size_t)t * 32);
-            if (j > i) {
+            {
                 const float4 o = a.pr_out[j];
                 const float overlap = me.w + o.w - len3(me.x - o.x, me.y - o.y, me.z - o.z);
                 if (overlap > threshold) {
@@ -583,6 +700,7 @@ __global__ void __launch_bounds__(kThreads) merge_kernel(DynArgs a) {
 struct ConnArgs {
     const Ctl *ctl;
     uint32_t n;  // count before the merge of the last step
+    const uint32_t *split;
     float surface_tension;
     const float4 *pr, *vt;
     const uint32_t *id;
@@ -608,7 +726,7 @@ __global__ void conn_list_kernel(ConnArgs a) {
     const uint32_t *col = a.nbr + g0 + (i & 31);
     const uint32_t *fcol = a.cflag + (g0 >> 5) + (i & 31);
     uint32_t k = 0, o = kWrite ? a.off[i] : 0;
-    for (uint32_t t = 0; t < m; ++t) {
+    for (uint32_t t = a.split[i]; t < m; ++t) {
         if (!((fcol[(size_t)(t >> 5) * 32] >> (t & 31)) & 1u)) continue;
         const uint32_t j = col[(size_t)t * 32];
         if (!conn_kept(a, i, j)) continue;
@@ -703,7 +821,10 @@ struct sbs_foam_sim {
     float4 *p0 = nullptr;
     int4 *cellc = nullptr;
     uint32_t *bcount = nullptr, *bstart = nullptr, *bitems = nullptr, *bkey = nullptr, *brank = nullptr;
-    uint32_t *cnt = nullptr, *gcap = nullptr, *goff = nullptr;
+    float4 *spr = nullptr;
+    unsigned long long *skey = nullptr;
+    int list_blocks = 1;  // grid of the count / fill passes (a few blocks per SM, grid-stride)
+    uint32_t *cnt = nullptr, *split = nullptr, *gcap = nullptr, *goff = nullptr;
     uint32_t *nbr = nullptr, *cflag = nullptr;
     size_t nbr_cap = 0;
     float rmax0 = 0.0f;
@@ -745,10 +866,13 @@ ListArgs list_args(sbs_foam_sim *s) {
     a.bcount = s->bcount;
     a.bstart = s->bstart;
     a.bitems = s->bitems;
+    a.spr = s->spr;
+    a.skey = s->skey;
     a.bkey = s->bkey;
     a.brank = s->brank;
     a.mask = s->mask;
     a.cnt = s->cnt;
+    a.split = s->split;
     a.gcap = s->gcap;
     a.goff = s->goff;
     a.nbr = s->nbr;
@@ -756,12 +880,13 @@ ListArgs list_args(sbs_foam_sim *s) {
     return a;
 }
 
-// Skin of the neighbour list: about 16 steps of travel at the speed limit, between 2 % and 15 % of
-// the largest interaction range 6 r_max, and never below 2.5 steps of travel.
+// Skin of the neighbour list: about 40 steps of travel at the speed limit, between 5 % and 15 % of
+// the largest interaction range 6 r_max (the extra candidates cost a distance test each), and never
+// below 2.5 steps of travel.
 float skin_for(const sbs_foam_sim *s, float dt) {
     const float range = 6.0f * s->rmax0;
     const float travel = kMaxSpeed * std::fabs(dt);
-    const float want = std::min(std::max(2.02f * travel * 16.0f, 0.02f * range), 0.15f * range);
+    const float want = std::min(std::max(2.02f * travel * 40.0f, 0.05f * range), 0.15f * range);
     return std::max(want, 2.5f * travel);
 }
 
@@ -775,13 +900,14 @@ void enqueue_list(sbs_foam_sim *s, bool forced, float skin) {
     ListArgs a = list_args(s);
     s->list_skin = skin;
     cudaMemsetAsync(s->bcount, 0, sizeof(uint32_t) * (s->mask + 1), s->stream);
+    cudaMemsetAsync(s->gcap, 0, sizeof(uint32_t) * ((s->n_cap + 31) / 32), s->stream);
     list_begin_kernel<<<1, 1024, 0, s->stream>>>(a, forced ? 1 : 0, skin);
     list_bin_kernel<<<blocks(s->n_cap), kThreads, 0, s->stream>>>(a);
     scan_kernel<<<1, 1024, 0, s->stream>>>(s->bcount, s->bstart, s->mask + 1, 0, a);
     list_scatter_kernel<<<blocks(s->n_cap), kThreads, 0, s->stream>>>(a);
-    list_count_kernel<<<blocks(s->n_cap), kThreads, 0, s->stream>>>(a);
+    list_count_kernel<<<s->list_blocks, kListWarps * 32, 0, s->stream>>>(a);
     scan_kernel<<<1, 1024, 0, s->stream>>>(s->gcap, s->goff, 0, 1, a);
-    list_fill_kernel<<<blocks(s->n_cap, kFillWarps), kFillWarps * 32, 0, s->stream>>>(a);
+    list_fill_kernel<<<s->list_blocks, kListWarps * 32, 0, s->stream>>>(a);
 }
 
 DynArgs dyn_args(sbs_foam_sim *s, float dt, int in, int out) {
@@ -798,6 +924,7 @@ DynArgs dyn_args(sbs_foam_sim *s, float dt, int in, int out) {
     a.id_out = s->b.id[out];
     a.force_out = nullptr;
     a.cnt = s->cnt;
+    a.split = s->split;
     a.goff = s->goff;
     a.nbr = s->nbr;
     a.cflag = s->cflag;
@@ -890,9 +1017,12 @@ int sbs_foam_sim_destroy(sbs_foam_sim *s) {
     cudaFree(s->bcount);
     cudaFree(s->bstart);
     cudaFree(s->bitems);
+    cudaFree(s->spr);
+    cudaFree(s->skey);
     cudaFree(s->bkey);
     cudaFree(s->brank);
     cudaFree(s->cnt);
+    cudaFree(s->split);
     cudaFree(s->gcap);
     cudaFree(s->goff);
     free_list(s);
@@ -919,8 +1049,12 @@ int sbs_foam_sim_create(uint32_t n, const float *position, const float *radius, 
         rmax = std::max(rmax, radius[i]);
     }
     if ((rc = require_device())) return rc;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return set_error(SBS_E_CUDA, "foam dynamics: no device attributes");
     sbs_foam_sim *s = new sbs_foam_sim();
     s->n_cap = n;
+    s->list_blocks = (int)std::max<uint32_t>(1, std::min<uint32_t>((n + kListWarps - 1) / kListWarps, (uint32_t)sms * 16));
     s->phys = *p;
     s->rmax0 = rmax;
     uint32_t M = 1024;
@@ -943,9 +1077,12 @@ int sbs_foam_sim_create(uint32_t n, const float *position, const float *radius, 
     if (e == cudaSuccess) e = cudaMalloc(&s->bcount, sizeof(uint32_t) * M);
     if (e == cudaSuccess) e = cudaMalloc(&s->bstart, sizeof(uint32_t) * (M + 1));
     if (e == cudaSuccess) e = cudaMalloc(&s->bitems, sizeof(uint32_t) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&s->spr, sizeof(float4) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&s->skey, sizeof(unsigned long long) * n);
     if (e == cudaSuccess) e = cudaMalloc(&s->bkey, sizeof(uint32_t) * n);
     if (e == cudaSuccess) e = cudaMalloc(&s->brank, sizeof(uint32_t) * n);
     if (e == cudaSuccess) e = cudaMalloc(&s->cnt, sizeof(uint32_t) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&s->split, sizeof(uint32_t) * n);
     if (e == cudaSuccess) e = cudaMalloc(&s->gcap, sizeof(uint32_t) * groups);
     if (e == cudaSuccess) e = cudaMalloc(&s->goff, sizeof(uint32_t) * (groups + 1));
     if (e != cudaSuccess) return fail(e);
@@ -1001,7 +1138,7 @@ int sbs_foam_sim_step(sbs_foam_sim *s, float dt, uint32_t steps) {
             enqueue_list(s, false, skin);
             DynArgs a = dyn_args(s, dt, s->cur, s->cur ^ 1);
             forces_kernel<<<blocks(s->n_cap), kThreads, 0, s->stream>>>(a);
-            connections_kernel<<<blocks(s->n_cap), kThreads, 0, s->stream>>>(a);
+            if (coal || k + 1 == steps) connections_kernel<<<blocks(s->n_cap), kThreads, 0, s->stream>>>(a);
             s->conn_buf = s->cur ^ 1;
             s->conn_npar = s->npar;
             if (coal) {
@@ -1230,6 +1367,7 @@ int sbs_foam_sim_connections(sbs_foam_sim *s, sbs_bubble_connection *out, uint32
     a.vt = s->b.vt[s->conn_buf];
     a.id = s->b.id[s->conn_buf];
     a.cnt = s->cnt;
+    a.split = s->split;
     a.goff = s->goff;
     a.nbr = s->nbr;
     a.cflag = s->cflag;

@@ -97,6 +97,16 @@ def test_coalescence_matches_oracle(fd, orc):
     _same_state(sim, want)
 
 
+def test_dense_lists(fd, orc):
+    """Large bubbles on the same lattice: lists of about 630 candidates, 140 of them above 1024
+    (the register sort and the shared-memory sort)."""
+    pos, rad = fd.fcc_foam(3000, min_radius=0.028, max_radius=0.036, seed=17)
+    sim = fd.FoamSimulator(pos, rad)
+    np.testing.assert_array_equal(sim.compute_forces(), orc.foam_forces(sim.physics, pos, rad))
+    sim.step(1e-3, 3)
+    _same_state(sim, orc.foam_step(sim.physics, 1e-3, 3, pos, rad))
+
+
 def test_compression_grows_the_list(fd, orc):
     """Bubbles streaming to the centre without damping or forces: neighbour counts rise several
     times over, the list outgrows its storage mid-run and is regrown; the result stays exact."""
