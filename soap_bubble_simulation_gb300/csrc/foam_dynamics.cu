@@ -12,12 +12,15 @@
 //
 // Neighbour list (Verlet list): bubble k lists every j with |p_j - p_k| < 3 (r_k + r_j) + skin at
 // the time of the build; it stays complete while no bubble has moved skin / 2 since (two bubbles
-// close by at most twice that). The connection pass checks every bubble's displacement after
-// each step and flags a rebuild for the next one; merges flag one too. A rebuild bins the
-// bubbles into a spatial hash of cells (edge 6 r_max + skin, so the 27 cells around a bubble hold
-// all its candidates), counts and collects each bubble's candidates, and sorts each list with a
-// warp-wide bitonic sort in shared memory. Lists of 32 consecutive bubbles are interleaved
-// (entry t of bubble k at goff[k / 32] + 32 t + k % 32) so the force pass reads them coalesced.
+// close by at most twice that). The force pass checks every bubble's displacement after each step
+// and flags a rebuild for the next one; merges flag one too. A rebuild bins the bubbles into a
+// spatial hash of cells (edge half of 6 r_max + skin, so the 5 x 5 x 5 cells around a bubble hold
+// all its candidates), counts each bubble's candidates (a warp per bubble), orders the bubbles by
+// descending count, collects the candidates again and sorts each list by index with a warp-wide
+// bitonic sort in registers. The lists of 32 bubbles at consecutive positions of that order are
+// interleaved (entry t of the bubble at position q at goff[q / 32] + 32 t + q % 32): one warp of
+// the force pass runs those 32 bubbles, reads their lists coalesced and, their lengths being
+// nearly equal, idles little.
 //
 // State: per bubble float4 (x, y, z, radius) and float4 (vx, vy, vz, thickness_nm) and the id,
 // double-buffered; the bubble count lives on the device (a merge changes it) and every kernel
@@ -164,6 +167,9 @@ struct ListArgs {
     uint32_t mask;          // hash buckets - 1
     uint32_t *cnt;          // list length per bubble
     uint32_t *split;        // entries j < k of each list (the sorted list's lower part)
+    uint32_t *perm;         // bubbles by descending list length: the order of the 32-bubble groups
+    uint32_t *inv;          // position of each bubble in perm
+    uint32_t *mhist, *mstart;  // bubbles per list length (kMaxCand + 1 bins, longest first)
     uint32_t *gcap;         // largest list length of each 32-bubble group
     uint32_t *goff;         // group offsets (ngroups + 1)
     uint32_t *nbr;          // interleaved lists
@@ -295,37 +301,90 @@ __global__ void list_scatter_kernel(ListArgs a) {
     a.cellc[k].w = (int)slot;
 }
 
-// The candidate walk of one warp for bubble k: the 5 x 5 x 5 cells around its own whose box comes
-// within its largest candidate range 3 (r_k + r_max) + skin (with a margin of 1 % of a cell for
-// the rounding of the cell coordinates), each bucket's slots 32 at a time; visit(i, ok) gets every
-// slot with ok = the slot holds a candidate of k (a bubble of that very cell, not k, within
-// 3 (r_k + r_j) + skin).
+// Per-warp table of the cells a walk visits: slot range, cell key and the running member count.
+struct CellTable {
+    uint32_t s[128], n[128], pre[129];
+    unsigned long long key[128];
+};
+
+// The candidate walk of one warp for bubble k. First the 5 x 5 x 5 cells around its own whose box
+// comes within its largest candidate range 3 (r_k + r_max) + skin (with a margin of 1 % of a cell
+// for the rounding of the cell coordinates) and whose bucket is not empty go into the table, 32
+// cells at a time; then the members of all of them are swept as one range, 32 slots a round, so
+// the loads of many cells are in flight together. visit(i, ok) gets every slot with ok = the slot
+// holds a candidate of k (a bubble of that very cell, not k, within 3 (r_k + r_j) + skin).
 template <class Visit>
-__device__ __forceinline__ void walk(const ListArgs &a, const Ctl *c, float4 p, int4 q, int lane, Visit &&visit) {
+__device__ __forceinline__ void walk(const ListArgs &a, const Ctl *c, float4 p, int4 q, int lane, CellTable &T,
+                                     Visit &&visit) {
     const float skin = c->skin, cs = c->cell;
     const float reach = (p.w + c->rmax) * 3.0f + skin + 0.01f * cs;
     const float reach2 = reach * reach;
-    for (int dz = -2; dz <= 2; ++dz) {
-        const int z = q.z + dz;
-        const float gz = fmaxf(fmaxf(z * cs - p.z, p.z - (z + 1) * cs), 0.0f);
-        for (int dy = -2; dy <= 2; ++dy) {
-            const int y = q.y + dy;
+    uint32_t nt = 0;
+    for (int c0 = 0; c0 < 125; c0 += 32) {
+        const int ci = c0 + lane;
+        bool use = false;
+        uint32_t s0 = 0, cnt = 0;
+        unsigned long long key = 0;
+        if (ci < 125) {
+            const int x = q.x + ci % 5 - 2, y = q.y + (ci / 5) % 5 - 2, z = q.z + ci / 25 - 2;
+            const float gx = fmaxf(fmaxf(x * cs - p.x, p.x - (x + 1) * cs), 0.0f);
             const float gy = fmaxf(fmaxf(y * cs - p.y, p.y - (y + 1) * cs), 0.0f);
-            for (int dx = -2; dx <= 2; ++dx) {
-                const int x = q.x + dx;
-                const float gx = fmaxf(fmaxf(x * cs - p.x, p.x - (x + 1) * cs), 0.0f);
-                if (gx * gx + gy * gy + gz * gz > reach2) continue;
+            const float gz = fmaxf(fmaxf(z * cs - p.z, p.z - (z + 1) * cs), 0.0f);
+            if (gx * gx + gy * gy + gz * gz <= reach2) {
                 const uint32_t h = cell_hash(x, y, z, a.mask);
-                const unsigned long long key = cell_key(x, y, z);
-                const uint32_t s = a.bstart[h], e = s + a.bcount[h];
-                for (uint32_t b0 = s; b0 < e; b0 += 32) {
-                    const uint32_t i = b0 + lane;
-                    const bool ok = i < e && i != (uint32_t)q.w && a.skey[i] == key && candidate(p, a.spr[i], skin);
-                    visit(i, ok);
+                cnt = a.bcount[h];
+                if (cnt) {
+                    s0 = a.bstart[h];
+                    key = cell_key(x, y, z);
+                    use = true;
                 }
             }
         }
+        const uint32_t bal = __ballot_sync(0xffffffffu, use);
+        if (use) {
+            const uint32_t r = nt + __popc(bal & ((1u << lane) - 1u));
+            T.s[r] = s0;
+            T.n[r] = cnt;
+            T.key[r] = key;
+        }
+        nt += __popc(bal);
     }
+    __syncwarp();
+    uint32_t v[4], sum = 0;  // exclusive running count over the table, 4 entries a lane
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t idx = lane * 4 + k;
+        v[k] = idx < nt ? T.n[idx] : 0u;
+        sum += v[k];
+    }
+    uint32_t x = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, x, 31);
+    uint32_t run = x - sum;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t idx = lane * 4 + k;
+        if (idx < nt) T.pre[idx] = run;
+        run += v[k];
+    }
+    if (lane == 0) T.pre[nt] = total;
+    __syncwarp();
+    uint32_t cc = 0;
+    for (uint32_t v0 = 0; v0 < total; v0 += 32) {
+        const uint32_t vv = v0 + lane;
+        bool ok = false;
+        uint32_t i = 0;
+        if (vv < total) {
+            while (T.pre[cc + 1] <= vv) ++cc;
+            i = T.s[cc] + (vv - T.pre[cc]);
+            ok = i != (uint32_t)q.w && a.skey[i] == T.key[cc] && candidate(p, a.spr[i], skin);
+        }
+        visit(i, ok);
+    }
+    __syncwarp();  // the table is rebuilt for the warp's next bubble
 }
 
 // Bitonic sort of 32 R values held R per lane (element r * 32 + lane in v[r]), ascending: strides of
@@ -386,8 +445,9 @@ __device__ __forceinline__ uint32_t sort_write(const uint32_t *buf, uint32_t m, 
 
 constexpr int kListWarps = 4;
 
-// Counts each bubble's candidates (a warp per bubble); the groups' largest counts size the list.
+// Counts each bubble's candidates (a warp per bubble), and the bubbles of each count.
 __global__ void __launch_bounds__(kListWarps * 32) list_count_kernel(ListArgs a) {
+    __shared__ CellTable s_tab[kListWarps];
     Ctl *c = a.ctl;
     if (!c->go) return;
     const uint32_t n = c->n[a.npar];
@@ -396,10 +456,11 @@ __global__ void __launch_bounds__(kListWarps * 32) list_count_kernel(ListArgs a)
         const float4 p = a.pr[k];
         const int4 q = a.cellc[k];
         uint32_t m = 0;
-        walk(a, c, p, q, lane, [&](uint32_t, bool ok) { m += __popc(__ballot_sync(0xffffffffu, ok)); });
+        walk(a, c, p, q, lane, s_tab[threadIdx.x >> 5],
+             [&](uint32_t, bool ok) { m += __popc(__ballot_sync(0xffffffffu, ok)); });
         if (lane == 0) {
             a.cnt[k] = m;
-            atomicMax(a.gcap + (k >> 5), m);
+            atomicAdd(a.mhist + (kMaxCand - min(m, (uint32_t)kMaxCand)), 1u);
             if (m > (uint32_t)kMaxCand && atomicCAS(&c->fault, kFaultNone, kFaultDense) == kFaultNone) {
                 c->dense_bubble = k;
                 c->dense_count = m;
@@ -436,11 +497,36 @@ __device__ __noinline__ uint32_t sort_smem(uint32_t *buf, uint32_t m, uint32_t k
     return below;
 }
 
+// Orders the bubbles by descending list length (counting sort over the lengths): the 32 bubbles of a
+// group, which one warp of the force pass runs, then have lists of nearly the same length, and the
+// longest groups start first.
+__global__ void list_order_kernel(ListArgs a) {
+    const Ctl *c = a.ctl;
+    if (!c->go || c->fault != kFaultNone) return;
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c->n[a.npar]) return;
+    const uint32_t pos = atomicAdd(a.mstart + (kMaxCand - a.cnt[k]), 1u);
+    a.perm[pos] = k;
+    a.inv[k] = pos;
+}
+
+// The largest list length of each group of 32 consecutive positions of the order.
+__global__ void list_gcap_kernel(ListArgs a) {
+    const Ctl *c = a.ctl;
+    if (!c->go || c->fault != kFaultNone) return;
+    const uint32_t n = c->n[a.npar];
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t m = t < n ? a.cnt[a.perm[t]] : 0u;
+    for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && t < ((n + 31) & ~31u)) a.gcap[t >> 5] = m;
+}
+
 // A warp per bubble: collects the candidates again into shared memory, sorts them by index in
 // registers (bitonic; in shared memory beyond 1024) and writes the bubble's column and the length
 // of its lower part.
 __global__ void __launch_bounds__(kListWarps * 32, 4) list_fill_kernel(ListArgs a) {
     __shared__ uint32_t s_buf[kListWarps][kMaxCand];
+    __shared__ CellTable s_tab[kListWarps];
     const Ctl *c = a.ctl;
     if (!c->go || c->fault != kFaultNone) return;
     const uint32_t n = c->n[a.npar];
@@ -451,7 +537,7 @@ __global__ void __launch_bounds__(kListWarps * 32, 4) list_fill_kernel(ListArgs 
         const int4 q = a.cellc[k];
         const uint32_t mk = a.cnt[k];  // the count pass's length (<= kMaxCand: the pass faults above it)
         uint32_t m = 0;
-        walk(a, c, p, q, lane, [&](uint32_t i, bool ok) {
+        walk(a, c, p, q, lane, s_tab[threadIdx.x >> 5], [&](uint32_t i, bool ok) {
             const uint32_t bal = __ballot_sync(0xffffffffu, ok);
             const uint32_t slot = m + __popc(bal & ((1u << lane) - 1u));
             if (ok && slot < mk) buf[slot] = a.bitems[i];
@@ -459,7 +545,8 @@ __global__ void __launch_bounds__(kListWarps * 32, 4) list_fill_kernel(ListArgs 
         });
         m = min(m, mk);  // equal: both passes make the same decisions
         __syncwarp();
-        uint32_t *col = a.nbr + a.goff[k >> 5] + (k & 31);
+        const uint32_t pos = a.inv[k];
+        uint32_t *col = a.nbr + a.goff[pos >> 5] + (pos & 31);
         uint32_t below;
         if (m <= 32) below = sort_write<1>(buf, m, k, col, lane);
         else if (m <= 64) below = sort_write<2>(buf, m, k, col, lane);
@@ -486,6 +573,7 @@ struct DynArgs {
     uint32_t *id_out;
     float *force_out;  // forces-only mode: [n][3]
     const uint32_t *cnt, *split, *goff, *nbr;
+    const uint32_t *perm;  // thread t of the force and connection passes runs bubble perm[t]
     uint32_t *cflag;   // connection bits, one per list entry
     const float4 *p0;
     float flag_sq;     // squared displacement from p0 beyond which the next step rebuilds (< 0: always)
@@ -497,14 +585,15 @@ __global__ void __launch_bounds__(kThreads, 5) forces_kernel(DynArgs a) {
     Ctl *c = a.ctl;
     if (c->fault != kFaultNone) return;
     const uint32_t n = c->n[a.npar];
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k == 0 && !a.force_out) {
+    const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t0 == 0 && !a.force_out) {
         c->steps_done += 1;
         c->nconn = 0;
         c->coal_key = kNoPair;
         c->merged_a = c->merged_b = kNone;
     }
-    if (k >= n) return;
+    if (t0 >= n) return;
+    const uint32_t k = a.perm[t0];
     const Phys &P = a.P;
     const float4 me = a.pr_in[k];
     const float4 mv = a.vt_in[k];
@@ -533,7 +622,7 @@ __global__ void __launch_bounds__(kThreads, 5) forces_kernel(DynArgs a) {
     // enters before the first j > k; the next entry's position is fetched one iteration ahead
     float fx = 0.0f, fy = 0.0f, fz = 0.0f;
     const uint32_t m = a.cnt[k], split = a.split[k];
-    const uint32_t *col = a.nbr + a.goff[k >> 5] + (k & 31);
+    const uint32_t *col = a.nbr + a.goff[t0 >> 5] + (t0 & 31);
     float4 next = m ? a.pr_in[__ldg(col)] : me;
     for (uint32_t t = 0; t < m; ++t) {
         const float4 o = next;
@@ -603,16 +692,17 @@ __global__ void __launch_bounds__(kThreads) connections_kernel(DynArgs a) {
     Ctl *c = a.ctl;
     if (c->fault != kFaultNone) return;
     const uint32_t n = c->n[a.npar];
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t count = 0;
-    if (i < n) {
+    if (pos < n) {
+        const uint32_t i = a.perm[pos];
         const Phys &P = a.P;
         const float4 me = a.pr_out[i];
         const float4 mv = a.vt_out[i];
         const uint32_t m = a.cnt[i], t0 = a.split[i];
-        const size_t g0 = a.goff[i >> 5];
-        const uint32_t *col = a.nbr + g0 + (i & 31);
-        uint32_t *fcol = a.cflag + (g0 >> 5) + (i & 31);
+        const size_t g0 = a.goff[pos >> 5];
+        const uint32_t *col = a.nbr + g0 + (pos & 31);
+        uint32_t *fcol = a.cflag + (g0 >> 5) + (pos & 31);
         const float threshold = -me.w * 0.3f;
         bool want = P.coalescence != 0;
         uint32_t word = 0;
@@ -700,7 +790,7 @@ __global__ void __launch_bounds__(kThreads) merge_kernel(DynArgs a) {
 struct ConnArgs {
     const Ctl *ctl;
     uint32_t n;  // count before the merge of the last step
-    const uint32_t *split;
+    const uint32_t *split, *inv;
     float surface_tension;
     const float4 *pr, *vt;
     const uint32_t *id;
@@ -721,10 +811,10 @@ template <bool kWrite>
 __global__ void conn_list_kernel(ConnArgs a) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
-    const uint32_t m = a.cnt[i];
-    const size_t g0 = a.goff[i >> 5];
-    const uint32_t *col = a.nbr + g0 + (i & 31);
-    const uint32_t *fcol = a.cflag + (g0 >> 5) + (i & 31);
+    const uint32_t m = a.cnt[i], pos = a.inv[i];
+    const size_t g0 = a.goff[pos >> 5];
+    const uint32_t *col = a.nbr + g0 + (pos & 31);
+    const uint32_t *fcol = a.cflag + (g0 >> 5) + (pos & 31);
     uint32_t k = 0, o = kWrite ? a.off[i] : 0;
     for (uint32_t t = a.split[i]; t < m; ++t) {
         if (!((fcol[(size_t)(t >> 5) * 32] >> (t & 31)) & 1u)) continue;
@@ -825,6 +915,7 @@ struct sbs_foam_sim {
     unsigned long long *skey = nullptr;
     int list_blocks = 1;  // grid of the count / fill passes (a few blocks per SM, grid-stride)
     uint32_t *cnt = nullptr, *split = nullptr, *gcap = nullptr, *goff = nullptr;
+    uint32_t *perm = nullptr, *inv = nullptr, *mhist = nullptr, *mstart = nullptr;
     uint32_t *nbr = nullptr, *cflag = nullptr;
     size_t nbr_cap = 0;
     float rmax0 = 0.0f;
@@ -874,6 +965,10 @@ ListArgs list_args(sbs_foam_sim *s) {
     a.cnt = s->cnt;
     a.split = s->split;
     a.gcap = s->gcap;
+    a.perm = s->perm;
+    a.inv = s->inv;
+    a.mhist = s->mhist;
+    a.mstart = s->mstart;
     a.goff = s->goff;
     a.nbr = s->nbr;
     a.nbr_cap = s->nbr_cap;
@@ -900,12 +995,15 @@ void enqueue_list(sbs_foam_sim *s, bool forced, float skin) {
     ListArgs a = list_args(s);
     s->list_skin = skin;
     cudaMemsetAsync(s->bcount, 0, sizeof(uint32_t) * (s->mask + 1), s->stream);
-    cudaMemsetAsync(s->gcap, 0, sizeof(uint32_t) * ((s->n_cap + 31) / 32), s->stream);
+    cudaMemsetAsync(s->mhist, 0, sizeof(uint32_t) * (kMaxCand + 1), s->stream);
     list_begin_kernel<<<1, 1024, 0, s->stream>>>(a, forced ? 1 : 0, skin);
     list_bin_kernel<<<blocks(s->n_cap), kThreads, 0, s->stream>>>(a);
     scan_kernel<<<1, 1024, 0, s->stream>>>(s->bcount, s->bstart, s->mask + 1, 0, a);
     list_scatter_kernel<<<blocks(s->n_cap), kThreads, 0, s->stream>>>(a);
     list_count_kernel<<<s->list_blocks, kListWarps * 32, 0, s->stream>>>(a);
+    scan_kernel<<<1, 1024, 0, s->stream>>>(s->mhist, s->mstart, kMaxCand + 1, 0, a);
+    list_order_kernel<<<blocks(s->n_cap), kThreads, 0, s->stream>>>(a);
+    list_gcap_kernel<<<blocks(s->n_cap), kThreads, 0, s->stream>>>(a);
     scan_kernel<<<1, 1024, 0, s->stream>>>(s->gcap, s->goff, 0, 1, a);
     list_fill_kernel<<<s->list_blocks, kListWarps * 32, 0, s->stream>>>(a);
 }
@@ -925,6 +1023,7 @@ DynArgs dyn_args(sbs_foam_sim *s, float dt, int in, int out) {
     a.force_out = nullptr;
     a.cnt = s->cnt;
     a.split = s->split;
+    a.perm = s->perm;
     a.goff = s->goff;
     a.nbr = s->nbr;
     a.cflag = s->cflag;
@@ -1023,6 +1122,10 @@ int sbs_foam_sim_destroy(sbs_foam_sim *s) {
     cudaFree(s->brank);
     cudaFree(s->cnt);
     cudaFree(s->split);
+    cudaFree(s->perm);
+    cudaFree(s->inv);
+    cudaFree(s->mhist);
+    cudaFree(s->mstart);
     cudaFree(s->gcap);
     cudaFree(s->goff);
     free_list(s);
@@ -1083,6 +1186,10 @@ int sbs_foam_sim_create(uint32_t n, const float *position, const float *radius, 
     if (e == cudaSuccess) e = cudaMalloc(&s->brank, sizeof(uint32_t) * n);
     if (e == cudaSuccess) e = cudaMalloc(&s->cnt, sizeof(uint32_t) * n);
     if (e == cudaSuccess) e = cudaMalloc(&s->split, sizeof(uint32_t) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&s->perm, sizeof(uint32_t) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&s->inv, sizeof(uint32_t) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&s->mhist, sizeof(uint32_t) * (kMaxCand + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&s->mstart, sizeof(uint32_t) * (kMaxCand + 2));
     if (e == cudaSuccess) e = cudaMalloc(&s->gcap, sizeof(uint32_t) * groups);
     if (e == cudaSuccess) e = cudaMalloc(&s->goff, sizeof(uint32_t) * (groups + 1));
     if (e != cudaSuccess) return fail(e);
@@ -1368,6 +1475,7 @@ int sbs_foam_sim_connections(sbs_foam_sim *s, sbs_bubble_connection *out, uint32
     a.id = s->b.id[s->conn_buf];
     a.cnt = s->cnt;
     a.split = s->split;
+    a.inv = s->inv;
     a.goff = s->goff;
     a.nbr = s->nbr;
     a.cflag = s->cflag;

@@ -8,7 +8,10 @@ spectral colour of --points seeded points, tensor-core or FP32 contraction), `su
 `surrogate-layered` (--steps 64-pass surrogate intervals of the field, untrained seeded weights:
 the same kernels and shapes as a trained network; --activation gelu or hswish), `foam` (the 4096-bubble foam batch, --steps
 steps with the default tiles), `shade` (--steps 3840 x 2160 headless frames of the bubble
-fragment shader), `caustics` (--steps caustic maps of the field after 100 WGSL passes). The field is the seeded smooth-mode field of
+fragment shader), `caustics` (--steps caustic maps of the field after 100 WGSL passes),
+`foam-dynamics` (FoamSimulator::step on an FCC foam of --bubbles bubbles: 3 steps, then --steps
+steps in one call), `branched` (--steps branched-flow steps at the reference's defaults, patch
+off, over a seeded 128 x 64 film). The field is the seeded smooth-mode field of
 the 2048-resolution workload, built at the requested resolution. Steps launch one kernel each
 (graph replay for runs of 8 or more).
 """
@@ -27,7 +30,7 @@ def main(argv=None) -> None:
     p = argparse.ArgumentParser()
     p.add_argument("--case", default="wgsl",
                    choices=["wgsl", "cpu", "cpu32", "spectral-tc", "spectral-fp32", "surrogate-fused", "surrogate-layered",
-                            "foam", "shade", "caustics"])
+                            "foam", "shade", "caustics", "foam-dynamics", "branched"])
     p.add_argument("--points", type=int, default=1 << 20, help="spectral cases: number of points")
     p.add_argument("--res", type=int, default=2048)
     p.add_argument("--steps", type=int, default=20)
@@ -54,6 +57,28 @@ def main(argv=None) -> None:
         for _ in range(a.steps):
             render_frame(u, cam, 3840, 2160)
         print(f"shaded {a.steps} 3840 x 2160 frames")
+        return
+    if a.case == "foam-dynamics":
+        from .foam_dynamics import FoamSimulator, fcc_foam
+
+        sim = FoamSimulator(*fcc_foam(a.bubbles, seed=0))
+        sim.step(1e-3, 3)
+        sim.step(1e-3, a.steps)
+        print(f"stepped a {a.bubbles}-bubble foam {a.steps + 3} times ({sim.connection_count()} connections)")
+        return
+    if a.case == "branched":
+        import numpy as np
+
+        from .branched import BranchedFlowParams, branched_flow_step, generate_scatterers
+
+        bp = BranchedFlowParams.default()
+        bp.patch_enabled = 0
+        th = (synthetic.smooth_modes(64, 128, seed=3) * 2e4).astype(np.float32)
+        sc = generate_scatterers(bp, time=1.5)
+        tex = np.zeros((bp.tex_height, bp.tex_width), np.uint32)
+        for _ in range(a.steps):
+            tex = branched_flow_step(bp, th, sc, tex)
+        print(f"ran {a.steps} branched-flow steps")
         return
     if a.case == "foam":
         from .foam import FoamDrainage
