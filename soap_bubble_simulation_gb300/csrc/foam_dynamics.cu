@@ -975,13 +975,13 @@ ListArgs list_args(sbs_foam_sim *s) {
     return a;
 }
 
-// Skin of the neighbour list: about 40 steps of travel at the speed limit, between 5 % and 15 % of
-// the largest interaction range 6 r_max (the extra candidates cost a distance test each), and never
-// below 2.5 steps of travel.
+// Skin of the neighbour list: about 80 steps of travel at the speed limit, between 8 % and 20 % of
+// the largest interaction range 6 r_max (the extra candidates cost a squared-distance test each),
+// and never below 2.5 steps of travel.
 float skin_for(const sbs_foam_sim *s, float dt) {
     const float range = 6.0f * s->rmax0;
     const float travel = kMaxSpeed * std::fabs(dt);
-    const float want = std::min(std::max(2.02f * travel * 40.0f, 0.05f * range), 0.15f * range);
+    const float want = std::min(std::max(2.02f * travel * 80.0f, 0.08f * range), 0.2f * range);
     return std::max(want, 2.5f * travel);
 }
 
