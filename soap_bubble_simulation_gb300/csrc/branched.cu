@@ -150,9 +150,13 @@ __device__ __forceinline__ void deposit(const TraceArgs &a, float u, float v, fl
 __global__ void __launch_bounds__(128) trace_kernel(TraceArgs a) {
     extern __shared__ __align__(16) uint8_t smem[];
     sbs_scatterer *sc = reinterpret_cast<sbs_scatterer *>(smem);
-    uint32_t *off = reinterpret_cast<uint32_t *>(sc + a.nscat);
+    float *scut = reinterpret_cast<float *>(sc + a.nscat);  // each scatterer's cutoff 4.5 / inv_sigma_sq
+    uint32_t *off = reinterpret_cast<uint32_t *>(scut + a.nscat);
     uint16_t *lst = reinterpret_cast<uint16_t *>(off + kGrid * kGrid + 1);
-    for (int k = threadIdx.x; k < a.nscat; k += blockDim.x) sc[k] = a.scat[k];
+    for (int k = threadIdx.x; k < a.nscat; k += blockDim.x) {
+        sc[k] = a.scat[k];
+        scut[k] = 4.5f / a.scat[k].inv_sigma_sq;
+    }
     for (int k = threadIdx.x; k <= kGrid * kGrid; k += blockDim.x) off[k] = a.list_off[k];
     for (int k = threadIdx.x; k < a.nlist; k += blockDim.x) lst[k] = a.list[k];
     __syncthreads();
@@ -202,11 +206,14 @@ __global__ void __launch_bounds__(128) trace_kernel(TraceArgs a) {
         // particle kick: total_scatterer_force (:256-290) over the ray cell's neighbourhood list
         float fx = 0.0f, fy = 0.0f;
         const int cell = grid_cell(v) * kGrid + grid_cell(u);
-        for (uint32_t k = off[cell]; k < off[cell + 1]; ++k) {
-            const sbs_scatterer q = sc[lst[k]];
+        const uint32_t k1 = off[cell + 1];
+#pragma unroll 2
+        for (uint32_t k = off[cell]; k < k1; ++k) {
+            const uint32_t idx = lst[k];
+            const sbs_scatterer q = sc[idx];
             const float dx = u - q.pos_u, dy = v - q.pos_v;
             const float r2 = dx * dx + dy * dy;
-            if (r2 > 4.5f / q.inv_sigma_sq) continue;  // scatterer_force's cutoff: adds zero
+            if (r2 > scut[idx]) continue;  // scatterer_force's cutoff: adds zero
             const float e = exp_cw(-r2 * q.inv_sigma_sq);
             fx += dx * q.strength * q.inv_sigma_sq * 2.0f * e;
             fy += dy * q.strength * q.inv_sigma_sq * 2.0f * e;
@@ -459,7 +466,7 @@ int sbs_branched_flow(const sbs_branched_params *p, const float *thickness, uint
         a.nscat = nscat;
         a.nlist = (int)lst.size();
         a.tex = d_tex;
-        const size_t smem = sc_b + off_b + sizeof(uint16_t) * lst.size() + 16;
+        const size_t smem = sc_b + sizeof(float) * nscat + off_b + sizeof(uint16_t) * lst.size() + 16;
         e = cudaFuncSetAttribute(trace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e == cudaSuccess) {
             trace_kernel<<<(p->num_rays + 127) / 128, 128, smem, s>>>(a);
