@@ -107,17 +107,23 @@ def test_dense_lists(fd, orc):
     _same_state(sim, orc.foam_step(sim.physics, 1e-3, 3, pos, rad))
 
 
-def test_compression_grows_the_list(fd, orc):
+@pytest.mark.parametrize("coalescence", [0, 1])
+def test_compression_grows_the_list(fd, orc, coalescence):
     """Bubbles streaming to the centre without damping or forces: neighbour counts rise several
-    times over, the list outgrows its storage mid-run and is regrown; the result stays exact."""
+    times over, the list outgrows its storage mid-run and is regrown (the steps after the
+    overflowing rebuild are redone from the last completed one); the result stays exact. With
+    coalescence the streams also merge, a bubble per step."""
     pos, rad = fd.fcc_foam(1000, spacing=0.05, jitter=0.2, min_radius=0.004, max_radius=0.006, seed=13)
     vel = (-0.1 * pos / np.maximum(np.linalg.norm(pos, axis=1, keepdims=True), 1e-6)).astype(np.float32)
     p = _phys(fd, gravity=[0.0, 0.0, 0.0], damping=1.0, van_der_waals_strength=0.0, repulsion_stiffness=0.0,
-              viscosity=0.0)
+              viscosity=0.0, coalescence_enabled=coalescence)
     sim = fd.FoamSimulator(pos, rad, physics=p)
     sim.set_state(velocity=vel)
     sim.step(0.01, 150)
-    _same_state(sim, orc.foam_step(p, 0.01, 150, pos, rad, velocity=vel))
+    want = orc.foam_step(p, 0.01, 150, pos, rad, velocity=vel)
+    if coalescence:
+        assert want["position"].shape[0] < 1000
+    _same_state(sim, want)
 
 
 def test_large_cluster_against_subset(fd, orc):
@@ -134,6 +140,30 @@ def test_large_cluster_against_subset(fd, orc):
     np.testing.assert_array_equal(sim.compute_forces()[idx],
                                   orc.foam_forces_subset(sim.physics, b["position"], b["radius"], idx,
                                                          velocity=b["velocity"]))
+
+
+def test_edge_clusters(fd, orc):
+    """One bubble; two bubbles on the same centre (the reference's distance < 1e-6 branch: no
+    force); far-apart clusters, 1 km and 30 km out (their cells share hash buckets with the
+    near ones)."""
+    one = fd.FoamSimulator([[0.1, 0.2, 0.3]], [0.02])
+    one.step(1e-3, 5)
+    _same_state(one, orc.foam_step(one.physics, 1e-3, 5, [[0.1, 0.2, 0.3]], [0.02]))
+    same = fd.FoamSimulator([[0, 0, 0], [0, 0, 0], [0.03, 0, 0]], [0.02, 0.02, 0.02])
+    np.testing.assert_array_equal(same.compute_forces(),
+                                  orc.foam_forces(same.physics, [[0, 0, 0], [0, 0, 0], [0.03, 0, 0]], [0.02] * 3))
+    a, ra = fd.fcc_foam(300, seed=31)
+    b, rb = fd.fcc_foam(200, seed=32)
+    c, rc = fd.fcc_foam(100, seed=33)
+    pos = np.concatenate([a, b + np.float32([1000.0, 0, 0]), c + np.float32([-3e4, 2e4, 5.0])]).astype(np.float32)
+    rad = np.concatenate([ra, rb, rc])
+    g = np.random.default_rng(34)
+    order = g.permutation(pos.shape[0])  # the clusters interleaved in bubble order
+    pos, rad = pos[order], rad[order]
+    sim = fd.FoamSimulator(pos, rad)
+    np.testing.assert_array_equal(sim.compute_forces(), orc.foam_forces(sim.physics, pos, rad))
+    sim.step(2e-3, 15)
+    _same_state(sim, orc.foam_step(sim.physics, 2e-3, 15, pos, rad))
 
 
 def test_couple_thickness(fd, sbs):
