@@ -1324,27 +1324,32 @@ int sbs_foam_sim_get_state(sbs_foam_sim *s, float *position, float *velocity, fl
         SBS_CUDA_TRY(cudaStreamSynchronize(s->stream));
         return SBS_OK;
     }
-    std::vector<float4> pr(n), vt(n);
-    std::vector<uint32_t> id(n);
-    SBS_CUDA_TRY(cudaMemcpyAsync(pr.data(), s->b.pr[c], sizeof(float4) * n, cudaMemcpyDeviceToHost, s->stream));
-    SBS_CUDA_TRY(cudaMemcpyAsync(vt.data(), s->b.vt[c], sizeof(float4) * n, cudaMemcpyDeviceToHost, s->stream));
-    SBS_CUDA_TRY(cudaMemcpyAsync(id.data(), s->b.id[c], sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s->stream));
-    SBS_CUDA_TRY(cudaStreamSynchronize(s->stream));
-    for (uint32_t i = 0; i < n; ++i) {
-        if (position) {
-            position[3 * (size_t)i] = pr[i].x;
-            position[3 * (size_t)i + 1] = pr[i].y;
-            position[3 * (size_t)i + 2] = pr[i].z;
+    // unpacked on the device into one scratch block, then copied straight into the caller's arrays
+    float *dev[4] = {nullptr, nullptr, nullptr, nullptr};
+    uint32_t *dids = nullptr;
+    float *host[4] = {position, velocity, radius, thickness_nm};
+    const size_t len[4] = {3 * (size_t)n, 3 * (size_t)n, n, n};
+    size_t total = ids ? n : 0;
+    for (int k = 0; k < 4; ++k) total += host[k] ? len[k] : 0;
+    if (total == 0) return SBS_OK;
+    char *base = nullptr;
+    SBS_CUDA_TRY(scratch_alloc((void **)&base, sizeof(float) * total + 64, s->stream));
+    size_t o = 0;
+    for (int k = 0; k < 4; ++k)
+        if (host[k]) {
+            dev[k] = (float *)base + o;
+            o += len[k];
         }
-        if (velocity) {
-            velocity[3 * (size_t)i] = vt[i].x;
-            velocity[3 * (size_t)i + 1] = vt[i].y;
-            velocity[3 * (size_t)i + 2] = vt[i].z;
-        }
-        if (radius) radius[i] = pr[i].w;
-        if (thickness_nm) thickness_nm[i] = vt[i].w;
-        if (ids) ids[i] = id[i];
-    }
+    if (ids) dids = (uint32_t *)((float *)base + o);
+    unpack_kernel<<<blocks(n), kThreads, 0, s->stream>>>(n, s->b.pr[c], s->b.vt[c], s->b.id[c], dev[0], dev[1], dev[2],
+                                                         dev[3], dids);
+    cudaError_t e = cudaGetLastError();
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k)
+        if (host[k]) e = cudaMemcpyAsync(host[k], dev[k], sizeof(float) * len[k], cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess && ids) e = cudaMemcpyAsync(ids, dids, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s->stream);
+    cudaFreeAsync(base, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return set_error(SBS_E_CUDA, "foam get_state: %s", cudaGetErrorString(e));
     return SBS_OK;
 }
 

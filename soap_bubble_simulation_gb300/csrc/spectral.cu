@@ -15,7 +15,8 @@
 //
 // Spectrum generation: sin(phase/2) with phase = 2 pi opd/lambda + pi equals cos(pi y), y =
 // opd/lambda; cos^2 has period 1 in y, so y is reduced exactly to u = y - rint(y) in [-1/2, 1/2]
-// and cos(pi u) is the Taylor series of cos up to u^14 (truncation < 1e-8 on that interval),
+// and cos(pi u) is the Taylor series of cos up to u^14 (truncation < 1e-8 on that interval; FP32
+// mode) or up to u^8 (< 2.6e-5; the BF16 tensor-core mode, whose spectra are rounded to BF16),
 // evaluated two wavelengths at a time with packed FP32 instructions.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -60,11 +61,24 @@ __device__ __forceinline__ float2 cos_pi_u2(float2 v) {
     return c;
 }
 
-// Airy reflectance F s^2 / (1 + F s^2) at two wavelengths (interference_lut.rs:123-133).
+// The same series to u^8 (k = 0..4; truncation below 2.6e-5 for |u| <= 1/2): enough for spectra
+// that are rounded to BF16 (relative step 3.9e-3) for the tensor-core contraction.
+__device__ __forceinline__ float2 cos_pi_u2_short(float2 v) {
+    float2 c = f2(0.23533063035889312f);
+    c = fma2(c, v, f2(-1.3352627688545893f));
+    c = fma2(c, v, f2(4.058712126416768f));
+    c = fma2(c, v, f2(-4.934802200544679f));
+    c = fma2(c, v, f2(1.0f));
+    return c;
+}
+
+// Airy reflectance F s^2 / (1 + F s^2) at two wavelengths (interference_lut.rs:123-133); SHORT:
+// the u^8 cosine series (BF16 spectra).
+template <bool SHORT = false>
 __device__ __forceinline__ float2 airy2(float opd, float F, float il0, float il1) {
     const float2 y = mul2(f2(opd), make_float2(il0, il1));
     const float2 u = sub2(y, make_float2(rintf(y.x), rintf(y.y)));
-    const float2 c = cos_pi_u2(mul2(u, u));
+    const float2 c = SHORT ? cos_pi_u2_short(mul2(u, u)) : cos_pi_u2(mul2(u, u));
     const float2 fs = mul2(f2(F), mul2(c, c));
     const float2 den = add2(f2(1.0f), fs);
     return make_float2(__fdividef(fs.x, den.x), __fdividef(fs.y, den.y));
@@ -132,9 +146,11 @@ __device__ __forceinline__ void write_spectrum_row(uint8_t *sA, int row, float o
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int l = k8 + 2 * j;
-            float2 v = airy2(opd, F, c.invl[l], c.invl[l + 1]);
-            if (l >= c.nl) v.x = 0.f;
-            if (l + 1 >= c.nl) v.y = 0.f;
+            float2 v = make_float2(0.f, 0.f);  // padding beyond nl: zeros, not evaluated
+            if (l < c.nl) {
+                v = airy2<true>(opd, F, c.invl[l], c.invl[l + 1]);
+                if (l + 1 >= c.nl) v.y = 0.f;
+            }
             __nv_bfloat162 b2 = __floats2bfloat162_rn(v.x, v.y);
             w[j] = *reinterpret_cast<uint32_t *>(&b2);
         }
