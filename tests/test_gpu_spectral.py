@@ -67,3 +67,22 @@ def test_spectral_rejects_bad_arguments(sbs):
 
     with pytest.raises(sbs.SbsError, match="nl"):
         sbs.spectral_rgb(t, c, nf, wl129, S.spectral_cmf(wl129))
+
+
+def test_spectral_thick_films_take_the_exact_rounding(sbs, orc):
+    """Points whose phase opd / lambda reaches 2^22 (films thicker than ~0.5 m) leave the packed
+    rounding of the phase for rintf; thin points of the same call keep their accuracy, and the thick
+    ones give finite reflectances in [0, 1] weighted by the CMF (their f32 phase is coarser than a
+    period, so no oracle comparison applies)."""
+    t, c, nf, wl, cmf = workload(4096, seed=9)
+    thick = np.arange(0, 4096, 7)
+    t = t.copy()
+    t[thick] = np.float32(2e9)
+    thin = np.setdiff1d(np.arange(4096), thick)
+    want = orc.spectral_rgb(t[thin], c[thin], nf[thin], wl, cmf)
+    cap = cmf.clip(min=0).sum(axis=0)
+    for mode, tol in (("fp32", 1e-4), ("tc", 1e-2)):
+        got = sbs.spectral_rgb(t, c, nf, wl, cmf, mode=mode)
+        assert rel_linf(got[thin], want) <= tol, mode
+        g = got[thick]
+        assert np.isfinite(g).all() and (g >= -1e-3).all() and (g <= cap * 1.01 + 1e-3).all(), mode
