@@ -21,7 +21,6 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
-#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -45,7 +44,6 @@ struct BTile {
 
 struct SpecConsts {
     float invl[kMaxLambda];     // 1 / lambda (nm^-1), zero beyond nl
-    float invl_max;             // the largest |1 / lambda|
     float cmf[kMaxLambda][3];   // FP32 colour-matching weights (FP32 mode)
     int nl;
 };
@@ -75,15 +73,11 @@ __device__ __forceinline__ float2 cos_pi_u2_short(float2 v) {
 }
 
 // Airy reflectance F s^2 / (1 + F s^2) at two wavelengths (interference_lut.rs:123-133); SHORT:
-// the u^8 cosine series (BF16 spectra). SMALL: |y| < 2^22 for both wavelengths, where rint(y) is
-// (y + 1.5 2^23) - 1.5 2^23 (the add rounds to the nearest even integer), two packed FP32
-// operations instead of two FRNDs; the same values as rintf.
-template <bool SHORT = false, bool SMALL = false>
+// the u^8 cosine series (BF16 spectra).
+template <bool SHORT = false>
 __device__ __forceinline__ float2 airy2(float opd, float F, float il0, float il1) {
     const float2 y = mul2(f2(opd), make_float2(il0, il1));
-    const float2 r = SMALL ? sub2(add2(y, f2(12582912.0f)), f2(12582912.0f))
-                           : make_float2(rintf(y.x), rintf(y.y));
-    const float2 u = sub2(y, r);
+    const float2 u = sub2(y, make_float2(rintf(y.x), rintf(y.y)));
     const float2 c = SHORT ? cos_pi_u2_short(mul2(u, u)) : cos_pi_u2(mul2(u, u));
     const float2 fs = mul2(f2(F), mul2(c, c));
     const float2 den = add2(f2(1.0f), fs);
@@ -143,8 +137,8 @@ __device__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
 }
 
 // Writes one point's spectrum (row `row` of an A tile) as KPAD BF16 values.
-template <int KPAD, bool SMALL>
-__device__ __forceinline__ void write_spectrum_row_t(uint8_t *sA, int row, float opd, float F, const SpecConsts &c) {
+template <int KPAD>
+__device__ __forceinline__ void write_spectrum_row(uint8_t *sA, int row, float opd, float F, const SpecConsts &c) {
     constexpr uint32_t SBO = (KPAD / 8) * 128;
 #pragma unroll
     for (int k8 = 0; k8 < KPAD; k8 += 8) {
@@ -154,7 +148,7 @@ __device__ __forceinline__ void write_spectrum_row_t(uint8_t *sA, int row, float
             const int l = k8 + 2 * j;
             float2 v = make_float2(0.f, 0.f);  // padding beyond nl: zeros, not evaluated
             if (l < c.nl) {
-                v = airy2<true, SMALL>(opd, F, c.invl[l], c.invl[l + 1]);
+                v = airy2<true>(opd, F, c.invl[l], c.invl[l + 1]);
                 if (l + 1 >= c.nl) v.y = 0.f;
             }
             __nv_bfloat162 b2 = __floats2bfloat162_rn(v.x, v.y);
@@ -162,19 +156,6 @@ __device__ __forceinline__ void write_spectrum_row_t(uint8_t *sA, int row, float
         }
         *reinterpret_cast<uint4 *>(sA + tile_off(row, k8, SBO)) = make_uint4(w[0], w[1], w[2], w[3]);
     }
-}
-
-// |opd / lambda| < 2^22 at every wavelength (films thinner than ~0.5 m): the packed rounding.
-__device__ __forceinline__ bool small_phase(float opd, const SpecConsts &c) {
-    return fabsf(opd) * c.invl_max < 4194304.0f;
-}
-
-template <int KPAD>
-__device__ __forceinline__ void write_spectrum_row(uint8_t *sA, int row, float opd, float F, const SpecConsts &c) {
-    if (small_phase(opd, c))
-        write_spectrum_row_t<KPAD, true>(sA, row, opd, F, c);
-    else
-        write_spectrum_row_t<KPAD, false>(sA, row, opd, F, c);
 }
 
 // With NBUF = 2 tiles are double-buffered: while the tensor core contracts tile i (A buffer i % 2
@@ -298,25 +279,6 @@ __global__ void __launch_bounds__(kTileM) spectral_tc_kernel(const float *__rest
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmem));
 }
 
-// The FP32 contraction of one point's spectrum.
-template <int KPAD, bool SMALL>
-__device__ __forceinline__ void fp32_spectrum(float opd, float F, const SpecConsts &c, float &r, float &g, float &b) {
-#pragma unroll
-    for (int l = 0; l < KPAD; l += 2) {
-        if (l < c.nl) {
-            const float2 v = airy2<false, SMALL>(opd, F, c.invl[l], c.invl[l + 1]);
-            r = fmaf(v.x, c.cmf[l][0], r);
-            g = fmaf(v.x, c.cmf[l][1], g);
-            b = fmaf(v.x, c.cmf[l][2], b);
-            if (l + 1 < c.nl) {
-                r = fmaf(v.y, c.cmf[l + 1][0], r);
-                g = fmaf(v.y, c.cmf[l + 1][1], g);
-                b = fmaf(v.y, c.cmf[l + 1][2], b);
-            }
-        }
-    }
-}
-
 template <int KPAD>
 __global__ void __launch_bounds__(128) spectral_fp32_kernel(const float *__restrict__ t_nm,
                                                            const float *__restrict__ cos_i,
@@ -327,10 +289,20 @@ __global__ void __launch_bounds__(128) spectral_fp32_kernel(const float *__restr
     float F, opd;
     point_setup(t_nm[p], cos_i[p], n_film[p], F, opd);
     float r = 0.f, g = 0.f, b = 0.f;
-    if (small_phase(opd, c))
-        fp32_spectrum<KPAD, true>(opd, F, c, r, g, b);
-    else
-        fp32_spectrum<KPAD, false>(opd, F, c, r, g, b);
+#pragma unroll
+    for (int l = 0; l < KPAD; l += 2) {
+        if (l < c.nl) {
+            const float2 v = airy2(opd, F, c.invl[l], c.invl[l + 1]);
+            r = fmaf(v.x, c.cmf[l][0], r);
+            g = fmaf(v.x, c.cmf[l][1], g);
+            b = fmaf(v.x, c.cmf[l][2], b);
+            if (l + 1 < c.nl) {
+                r = fmaf(v.y, c.cmf[l + 1][0], r);
+                g = fmaf(v.y, c.cmf[l + 1][1], g);
+                b = fmaf(v.y, c.cmf[l + 1][2], b);
+            }
+        }
+    }
     rgb[3 * p] = r;
     rgb[3 * p + 1] = g;
     rgb[3 * p + 2] = b;
@@ -389,7 +361,6 @@ extern "C" int sbs_spectral_rgb(const float *t_nm, const float *cos_i, const flo
     for (uint32_t l = 0; l < nl; ++l) {
         SBS_CHECK_ARG(wl_nm[l] > 0.f, "wavelengths must be positive");
         c.invl[l] = 1.0f / wl_nm[l];
-        c.invl_max = std::max(c.invl_max, c.invl[l]);
         for (int ch = 0; ch < 3; ++ch) c.cmf[l][ch] = cmf[3 * l + ch];
     }
     const int kpad = nl <= 32 ? 32 : (nl <= 64 ? 64 : (nl <= 96 ? 96 : 128));

@@ -69,11 +69,11 @@ def test_spectral_rejects_bad_arguments(sbs):
         sbs.spectral_rgb(t, c, nf, wl129, S.spectral_cmf(wl129))
 
 
-def test_spectral_thick_films_take_the_exact_rounding(sbs, orc):
-    """Points whose phase opd / lambda reaches 2^22 (films thicker than ~0.5 m) leave the packed
-    rounding of the phase for rintf; thin points of the same call keep their accuracy, and the thick
-    ones give finite reflectances in [0, 1] weighted by the CMF (their f32 phase is coarser than a
-    period, so no oracle comparison applies)."""
+def test_spectral_very_thick_films(sbs, orc):
+    """Points whose phase opd / lambda reaches 2^22 (films thicker than ~0.5 m) next to ordinary
+    ones: the thin points keep their accuracy, and the thick ones give finite reflectances in
+    [0, 1] weighted by the CMF (their f32 phase is coarser than a period, so no oracle comparison
+    applies)."""
     t, c, nf, wl, cmf = workload(4096, seed=9)
     thick = np.arange(0, 4096, 7)
     t = t.copy()
