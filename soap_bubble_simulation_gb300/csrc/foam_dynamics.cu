@@ -581,18 +581,29 @@ struct DynArgs {
 
 // compute_forces + the integration of step (foam_dynamics.rs:62-94, 172-202); with force_out set,
 // only the forces of the current state.
+//
+// L lanes per bubble (L = 1 for large foams, where one thread per bubble already fills the GPU;
+// 4 or 16 for small ones, which would otherwise leave most SMs idle): the lanes evaluate the pair
+// forces of L consecutive list entries at once, then every lane of the group adds the L results
+// into the sum one by one in list order (shuffles), the buoyancy before the first j > k: the
+// reference's sums, the same on every lane; the group's first lane writes.
+template <int L>
 __global__ void __launch_bounds__(kThreads, 5) forces_kernel(DynArgs a) {
     Ctl *c = a.ctl;
     if (c->fault != kFaultNone) return;
     const uint32_t n = c->n[a.npar];
-    const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t0 == 0 && !a.force_out) {
+    const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t t0 = gtid / L;
+    const int sub = (int)(gtid % L);
+    const int lane0 = (int)(threadIdx.x & 31) - sub;
+    const unsigned gmask = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << lane0);
+    if (gtid == 0 && !a.force_out) {
         c->steps_done += 1;
         c->nconn = 0;
         c->coal_key = kNoPair;
         c->merged_a = c->merged_b = kNone;
     }
-    if (t0 >= n) return;
+    if (t0 >= n) return;  // the whole group: t0 is the group's
     const uint32_t k = a.perm[t0];
     const Phys &P = a.P;
     const float4 me = a.pr_in[k];
@@ -617,27 +628,58 @@ __global__ void __launch_bounds__(kThreads, 5) forces_kernel(DynArgs a) {
         by = ny * net;
         bz = nz * net;
     }
-    // one loop over the sorted list (no divergence between the two halves): entries t < split
-    // are j < k, whose pair force is evaluated with j first and enters negated; the buoyancy
-    // enters before the first j > k; the next entry's position is fetched one iteration ahead
+    // entries t < split are j < k, whose pair force is evaluated with j first and enters negated;
+    // the buoyancy enters before the first j > k
     float fx = 0.0f, fy = 0.0f, fz = 0.0f;
     const uint32_t m = a.cnt[k], split = a.split[k];
     const uint32_t *col = a.nbr + a.goff[t0 >> 5] + (t0 & 31);
-    float4 next = m ? a.pr_in[__ldg(col)] : me;
-    for (uint32_t t = 0; t < m; ++t) {
-        const float4 o = next;
-        if (t + 1 < m) next = a.pr_in[__ldg(col + (size_t)(t + 1) * 32)];
-        if (t == split) {
-            fx = fx + bx;
-            fy = fy + by;
-            fz = fz + bz;
+    if constexpr (L == 1) {
+        // one loop over the sorted list; the next entry's position fetched one iteration ahead
+        float4 next = m ? a.pr_in[__ldg(col)] : me;
+        for (uint32_t t = 0; t < m; ++t) {
+            const float4 o = next;
+            if (t + 1 < m) next = a.pr_in[__ldg(col + (size_t)(t + 1) * 32)];
+            if (t == split) {
+                fx = fx + bx;
+                fy = fy + by;
+                fz = fz + bz;
+            }
+            const bool lower = t < split;
+            float gx, gy, gz;
+            pair_force(P, lower ? o : me, lower ? me : o, gx, gy, gz);
+            fx = fx + (lower ? -gx : gx);
+            fy = fy + (lower ? -gy : gy);
+            fz = fz + (lower ? -gz : gz);
         }
-        const bool lower = t < split;
-        float gx, gy, gz;
-        pair_force(P, lower ? o : me, lower ? me : o, gx, gy, gz);
-        fx = fx + (lower ? -gx : gx);
-        fy = fy + (lower ? -gy : gy);
-        fz = fz + (lower ? -gz : gz);
+    } else {
+        for (uint32_t base = 0; base < m; base += L) {
+            const uint32_t t = base + sub;
+            float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+            if (t < m) {
+                const float4 o = a.pr_in[__ldg(col + (size_t)t * 32)];
+                const bool lower = t < split;
+                pair_force(P, lower ? o : me, lower ? me : o, gx, gy, gz);
+            }
+            const uint32_t cnt = min((uint32_t)L, m - base);  // the same on every lane of the group
+#pragma unroll
+            for (int jj = 0; jj < L; ++jj) {
+                const float hx = __shfl_sync(gmask, gx, lane0 + jj);
+                const float hy = __shfl_sync(gmask, gy, lane0 + jj);
+                const float hz = __shfl_sync(gmask, gz, lane0 + jj);
+                if ((uint32_t)jj < cnt) {
+                    const uint32_t tt = base + jj;
+                    if (tt == split) {
+                        fx = fx + bx;
+                        fy = fy + by;
+                        fz = fz + bz;
+                    }
+                    const bool lower = tt < split;
+                    fx = fx + (lower ? -hx : hx);
+                    fy = fy + (lower ? -hy : hy);
+                    fz = fz + (lower ? -hz : hz);
+                }
+            }
+        }
     }
     if (split == m) {
         fx = fx + bx;
@@ -649,6 +691,7 @@ __global__ void __launch_bounds__(kThreads, 5) forces_kernel(DynArgs a) {
     fx = fx + (-mv.x) * drag_coeff;
     fy = fy + (-mv.y) * drag_coeff;
     fz = fz + (-mv.z) * drag_coeff;
+    if (sub != 0) return;
     if (a.force_out) {
         a.force_out[3 * (size_t)k] = fx;
         a.force_out[3 * (size_t)k + 1] = fy;
@@ -1032,6 +1075,17 @@ DynArgs dyn_args(sbs_foam_sim *s, float dt, int in, int out) {
     return a;
 }
 
+// Lanes per bubble of the force pass: enough threads to fill the GPU's SMs for small foams.
+void launch_forces(sbs_foam_sim *s, const DynArgs &a) {
+    const uint32_t n = s->n_cap;
+    if (n >= 131072)
+        forces_kernel<1><<<blocks(n), kThreads, 0, s->stream>>>(a);
+    else if (n >= 32768)
+        forces_kernel<4><<<blocks((size_t)n * 4), kThreads, 0, s->stream>>>(a);
+    else
+        forces_kernel<16><<<blocks((size_t)n * 16), kThreads, 0, s->stream>>>(a);
+}
+
 void free_list(sbs_foam_sim *s) {
     cudaFree(s->nbr);
     cudaFree(s->cflag);
@@ -1244,7 +1298,7 @@ int sbs_foam_sim_step(sbs_foam_sim *s, float dt, uint32_t steps) {
         for (uint32_t k = done; k < steps; ++k) {
             enqueue_list(s, false, skin);
             DynArgs a = dyn_args(s, dt, s->cur, s->cur ^ 1);
-            forces_kernel<<<blocks(s->n_cap), kThreads, 0, s->stream>>>(a);
+            launch_forces(s, a);
             if (coal || k + 1 == steps) connections_kernel<<<blocks(s->n_cap), kThreads, 0, s->stream>>>(a);
             s->conn_buf = s->cur ^ 1;
             s->conn_npar = s->npar;
@@ -1431,7 +1485,7 @@ int sbs_foam_sim_forces(sbs_foam_sim *s, float *forces, int mem) {
     if (mem == SBS_MEM_HOST) SBS_CUDA_TRY(scratch_alloc((void **)&dout, sizeof(float) * 3 * n, s->stream));
     DynArgs a = dyn_args(s, 0.0f, s->cur, s->cur ^ 1);
     a.force_out = dout;
-    forces_kernel<<<blocks(s->n_cap), kThreads, 0, s->stream>>>(a);
+    launch_forces(s, a);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && mem == SBS_MEM_HOST)
         e = cudaMemcpyAsync(forces, dout, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, s->stream);
