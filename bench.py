@@ -488,15 +488,15 @@ def branched_section(sbs, synthetic, torch):
 def foam_dynamics_section(sbs, cpu_seconds: float):
     """Foam cluster dynamics (FoamSimulator::step): a face-centred cubic foam of 1,048,576 bubbles
     (FoamGenerator::generate_fcc's layout, spacing 5 cm, radii 1.5-3 cm, jitter 0.1, seeded),
-    dt = 1 ms, 40 steps timed in one call (the neighbour list is rebuilt about every 40 steps, so
-    the rebuilds are included at their rate); e2e adds the per-frame read-back of every bubble's
+    dt = 1 ms, 200 steps timed in one call (the neighbour list is rebuilt about every 70 steps at
+    this dt, so the rebuilds are included at their rate); e2e adds the per-frame read-back of every bubble's
     position, velocity, radius and thickness. The same at 4,096 bubbles next to the oracle's
     restatement of the reference's all-pairs loops on one host core (the reference is
     single-threaded), timed on a bounded number of steps."""
     from soap_bubble_simulation_gb300 import foam_dynamics as fd
 
     out = {}
-    for n, k in ((1_048_576, 40), (4096, 200)):
+    for n, k in ((1_048_576, 200), (4096, 1000)):
         pos, rad = fd.fcc_foam(n, seed=0)
         sim = fd.FoamSimulator(pos, rad)
         sim.step(1e-3, 3)
