@@ -158,3 +158,21 @@ def test_fcc_layout(fd):
     np.testing.assert_allclose(pos[0], [-(n - 1) * 0.05 / 2] * 3, atol=1e-7)
     np.testing.assert_allclose(pos[1] - pos[0], [0.025, 0.025, 0.0], atol=1e-7)
     assert len({tuple(np.round(q, 6)) for q in pos}) == 500
+
+
+def test_no_gpu_is_an_error_not_a_fallback(fd):
+    """Without a GPU the simulator refuses to start (no CPU path); bad arguments are rejected
+    before the device is looked at."""
+    import ctypes
+
+    from soap_bubble_simulation_gb300 import _native as N
+
+    with pytest.raises(N.SbsError) as bad:
+        fd.FoamSimulator([[0.0, 0.0, 0.0]], [-1.0])
+    assert bad.value.code == N.SBS_E_INVALID
+    n = ctypes.c_int(-1)
+    if N.lib().sbs_device_count(ctypes.byref(n)) == 0 and n.value > 0:
+        pytest.skip("a GPU is visible here")
+    with pytest.raises(N.SbsError) as e:
+        fd.FoamSimulator([[0.0, 0.0, 0.0]], [0.01])
+    assert e.value.code == N.SBS_E_CUDA
