@@ -136,6 +136,14 @@ class FoamSimulator:
             N.call("sbs_foam_sim_connections", self._h, C.c_void_p(out.ctypes.data), count.value, C.byref(count))
         return out
 
+    def query_nearby(self, position, radius: float) -> list:
+        """BubbleCluster::query_nearby (foam.rs:314-317) over the cluster's 10 cm spatial hash as
+        update_connections last rebuilt it (the current bubbles in cluster order)."""
+        b = self.bubbles()
+        h = SpatialHash(0.1)
+        h.rebuild(b["ids"], b["position"])
+        return h.query(position, radius)
+
     def couple_thickness(self, batch) -> None:
         """thickness_nm[i] = the sin(theta)-weighted mean of batch bubble i's thickness field, in nm."""
         N.call("sbs_foam_sim_couple_thickness", self._h, batch._h)
@@ -143,6 +151,42 @@ class FoamSimulator:
     @property
     def handle(self) -> C.c_void_p:
         return self._h
+
+
+class SpatialHash:
+    """SpatialHash (foam.rs:149-216): bubble ids binned by floor(position / cell_size) in f32;
+    query returns the ids of the cells within ceil(radius / cell_size) cells of the position's,
+    offsets walked x, then y, then z, each cell in insertion order. A host-side helper: the
+    GPU's own spatial hash lives inside the neighbour-list build."""
+
+    def __init__(self, cell_size: float):
+        self.cell_size = np.float32(cell_size)
+        self.cells: dict[tuple, list] = {}
+
+    def cell_coords(self, position) -> tuple:
+        p = np.asarray(position, dtype=np.float32).reshape(3)
+        return tuple(int(np.floor(p[k] / self.cell_size)) for k in range(3))
+
+    def clear(self) -> None:
+        self.cells.clear()
+
+    def insert(self, bubble_id: int, position) -> None:
+        self.cells.setdefault(self.cell_coords(position), []).append(int(bubble_id))
+
+    def query(self, position, radius: float) -> list:
+        r = int(np.ceil(np.float32(radius) / self.cell_size))
+        cx, cy, cz = self.cell_coords(position)
+        out = []
+        for dx in range(-r, r + 1):
+            for dy in range(-r, r + 1):
+                for dz in range(-r, r + 1):
+                    out.extend(self.cells.get((cx + dx, cy + dy, cz + dz), ()))
+        return out
+
+    def rebuild(self, ids, positions) -> None:
+        self.clear()
+        for i, p in zip(ids, np.asarray(positions, dtype=np.float32).reshape(-1, 3)):
+            self.insert(i, p)
 
 
 def fcc_foam(count: int, spacing: float = 0.05, jitter: float = 0.1, min_radius: float = 0.015,

@@ -176,3 +176,17 @@ def test_no_gpu_is_an_error_not_a_fallback(fd):
     with pytest.raises(N.SbsError) as e:
         fd.FoamSimulator([[0.0, 0.0, 0.0]], [0.01])
     assert e.value.code == N.SBS_E_CUDA
+
+
+def test_reference_spatial_hash(fd):
+    """foam.rs:470-480 (test_spatial_hash), and the query order of SpatialHash::query."""
+    h = fd.SpatialHash(1.0)
+    h.insert(0, [0.0, 0.0, 0.0])
+    h.insert(1, [0.5, 0.0, 0.0])
+    h.insert(2, [5.0, 0.0, 0.0])
+    near = h.query([0.0, 0.0, 0.0], 1.0)
+    assert 0 in near and 1 in near and 2 not in near
+    h.insert(3, [-0.5, -0.5, -0.5])  # cell (-1, -1, -1): the first offset walked
+    assert h.query([0.0, 0.0, 0.0], 1.0) == [3, 0, 1]
+    h.rebuild([7, 8], [[0.2, 0.2, 0.2], [3.0, 3.0, 3.0]])
+    assert h.query([0.0, 0.0, 0.0], 0.5) == [7]
