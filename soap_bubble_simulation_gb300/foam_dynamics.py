@@ -72,6 +72,14 @@ class FoamSimulator:
             N.lib().sbs_foam_sim_destroy(self._h)
             self._h = C.c_void_p()
 
+    def reset(self) -> None:
+        """FoamSimulator::reset (foam_dynamics.rs:274-276): the default cluster again, physics kept."""
+        self.close()
+        pos, rad = default_cluster()
+        self._h = C.c_void_p()
+        N.call("sbs_foam_sim_create", pos.shape[0], N.ptr(pos), N.ptr(rad), None,
+               C.cast(C.byref(self.physics), C.c_void_p), C.byref(self._h))
+
     def __del__(self):
         try:
             self.close()

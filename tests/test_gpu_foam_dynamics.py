@@ -51,6 +51,9 @@ def test_default_cluster_reference_tests(fd, orc):
     for k in range(11):  # test_connections_after_physics_step (foam.rs:512-531)
         sim.step(0.016)
     _same_state(sim, orc.foam_step(sim.physics, 0.016, 11, pos, rad))
+    sim.reset()  # FoamSimulator::reset: the default cluster again
+    np.testing.assert_array_equal(sim.bubbles()["position"], pos)
+    assert sim.query_nearby([0.0, 0.0, 0.0], 0.1) == [2, 4, 0, 1, 3]  # cells (-1,0,0), (0,-1,0), (0,0,0)
     # test_repulsion_separates_overlapping_bubbles (foam_dynamics.rs:348-367)
     s2 = fd.FoamSimulator([[0, 0, 0], [0.04, 0, 0]], [0.03, 0.03], physics=_phys(fd, gravity=[0.0, 0.0, 0.0]))
     s2.step(0.001, 100)
