@@ -78,6 +78,18 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(*vals):
+    """Each value's maximum over the ranks (one all-reduce over the process group; the values
+    themselves for a single process): the slowest replica's times set the whole-job rate."""
+    import torch
+
+    t = torch.tensor(vals, dtype=torch.float64)
+    dist = torch.distributed
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 def hbm_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -642,10 +654,7 @@ def main():
         barrier()
     total_ms = start_all.elapsed_time(end_all)
     kern_ms = sum(a.elapsed_time(b) for a, b in ev)
-    t = torch.tensor([total_ms, kern_ms], dtype=torch.float64)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    total_ms, kern_ms = float(t[0]), float(t[1])
+    total_ms, kern_ms = max_over_ranks(total_ms, kern_ms)
     value = world * cells * STEPS_PER_RUN * args.steps / (total_ms / 1e3)
     kb = ctypes.c_int()
     N.call("sbs_gpu_drainage_time_blocking", sim.handle, ctypes.byref(kb))
@@ -683,10 +692,7 @@ def main():
         e2e_once()
     barrier()
     e2e_s = time.perf_counter() - t0
-    if world > 1:
-        tt = torch.tensor([e2e_s], dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(tt[0])
+    (e2e_s,) = max_over_ranks(e2e_s)
     e2e_value = world * cells * STEPS_PER_RUN * e2e_steps / e2e_s
 
     # ---- the reference's CPU semantics on the GPU, for context (compensated f32x2) --------------
