@@ -420,29 +420,6 @@ __device__ __forceinline__ void warp_sort(uint32_t (&v)[R], int lane) {
     }
 }
 
-// Sorts buf[0..m) (m <= 32 R, padded with kNone) in registers and writes it to the column; returns
-// the number of entries below k.
-template <int R>
-__device__ __forceinline__ uint32_t sort_write(const uint32_t *buf, uint32_t m, uint32_t k, uint32_t *col, int lane) {
-    uint32_t v[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const uint32_t e = r * 32 + lane;
-        v[r] = e < m ? buf[e] : kNone;
-    }
-    warp_sort<R>(v, lane);
-    uint32_t below = 0;
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const uint32_t e = r * 32 + lane;
-        if (e < m) {
-            col[(size_t)e * 32] = v[r];
-            below += v[r] < k;
-        }
-    }
-    return below;
-}
-
 constexpr int kListWarps = 4;
 
 // Counts each bubble's candidates (a warp per bubble), and the bubbles of each count.
@@ -521,40 +498,78 @@ __global__ void list_gcap_kernel(ListArgs a) {
     if ((threadIdx.x & 31) == 0 && t < ((n + 31) & ~31u)) a.gcap[t >> 5] = m;
 }
 
-// A warp per bubble: collects the candidates again into shared memory, sorts them by index in
-// registers (bitonic; in shared memory beyond 1024) and writes the bubble's column and the length
-// of its lower part.
-__global__ void __launch_bounds__(kListWarps * 32, 4) list_fill_kernel(ListArgs a) {
-    __shared__ uint32_t s_buf[kListWarps][kMaxCand];
+// A warp per bubble: collects the candidates again, in the walk's order, straight into the bubble's
+// column (few registers: many warps hide the walk's load latency).
+__global__ void __launch_bounds__(kListWarps * 32) list_walk_kernel(ListArgs a) {
     __shared__ CellTable s_tab[kListWarps];
+    const Ctl *c = a.ctl;
+    if (!c->go || c->fault != kFaultNone) return;
+    const uint32_t n = c->n[a.npar];
+    const int lane = threadIdx.x & 31;
+    for (uint32_t k = blockIdx.x * kListWarps + (threadIdx.x >> 5); k < n; k += gridDim.x * kListWarps) {
+        const float4 p = a.pr[k];
+        const int4 q = a.cellc[k];
+        const uint32_t mk = a.cnt[k];  // the count pass's length: the same decisions, the same count
+        const uint32_t pos = a.inv[k];
+        uint32_t *col = a.nbr + a.goff[pos >> 5] + (pos & 31);
+        uint32_t m = 0;
+        walk(a, c, p, q, lane, s_tab[threadIdx.x >> 5], [&](uint32_t i, bool ok) {
+            const uint32_t bal = __ballot_sync(0xffffffffu, ok);
+            const uint32_t slot = m + __popc(bal & ((1u << lane) - 1u));
+            if (ok && slot < mk) col[(size_t)slot * 32] = a.bitems[i];
+            m += __popc(bal);
+        });
+    }
+}
+
+// Sorts the column's m entries in registers (element r * 32 + lane in v[r]) and writes them back;
+// returns the number of entries below k.
+template <int R>
+__device__ __forceinline__ uint32_t sort_column(uint32_t *col, uint32_t m, uint32_t k, int lane) {
+    uint32_t v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const uint32_t e = r * 32 + lane;
+        v[r] = e < m ? col[(size_t)e * 32] : kNone;
+    }
+    warp_sort<R>(v, lane);
+    uint32_t below = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const uint32_t e = r * 32 + lane;
+        if (e < m) {
+            col[(size_t)e * 32] = v[r];
+            below += v[r] < k;
+        }
+    }
+    return below;
+}
+
+// A warp per bubble: sorts its column by index in registers (bitonic; in shared memory beyond 1024
+// entries) and records the length of its lower part.
+__global__ void __launch_bounds__(kListWarps * 32, 4) list_sort_kernel(ListArgs a) {
+    __shared__ uint32_t s_buf[kListWarps][kMaxCand];
     const Ctl *c = a.ctl;
     if (!c->go || c->fault != kFaultNone) return;
     const uint32_t n = c->n[a.npar];
     const int lane = threadIdx.x & 31;
     uint32_t *buf = s_buf[threadIdx.x >> 5];
     for (uint32_t k = blockIdx.x * kListWarps + (threadIdx.x >> 5); k < n; k += gridDim.x * kListWarps) {
-        const float4 p = a.pr[k];
-        const int4 q = a.cellc[k];
-        const uint32_t mk = a.cnt[k];  // the count pass's length (<= kMaxCand: the pass faults above it)
-        uint32_t m = 0;
-        walk(a, c, p, q, lane, s_tab[threadIdx.x >> 5], [&](uint32_t i, bool ok) {
-            const uint32_t bal = __ballot_sync(0xffffffffu, ok);
-            const uint32_t slot = m + __popc(bal & ((1u << lane) - 1u));
-            if (ok && slot < mk) buf[slot] = a.bitems[i];
-            m += __popc(bal);
-        });
-        m = min(m, mk);  // equal: both passes make the same decisions
-        __syncwarp();
+        const uint32_t m = a.cnt[k];
         const uint32_t pos = a.inv[k];
         uint32_t *col = a.nbr + a.goff[pos >> 5] + (pos & 31);
         uint32_t below;
-        if (m <= 32) below = sort_write<1>(buf, m, k, col, lane);
-        else if (m <= 64) below = sort_write<2>(buf, m, k, col, lane);
-        else if (m <= 128) below = sort_write<4>(buf, m, k, col, lane);
-        else if (m <= 256) below = sort_write<8>(buf, m, k, col, lane);
-        else if (m <= 512) below = sort_write<16>(buf, m, k, col, lane);
-        else if (m <= 1024) below = sort_write<32>(buf, m, k, col, lane);
-        else below = sort_smem(buf, m, k, col, lane);
+        if (m <= 32) below = sort_column<1>(col, m, k, lane);
+        else if (m <= 64) below = sort_column<2>(col, m, k, lane);
+        else if (m <= 128) below = sort_column<4>(col, m, k, lane);
+        else if (m <= 256) below = sort_column<8>(col, m, k, lane);
+        else if (m <= 512) below = sort_column<16>(col, m, k, lane);
+        else if (m <= 1024) below = sort_column<32>(col, m, k, lane);
+        else {
+            for (uint32_t t = lane; t < m; t += 32) buf[t] = col[(size_t)t * 32];
+            __syncwarp();
+            below = sort_smem(buf, m, k, col, lane);
+        }
         for (int o = 16; o; o >>= 1) below += __shfl_xor_sync(0xffffffffu, below, o);
         if (lane == 0) a.split[k] = below;
         __syncwarp();
@@ -1048,7 +1063,8 @@ void enqueue_list(sbs_foam_sim *s, bool forced, float skin) {
     list_order_kernel<<<blocks(s->n_cap), kThreads, 0, s->stream>>>(a);
     list_gcap_kernel<<<blocks(s->n_cap), kThreads, 0, s->stream>>>(a);
     scan_kernel<<<1, 1024, 0, s->stream>>>(s->gcap, s->goff, 0, 1, a);
-    list_fill_kernel<<<s->list_blocks, kListWarps * 32, 0, s->stream>>>(a);
+    list_walk_kernel<<<s->list_blocks, kListWarps * 32, 0, s->stream>>>(a);
+    list_sort_kernel<<<s->list_blocks, kListWarps * 32, 0, s->stream>>>(a);
 }
 
 DynArgs dyn_args(sbs_foam_sim *s, float dt, int in, int out) {
