@@ -6,9 +6,10 @@
 // f_ij, force_buffer[j] += -f_ij), so bubble k receives, in this order: -f_jk for j < k
 // ascending, its buoyancy, f_kj for j > k ascending, its drag. A pair farther apart than
 // 3 (r_a + r_b) contributes exact zeros (no van der Waals, repulsion or adhesion term applies),
-// and adding a zero leaves a sum unchanged. So one thread per bubble that walks a neighbour
-// list sorted by bubble index, holding every pair that can come within that range, forms the
-// reference's f32 sums exactly, in O(n) instead of O(n^2).
+// and adding a zero leaves a sum unchanged. So a walk over a neighbour list sorted by bubble
+// index, holding every pair that can come within that range, forms the reference's f32 sums
+// exactly, in O(n) instead of O(n^2): one thread per bubble, or for small foams a few lanes that
+// evaluate consecutive entries together and add them in order.
 //
 // Neighbour list (Verlet list): bubble k lists every j with |p_j - p_k| < 3 (r_k + r_j) + skin at
 // the time of the build; it stays complete while no bubble has moved skin / 2 since (two bubbles
@@ -16,11 +17,11 @@
 // and flags a rebuild for the next one; merges flag one too. A rebuild bins the bubbles into a
 // spatial hash of cells (edge half of 6 r_max + skin, so the 5 x 5 x 5 cells around a bubble hold
 // all its candidates), counts each bubble's candidates (a warp per bubble), orders the bubbles by
-// descending count, collects the candidates again and sorts each list by index with a warp-wide
-// bitonic sort in registers. The lists of 32 bubbles at consecutive positions of that order are
-// interleaved (entry t of the bubble at position q at goff[q / 32] + 32 t + q % 32): one warp of
-// the force pass runs those 32 bubbles, reads their lists coalesced and, their lengths being
-// nearly equal, idles little.
+// descending count, collects the candidates again into each bubble's column and sorts each column
+// by index with a warp-wide bitonic sort in registers. The lists of 32 bubbles at consecutive
+// positions of that order are interleaved (entry t of the bubble at position q at
+// goff[q / 32] + 32 t + q % 32): the force pass reads them coalesced and, the lengths of
+// neighbouring positions being nearly equal, its lanes idle little.
 //
 // State: per bubble float4 (x, y, z, radius) and float4 (vx, vy, vz, thickness_nm) and the id,
 // double-buffered; the bubble count lives on the device (a merge changes it) and every kernel
@@ -971,7 +972,7 @@ struct sbs_foam_sim {
     uint32_t *bcount = nullptr, *bstart = nullptr, *bitems = nullptr, *bkey = nullptr, *brank = nullptr;
     float4 *spr = nullptr;
     unsigned long long *skey = nullptr;
-    int list_blocks = 1;  // grid of the count / fill passes (a few blocks per SM, grid-stride)
+    int list_blocks = 1;  // grid of the count / walk / sort passes (a few blocks per SM, grid-stride)
     uint32_t *cnt = nullptr, *split = nullptr, *gcap = nullptr, *goff = nullptr;
     uint32_t *perm = nullptr, *inv = nullptr, *mhist = nullptr, *mstart = nullptr;
     uint32_t *nbr = nullptr, *cflag = nullptr;
