@@ -74,11 +74,19 @@ class Camera:
         return np.asarray(self.target, dtype=np.float64) + np.array([x, y, z])
 
     def orbit(self, dx: float, dy: float) -> None:
+        """Camera::orbit (camera.rs:70-77): yaw and pitch by 0.01 per unit, pitch kept off the poles."""
         self.yaw += dx * 0.01
         self.pitch = min(max(self.pitch + dy * 0.01, -(math.pi / 2 - 0.01)), math.pi / 2 - 0.01)
 
-    def view_proj(self) -> np.ndarray:
-        """Column-major 4 x 4 (as CameraUniform.view_proj), float32, flattened."""
+    def zoom(self, delta: float) -> None:
+        """Camera::zoom (camera.rs:80-83): distance scaled by 1 - 0.1 delta, kept in [0.05, 10]."""
+        self.distance = min(max(self.distance * (1.0 - delta * 0.1), 0.05), 10.0)
+
+    def set_aspect(self, aspect: float) -> None:
+        self.aspect = aspect
+
+    def view_matrix(self) -> np.ndarray:
+        """Mat4::look_at_rh(position, target, +y) (camera.rs:91-94), row-major 4 x 4, float64."""
         eye = self.position()
         f = np.asarray(self.target, dtype=np.float64) - eye
         f /= np.linalg.norm(f)
@@ -88,11 +96,26 @@ class Camera:
         view = np.identity(4)
         view[0, :3], view[1, :3], view[2, :3] = s, u, -f
         view[:3, 3] = [-eye @ s, -eye @ u, eye @ f]
+        return view
+
+    def projection_matrix(self) -> np.ndarray:
+        """Mat4::perspective_rh (depth 0..1) (camera.rs:97-99), row-major 4 x 4, float64."""
         h = math.cos(0.5 * self.fov) / math.sin(0.5 * self.fov)
         r = self.far / (self.near - self.far)
         proj = np.zeros((4, 4))
         proj[0, 0], proj[1, 1], proj[2, 2], proj[3, 2], proj[2, 3] = h / self.aspect, h, r, -1.0, r * self.near
-        return (proj @ view).T.astype(np.float32).ravel()  # row-major of the transpose = column-major
+        return proj
+
+    def view_projection_matrix(self) -> np.ndarray:
+        return self.projection_matrix() @ self.view_matrix()
+
+    def view_proj(self) -> np.ndarray:
+        """Column-major 4 x 4 (as CameraUniform.view_proj), float32, flattened."""
+        return self.view_projection_matrix().T.astype(np.float32).ravel()  # row-major of the transpose
+
+    def uniform(self):
+        """Camera::uniform (camera.rs:107-114): (view_proj column-major [16] f32, camera_pos [3] f32)."""
+        return self.view_proj(), self.position().astype(np.float32)
 
 
 def _u8(a, shape):

@@ -180,3 +180,77 @@ def test_frame_background_and_centre(orc, shading):
     frac = hit.mean()
     r = math.tan(math.asin(0.025 / 0.2)) / math.tan(math.radians(22.5))
     assert abs(frac - math.pi * r * r / 4) < 0.02
+
+
+# --- the reference's camera.rs (:122-345) and BubbleUniform (pipeline.rs:2884-2955,
+# headless.rs:566-571) tests, on the host-side mirrors ---------------------------------------------
+def test_reference_camera(shading):
+    C = shading.Camera
+    cam = C(aspect=16 / 9)
+    assert cam.distance > 0 and cam.fov > 0  # test_camera_creation
+    cam = C(aspect=1.0)
+    assert abs(np.linalg.norm(cam.position()) - cam.distance) < 1e-3  # test_camera_position
+    for dx, sign in ((100.0, 1), (-100.0, -1)):  # test_orbit_increases_yaw / decreases
+        c = C(aspect=1.0)
+        y0 = c.yaw
+        c.orbit(dx, 0.0)
+        assert (c.yaw - y0) * sign > 0
+    c = C(aspect=1.0)
+    p0 = c.position()
+    c.orbit(50.0, 50.0)
+    assert np.linalg.norm(p0 - c.position()) > 1e-3  # test_orbit_changes_position
+    for dy in (10000.0, -10000.0):  # test_pitch_clamping_upper / lower
+        c = C(aspect=1.0)
+        c.orbit(0.0, dy)
+        assert abs(c.pitch) <= math.pi / 2 - 0.01 + 1e-12
+    for d, smaller in ((2.0, True), (-2.0, False)):  # test_zoom_in / out
+        c = C(aspect=1.0)
+        d0 = c.distance
+        c.zoom(d)
+        assert (c.distance < d0) == smaller
+    c = C(aspect=1.0)
+    c.zoom(1000.0)
+    assert c.distance >= 0.05  # test_zoom_min_bound
+    c.zoom(-1000.0)
+    assert c.distance <= 10.0  # test_zoom_max_bound
+    c = C(aspect=16 / 9)
+    c.set_aspect(4 / 3)
+    assert abs(c.aspect - 4 / 3) < 1e-3  # test_aspect_ratio_update
+    c = C(aspect=1.0)
+    assert abs(np.linalg.det(c.view_matrix())) > 1e-3  # test_view_matrix_is_valid
+    assert abs(np.linalg.det(c.projection_matrix())) > 1e-3  # test_projection_matrix_is_valid
+    c = C(aspect=1.0)  # test_input_sequence_simulation
+    p0 = c.position()
+    for _ in range(10):
+        c.orbit(10.0, 5.0)
+    c.zoom(2.0)
+    assert np.linalg.norm(p0 - c.position()) > 0.01
+    assert abs(np.linalg.norm(c.position() - np.asarray(c.target)) - c.distance) < 1e-3
+    c = C(aspect=1.0)  # test_orbit_360_degrees
+    p0 = c.position()
+    for _ in range(628):
+        c.orbit(1.0, 0.0)
+    assert np.linalg.norm(p0 - c.position()) < 0.1
+    c = C(aspect=1.0)  # test_camera_uniform_contents
+    vp, pos = c.uniform()
+    np.testing.assert_allclose(pos, c.position(), atol=1e-3)
+    np.testing.assert_allclose(vp.reshape(4, 4), c.view_projection_matrix().T, atol=1e-3)  # columns
+
+
+def test_reference_bubble_uniform(shading):
+    import ctypes
+
+    U = shading.BubbleUniform
+    u = U.default()  # test_bubble_uniform_default_values, headless.rs test_bubble_uniform_defaults
+    for name, want in (("refractive_index", 1.33), ("base_thickness_nm", 500.0), ("interference_intensity", 4.0),
+                       ("base_alpha", 0.3), ("edge_alpha", 0.6), ("film_time", 0.0), ("swirl_intensity", 1.0),
+                       ("drainage_speed", 0.5), ("pattern_scale", 1.0)):
+        assert abs(getattr(u, name) - want) < 1e-6, name
+    for name, v in (("film_time", 10.0), ("swirl_intensity", 2.0), ("drainage_speed", 0.5), ("pattern_scale", 3.0)):
+        setattr(u, name, v)  # test_bubble_uniform_film_dynamics_present
+        assert abs(getattr(u, name) - v) < 1e-6
+    assert ctypes.sizeof(U) == 128  # test_bubble_uniform_size_alignment
+    for name, off in (("refractive_index", 0), ("base_thickness_nm", 4), ("time", 8), ("interference_intensity", 12),
+                      ("base_alpha", 16), ("edge_alpha", 20), ("film_time", 36), ("swirl_intensity", 40),
+                      ("drainage_speed", 44), ("pattern_scale", 48)):  # test_bubble_uniform_field_offsets
+        assert getattr(U, name).offset == off, name
