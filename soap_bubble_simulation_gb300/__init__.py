@@ -20,7 +20,7 @@ from .surrogate import SURROGATE_STEPS, DrainageSurrogate, field_params, masked_
 from .shading import BubbleUniform, Camera, render_frame, shade_fragments
 from .caustics import CausticParams, caustic_map
 from .branched import BranchedFlowParams, BranchedFlowSimulator, branched_flow_step, generate_scatterers
-from .foam_dynamics import FoamPhysics, FoamSimulator, default_cluster, fcc_foam
+from .foam_dynamics import FoamPhysics, FoamSimulator, SpatialHash, default_cluster, fcc_foam
 
 __all__ = [
     "BubbleParameters", "ConfigError", "EnvironmentParameters", "FluidParameters", "SimulationConfig",
@@ -31,5 +31,5 @@ __all__ = [
     "wavelengths", "SbsError", "FoamDrainage", "SURROGATE_STEPS", "DrainageSurrogate", "field_params",
     "masked_error", "BubbleUniform", "Camera", "render_frame", "shade_fragments", "CausticParams", "caustic_map",
     "BranchedFlowParams", "BranchedFlowSimulator", "branched_flow_step", "generate_scatterers", "FoamPhysics",
-    "FoamSimulator", "default_cluster", "fcc_foam",
+    "FoamSimulator", "SpatialHash", "default_cluster", "fcc_foam",
 ]
