@@ -190,3 +190,36 @@ def test_reference_spatial_hash(fd):
     assert h.query([0.0, 0.0, 0.0], 1.0) == [3, 0, 1]
     h.rebuild([7, 8], [[0.2, 0.2, 0.2], [3.0, 3.0, 3.0]])
     assert h.query([0.0, 0.0, 0.0], 0.5) == [7]
+
+
+def test_argument_validation_before_device(fd):
+    """The C ABI rejects bad arguments with SBS_E_INVALID before it looks for a device."""
+    import ctypes
+
+    from soap_bubble_simulation_gb300 import _native as N
+
+    L = N.lib()
+    p = fd.FoamPhysics.default()
+    pp = ctypes.cast(ctypes.byref(p), ctypes.c_void_p)
+    pos = np.zeros((2, 3), np.float32)
+    rad = np.full(2, 0.01, np.float32)
+    h = ctypes.c_void_p()
+    assert L.sbs_foam_sim_create(0, N.ptr(pos), N.ptr(rad), None, pp, ctypes.byref(h)) == N.SBS_E_INVALID
+    assert L.sbs_foam_sim_create(2, None, N.ptr(rad), None, pp, ctypes.byref(h)) == N.SBS_E_INVALID
+    assert L.sbs_foam_sim_create(2, N.ptr(pos), N.ptr(rad), None, None, ctypes.byref(h)) == N.SBS_E_INVALID
+    bad = fd.FoamPhysics.default()
+    bad.damping = float("nan")
+    assert L.sbs_foam_sim_create(2, N.ptr(pos), N.ptr(rad), None, ctypes.cast(ctypes.byref(bad), ctypes.c_void_p),
+                                 ctypes.byref(h)) == N.SBS_E_INVALID
+    assert b"finite" in L.sbs_last_error()
+    thick = np.array([500.0, np.inf], np.float32)
+    assert L.sbs_foam_sim_create(2, N.ptr(pos), N.ptr(rad), N.ptr(thick), pp, ctypes.byref(h)) == N.SBS_E_INVALID
+    assert not h
+    for fn, args in (("sbs_foam_sim_step", (None, 1e-3, 1)), ("sbs_foam_sim_counts", (None, None, None)),
+                     ("sbs_foam_sim_forces", (None, None, N.MEM_HOST)),
+                     ("sbs_foam_sim_couple_thickness", (None, None))):
+        assert getattr(L, fn)(*args) == N.SBS_E_INVALID, fn
+    assert L.sbs_foam_sim_destroy(None) == 0
+    out = fd.FoamPhysics()
+    assert L.sbs_foam_physics_default(None) == N.SBS_E_INVALID
+    assert L.sbs_foam_physics_default(ctypes.cast(ctypes.byref(out), ctypes.c_void_p)) == 0
