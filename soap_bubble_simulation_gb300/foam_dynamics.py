@@ -87,8 +87,9 @@ class FoamSimulator:
             pass
 
     def set_physics(self, physics: FoamPhysics | None = None, **fields) -> None:
-        """Replaces the physics (or changes the named fields, e.g. coalescence_enabled=1)."""
-        p = self.physics if physics is None else physics
+        """Replaces the physics (or changes the named fields, e.g. coalescence_enabled=1); on an
+        error (a non-finite value) the simulator keeps its physics."""
+        p = FoamPhysics.from_buffer_copy(self.physics if physics is None else physics)
         for k, v in fields.items():
             if k == "gravity":
                 p.gravity[:] = [float(x) for x in v]

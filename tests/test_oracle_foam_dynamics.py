@@ -223,3 +223,16 @@ def test_argument_validation_before_device(fd):
     out = fd.FoamPhysics()
     assert L.sbs_foam_physics_default(None) == N.SBS_E_INVALID
     assert L.sbs_foam_physics_default(ctypes.cast(ctypes.byref(out), ctypes.c_void_p)) == 0
+
+
+def test_set_physics_keeps_the_old_values_on_error(fd):
+    """set_physics builds the new values on a copy: a rejected update leaves the simulator's physics
+    as they were (exercised here without a device through the library's argument check)."""
+    from soap_bubble_simulation_gb300 import _native as N
+
+    sim = fd.FoamSimulator.__new__(fd.FoamSimulator)  # no device: a handle-less simulator
+    sim.physics = fd.FoamPhysics.default()
+    sim._h = None
+    with pytest.raises(N.SbsError):
+        sim.set_physics(damping=float("nan"))
+    assert sim.physics.damping == np.float32(0.8)
