@@ -243,6 +243,15 @@ int sbs_gpu_drainage_set_marangoni_params(sbs_drainage *h, float gamma_air, floa
  * results are bit-identical either way. Default 4 where supported. */
 int sbs_gpu_drainage_set_time_blocking(sbs_drainage *h, int steps_per_launch);
 int sbs_gpu_drainage_time_blocking(const sbs_drainage *h, int *out);
+/* The same for a handle of either semantics (no reference counterpart). For the
+ * DrainageSimulator semantics 2..4 steps per launch advance the stencil, the
+ * pole-ring means and the marginal-regeneration fronts K steps at a time (each
+ * row strip one thread-block cluster spanning the ring); it needs an even
+ * resolution and at least 2 (K + 1) theta rows. Results are bit-identical to
+ * single steps. Default where supported: 2 for the compensated f32x2 storage,
+ * 4 for plain f32 (WGSL semantics: 4). */
+int sbs_drainage_set_time_blocking(sbs_drainage *h, int steps_per_launch);
+int sbs_drainage_time_blocking(const sbs_drainage *h, int *out);
 
 /* Public fields of GPUDrainageSimulator (gpu_drainage.rs:100-107). */
 int sbs_gpu_drainage_set_enabled(sbs_drainage *h, int enabled);

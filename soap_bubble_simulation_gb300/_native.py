@@ -165,6 +165,8 @@ SIGNATURES: dict[str, list] = {
     "sbs_gpu_drainage_set_marangoni_params": [_P, _F, _F, _F, _F],
     "sbs_gpu_drainage_set_time_blocking": [_P, _I],
     "sbs_gpu_drainage_time_blocking": [_P, _IP],
+    "sbs_drainage_set_time_blocking": [_P, _I],
+    "sbs_drainage_time_blocking": [_P, _IP],
     "sbs_gpu_drainage_set_enabled": [_P, _I],
     "sbs_gpu_drainage_set_time_scale": [_P, _F],
     "sbs_gpu_drainage_set_steps_per_frame": [_P, _U32],

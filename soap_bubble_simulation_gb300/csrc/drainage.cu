@@ -238,6 +238,13 @@ int allocate(sbs_drainage *h) {
         h->wtb_k = 4;
         h->wgeom = wtb_geometry(h->nt, h->np, h->wtb_k);
     }
+    if (h->sem == SBS_CPU_SEMANTICS) {
+        // steps per launch measured fastest at 2048 x 4096: 2 for the compensated storage (its
+        // register windows grow with K and cost warps), 4 for plain f32
+        const int k = h->x2 ? 2 : 4;
+        h->cgeom = wtbc_geometry(h->nt, h->np, k, h->x2);
+        if (h->cgeom.nby > 0) h->cpu_k = k;
+    }
     for (int i = 0; i < 2; ++i) {
         SBS_CUDA_TRY(cudaMalloc(&h->part[i], sizeof(double) * 4 * h->geom.nbx));
         SBS_CUDA_TRY(cudaMemset(h->part[i], 0, sizeof(double) * 4 * h->geom.nbx));
@@ -249,6 +256,11 @@ int allocate(sbs_drainage *h) {
     if (h->sem == SBS_WGSL_SEMANTICS && wtb_supported(h->nt, h->np))
         for (int k = 2; k <= 4; ++k) {
             const StepGeom g = wtb_geometry(h->nt, h->np, k);
+            vol_blocks = std::max(vol_blocks, (size_t)g.nbx * g.nby);
+        }
+    if (h->sem == SBS_CPU_SEMANTICS)
+        for (int k = 2; k <= 4; ++k) {
+            const StepGeom g = wtbc_geometry(h->nt, h->np, k, h->x2);
             vol_blocks = std::max(vol_blocks, (size_t)g.nbx * g.nby);
         }
     SBS_CUDA_TRY(cudaMalloc(&h->vol_partials, sizeof(double) * vol_blocks));
@@ -303,6 +315,54 @@ void release(sbs_drainage *h) {
 int enqueue_steps(sbs_drainage *h, int start, int count, float dt, bool vol_last, bool use_sched, bool last_single,
                   int *end) {
     const Consts &k = consts_of(h);
+    if (h->sem == SBS_CPU_SEMANTICS) {
+        // runs of cpu_k steps through the blocked kernel (pole rows materialised in memory
+        // before and after each launch), then the remainder as single steps whose pole rows
+        // after the first are the ring partials of the previous step
+        const int K = h->cpu_k > 1 ? h->cpu_k : 1;
+        const int groups = K > 1 ? count / K : 0;
+        const int singles = count - groups * K;
+        const int total = groups + singles;
+        int cur = start, step = 0;
+        for (int n = 0; n < total; ++n) {
+            const bool blocked = n < groups;
+            const int j = n - groups;  // index among the single steps
+            StepArgs a{};
+            a.hin = h->h[cur];
+            a.hout = h->h[cur ^ 1];
+            a.lin = h->hl[cur];
+            a.lout = h->hl[cur ^ 1];
+            a.rows = h->rows;
+            a.pin = h->part[(j + 1) & 1];
+            a.pout = h->part[j & 1];
+            a.tfe = use_sched ? h->sched_dev + step : nullptr;
+            a.vol_w = vol_last && n + 1 == total ? h->vol_w : nullptr;
+            a.vol_partials = h->vol_partials;
+            a.vol_counter = h->vol_counter;
+            a.vol_out = h->vol_out;
+            a.vol_index = h->vol_index;
+            a.nt = h->nt;
+            a.np = h->np;
+            a.pitch = (int)h->pitch;
+            a.rb = blocked ? h->cgeom.rb : h->geom.rb;
+            a.poles_virtual = !blocked && j > 0 ? 1 : 0;
+            a.crit = k.crit;
+            a.b = k.b;
+            a.DR2 = k.DR2;
+            a.dt = dt;
+            if (blocked)
+                SBS_CUDA_TRY(launch_wtbc(K, h->x2, a, h->cgeom, h->stream));
+            else
+                SBS_CUDA_TRY(launch_step(h->sem, h->x2, a, h->geom, h->stream));
+            step += blocked ? K : 1;
+            cur ^= 1;
+        }
+        if (singles > 0)
+            SBS_CUDA_TRY(launch_finalize_poles(h->h[cur], h->hl[cur], h->part[(singles - 1) & 1], h->geom.nbx, h->nt,
+                                               h->np, (int)h->pitch, h->stream));
+        *end = cur;
+        return SBS_OK;
+    }
     std::vector<int> plan;  // steps per launch
     if (h->sem == SBS_WGSL_SEMANTICS && h->wtb_k > 1) {
         int rem = count - (last_single && count > 0 ? 1 : 0);
@@ -362,6 +422,7 @@ int enqueue_steps(sbs_drainage *h, int start, int count, float dt, bool vol_last
 
 // Number of launches enqueue_steps uses for `count` steps (each flips the ping-pong buffers).
 int launches_in(const sbs_drainage *h, int count, bool last_single) {
+    if (h->sem == SBS_CPU_SEMANTICS) return h->cpu_k > 1 ? count / h->cpu_k + count % h->cpu_k : count;
     if (!(h->sem == SBS_WGSL_SEMANTICS && h->wtb_k > 1)) return count;
     const int tail = last_single && count > 0 ? 1 : 0;
     const int body = count - tail;
@@ -403,7 +464,8 @@ int run_chunk(sbs_drainage *h, int count, double dt, bool vol_last, bool last_si
         std::memcpy(&bits, &dtf, 4);
         std::string key = std::to_string(h->cur) + ":" + std::to_string(count) + ":" + std::to_string(vol_last) +
                           ":" + std::to_string(use_sched) + ":" + std::to_string(bits) + ":" +
-                          std::to_string(last_single) + ":" + std::to_string(h->wtb_k);
+                          std::to_string(last_single) + ":" + std::to_string(h->wtb_k) + ":" +
+                          std::to_string(h->cpu_k);
         auto it = h->graphs.find(key);
         cudaGraphExec_t exec = nullptr;
         if (it == h->graphs.end()) {
@@ -1004,6 +1066,34 @@ int sbs_gpu_drainage_time_blocking(const sbs_drainage *h, int *out) {
     CHECK_HANDLE(h);
     SBS_CHECK_ARG(out != nullptr, "out is null");
     *out = h->wtb_k > 1 ? h->wtb_k : 1;
+    return SBS_OK;
+}
+
+int sbs_drainage_set_time_blocking(sbs_drainage *h, int steps_per_launch) {
+    clear_error();
+    CHECK_HANDLE(h);
+    if (h->sem == SBS_WGSL_SEMANTICS) return sbs_gpu_drainage_set_time_blocking(h, steps_per_launch);
+    SBS_CHECK_ARG(steps_per_launch >= 0 && steps_per_launch <= 4, "steps_per_launch must be 0..4");
+    StepGeom g{};
+    if (steps_per_launch > 1) {
+        g = wtbc_geometry(h->nt, h->np, steps_per_launch, h->x2);
+        if (g.nby < 1)
+            return set_error(SBS_E_INVALID,
+                             "time blocking needs an even resolution and at least %d theta rows (grid %d x %d)",
+                             2 * (steps_per_launch + 1), h->nt, h->np);
+    }
+    SBS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    destroy_graphs(h);
+    h->cpu_k = steps_per_launch > 1 ? steps_per_launch : 0;
+    h->cgeom = g;
+    return SBS_OK;
+}
+
+int sbs_drainage_time_blocking(const sbs_drainage *h, int *out) {
+    CHECK_HANDLE(h);
+    SBS_CHECK_ARG(out != nullptr, "out is null");
+    if (h->sem == SBS_WGSL_SEMANTICS) return sbs_gpu_drainage_time_blocking(h, out);
+    *out = h->cpu_k > 1 ? h->cpu_k : 1;
     return SBS_OK;
 }
 

@@ -103,6 +103,11 @@ StepGeom step_geometry(int nt, int np, int semantics, int x2);
 bool wtb_supported(int nt, int np);
 StepGeom wtb_geometry(int nt, int np, int K);
 cudaError_t launch_wtb(int K, const StepArgs &a, const StepGeom &g, cudaStream_t s);
+// Temporally blocked CPU-semantics step (K = 2..4 steps per launch, pole means and fronts
+// included), drainage_wtb_cpu.cu. Each row strip is one cluster of nbx blocks of wx warps that
+// spans the ring; nby strips of at most rb rows. nby == 0: the grid is not supported.
+StepGeom wtbc_geometry(int nt, int np, int K, int x2);
+cudaError_t launch_wtbc(int K, int x2, const StepArgs &a, const StepGeom &g, cudaStream_t s);
 // x2: compensated f32x2 thickness (hi + lo words); CPU semantics only.
 cudaError_t launch_step(int semantics, int x2, const StepArgs &a, const StepGeom &g, cudaStream_t s);
 // Writes the pole rows of `h` (and `hl`, if not null) from the ring partials of the last step.
@@ -206,6 +211,8 @@ struct sbs_drainage {
     sbs::StepGeom geom{};
     int wtb_k = 0;  // steps per temporally blocked launch (WGSL semantics; 0 = single steps only)
     sbs::StepGeom wgeom{};
+    int cpu_k = 0;  // steps per temporally blocked launch (CPU semantics; 0 = single steps only)
+    sbs::StepGeom cgeom{};
 
     // CPU semantics parameters (from sbs_config)
     sbs_config cfg{};

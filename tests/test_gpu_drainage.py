@@ -84,6 +84,66 @@ def test_cpu_semantics_bit_exact(sbs, orc, precision, res):
         assert (got < h0 * 0.99999).any()  # fronts thinned something
 
 
+def set_cpu_blocking(sbs, sim, k):
+    sbs._native.call("sbs_drainage_set_time_blocking", sim.handle, k)
+
+
+def cpu_blocking(sbs, sim):
+    out = ctypes.c_int()
+    sbs._native.call("sbs_drainage_time_blocking", sim.handle, ctypes.byref(out))
+    return out.value
+
+
+@pytest.mark.parametrize("precision", ["f32x2", "f32"])
+@pytest.mark.parametrize("res", [10, 12, 64, 130, 256])
+def test_cpu_time_blocking_bit_identical(sbs, orc, precision, res):
+    """K = 1..4 steps per launch (the blocked kernel's polar strips form each step's ring means
+    as a cluster reduction): the same bits as single steps and as the kernel-order oracle, with
+    fronts active (first spawn at step 50), a frozen critical patch, volume checks and chunk
+    ends at every K."""
+    from soap_bubble_simulation_gb300 import synthetic
+
+    h0 = synthetic.bubble_c0(res, seed=res + 1)
+    h0[res // 3, : res // 2] = 5e-9  # below the 10 nm critical thickness: frozen
+    if precision == "f32":
+        h0 = h0.astype(np.float32).astype(np.float64)
+    results = []
+    for k in (1, 2, 3, 4):
+        sim = make_sim(sbs, res, precision)
+        assert cpu_blocking(sbs, sim) == (2 if precision == "f32x2" else 4)  # the defaults
+        set_cpu_blocking(sbs, sim, k)
+        assert cpu_blocking(sbs, sim) == k
+        set64(sbs, sim, h0)
+        sim.step_n(0.01, 23)
+        vols = sim.run_checked(0.01, 60, 20)
+        for _ in range(3):
+            sim.step(0.01)
+        results.append((field64(sbs, sim), vols, sim.active_tfe_count()))
+        sim.close()
+    for f, v, n in results[1:]:
+        np.testing.assert_array_equal(f, results[0][0])
+        np.testing.assert_allclose(v, results[0][1], rtol=1e-12)
+        assert n == results[0][2]
+    ref = orc.CpuSim(resolution=res, precision=ORC_PREC[precision])
+    ref.set_field(h0)
+    ref.step_n(0.01, 86)
+    np.testing.assert_array_equal(results[0][0], ref.field())
+    assert results[0][2] == ref.active_tfe_count() >= 1
+
+
+def test_cpu_time_blocking_needs_even_resolution(sbs):
+    sim = make_sim(sbs, 33)  # 66 columns: not a multiple of 4
+    assert cpu_blocking(sbs, sim) == 1
+    with pytest.raises(sbs.SbsError, match="even resolution"):
+        set_cpu_blocking(sbs, sim, 4)
+    set_cpu_blocking(sbs, sim, 1)
+    sim.step_n(0.001, 5)
+    small = make_sim(sbs, 8)  # fewer than 2 (K + 1) rows
+    assert cpu_blocking(sbs, small) == 1
+    with pytest.raises(sbs.SbsError):
+        set_cpu_blocking(sbs, small, 4)
+
+
 def test_step_n_equals_repeated_steps(sbs):
     from soap_bubble_simulation_gb300 import synthetic
 
