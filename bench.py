@@ -14,9 +14,17 @@ surfactant from pinned host memory, runs, and reads both fields and the volumes 
 roofline: the dominant kernel, the temporally blocked step (wtb_wgsl_kernel, 4 steps per
 launch), at 16 algorithmic bytes per cell-step (read h, Gamma; write h, Gamma) times the steps
 of a launch, against the measured copy bandwidth; `traffic` is its ncu DRAM bytes per launch.
-cpu_baseline: the oracle's f64 restatement of DrainageSimulator::step (drainage.rs:298-392) on
-all host cores, on a bounded sample of the same field (about --cpu-seconds of work);
-cpu_baseline_single_thread: the same on one core (the reference's CPU path is single-threaded).
+cpu_baseline: the oracle's restatement of drainage.wgsl (the same semantics: f32 h and
+surfactant, drainage.wgsl's own operation order) on all host cores, on a bounded sample of the
+same field (about --cpu-seconds of work); cpu_baseline_single_thread: the same on one core.
+parity: the GPU field after the baseline sample's number of passes against the sample's
+result (relative L-inf unmasked and on the CFL-stable rows, the rows the polar instability has
+not reached and sin(theta) >= 0.2), and 100 passes bit for bit against the oracle's restatement
+of the kernels' operation order.
+cpu_semantics: the reference's own solver, DrainageSimulator::step (pole means, fronts), at the
+same size: compensated f32x2 (16 B per cell-step; also given at 8 B, h only) and plain f32, with
+the f64 restatement of drainage.rs:298-503 on all host cores beside it.
+res4096: the WGSL step at 4096 x 8192 cells (537 MB, four times L2).
 surrogate: the learned 64-step operator (include/sbs_nn.h) trained here on 512 plain-solver
 trajectories at 256 x 512, then a 10,000-step rollout of the same 2048 x 4096 field with a plain
 check every 8 intervals; effective cell-steps/s and the masked relative L-inf error of the final
@@ -32,8 +40,10 @@ branched_flow: one step of the branched-flow ray tracer at the reference's defau
 foam_dynamics: FoamSimulator::step over a 1,048,576-bubble FCC foam (and 4,096 bubbles beside the
 oracle's all-pairs loops on one host core), bubble-steps/s.
 
---impl reference: times that CPU restatement alone (the reference is Rust and cannot be
-built here), same metric and config.
+--impl reference: times the drainage.wgsl restatement alone on all host cores (the reference is
+Rust and WGSL; neither can run here), same metric, config and semantics.
+
+The line ends with `summary`: the headline figures of every section, rounded.
 """
 from __future__ import annotations
 
@@ -158,12 +168,47 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
-def cpu_baseline(h: np.ndarray, target_s: float, threads: int):
-    """The oracle's f64 DrainageSimulator::step on `threads` host cores over a bounded sample."""
+def workload_config(world: int) -> dict:
+    """The workload both arms report (the same dict, so the driver can compare them)."""
+    return {"workload": "bubble resolution 2048 (2048 theta x 4096 phi = 8.4M cells), h 550 nm + 16 seeded modes, "
+                        "surfactant 0.5+-0.1, fluid defaults, dt 1e-3 s, 10,000 steps of GPUDrainageSimulator "
+                        "semantics (drainage.wgsl: f32 h and surfactant) per bench step, FP64 volume check every 100 "
+                        "steps",
+            "cells": RES * 2 * RES, "drainage_steps_per_bench_step": STEPS_PER_RUN, "check_every": CHECK_EVERY,
+            "l2": "512 MB write before every bench step (working set 128 MB)", "replicas": world}
+
+
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
 
-    sim = orc.CpuSim(resolution=RES, precision="f64", threads=threads)
+    return orc
+
+
+def cpu_baseline(h: np.ndarray, c: np.ndarray, target_s: float, threads: int):
+    """The oracle's restatement of drainage.wgsl (drainage.wgsl:72-202, its own f32 operation order,
+    h and surfactant) on `threads` host cores over a bounded sample of the workload. Returns the
+    baseline record and the sample's final fields (for the parity check)."""
+    orc = _oracle()
+    nt, np_ = h.shape
+    p = orc.wgsl_params(grid_width=np_, grid_height=nt)
+    t0 = time.perf_counter()
+    orc.wgsl_run(p, h, c, 1, "wgsl", threads)
+    one = time.perf_counter() - t0
+    n = int(max(2, min(20000, target_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    hn, cn = orc.wgsl_run(p, h, c, n, "wgsl", threads)
+    dt = time.perf_counter() - t0
+    rec = {"value": h.size * n / dt, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+           "sample": f"{n} passes of drainage_step (drainage.wgsl:72-202, f32 h and surfactant, its own operation "
+                     f"order) on the 2048 x 4096 field, {dt:.1f} s"}
+    return rec, (n, hn, cn)
+
+
+def cpu_baseline_f64(h: np.ndarray, target_s: float, threads: int):
+    """The oracle's f64 restatement of DrainageSimulator::step (drainage.rs:298-503) over a bounded sample."""
+    orc = _oracle()
+    sim = orc.CpuSim(resolution=h.shape[0], precision="f64", threads=threads)
     sim.set_field(h.astype(np.float64))
     t0 = time.perf_counter()
     sim.step(0.001)
@@ -172,10 +217,30 @@ def cpu_baseline(h: np.ndarray, target_s: float, threads: int):
     t0 = time.perf_counter()
     sim.step_n(0.001, n)
     dt = time.perf_counter() - t0
-    cells = h.size
-    return {"value": cells * n / dt, "unit": "cell-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{n} steps of DrainageSimulator::step (f64, drainage.rs:298-392) on the 2048 x 4096 field, "
+    return {"value": h.size * n / dt, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{n} steps of DrainageSimulator::step (f64, drainage.rs:298-503) on the 2048 x 4096 field, "
                       f"{dt:.1f} s"}
+
+
+def parity_section(sbs, sample, h0, c0):
+    """The GPU path against the CPU sample's fields (same input, same number of passes), and 100
+    passes bit for bit against the oracle's restatement of the kernels' own operation order."""
+    from soap_bubble_simulation_gb300 import parity
+
+    orc = _oracle()
+    n, hn, _ = sample
+    nt, np_ = h0.shape
+    sim = sbs.GPUDrainageSimulator(None, 550e-9, np_, nt)
+    sim.set_thickness_array(h0)
+    sim.set_concentration_array(c0)
+    sim.run(100)
+    hk, ck = orc.wgsl_run(orc.wgsl_params(grid_width=np_, grid_height=nt), h0, c0, 100, "kernel")
+    differing = int(np.count_nonzero(sim.thickness_array() != hk) + np.count_nonzero(sim.concentration_array() != ck))
+    sim.run(n - 100)
+    r = parity.report(sim.thickness_array(), hn, h0, {"sin_floor": 1e-4})
+    sim.close()
+    return {"steps": n, "reference": "drainage.wgsl operation order (f32)", **r,
+            "kernel_order_cells_differing_after_100": differing}
 
 
 def run_reference(args):
@@ -184,17 +249,16 @@ def run_reference(args):
         return
     from soap_bubble_simulation_gb300 import synthetic
 
-    h, _ = synthetic.bubble_c1(RES)
+    h, c = synthetic.bubble_c1(RES)
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_baseline(h, 0.5, threads)
-    vals = [cpu_baseline(h, args.cpu_seconds / max(args.steps, 1), threads) for _ in range(args.steps)]
+        cpu_baseline(h, c, 0.3, threads)
+    vals = [cpu_baseline(h, c, args.cpu_seconds / max(args.steps, 1), threads)[0] for _ in range(args.steps)]
     v = statistics.median(x["value"] for x in vals)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "cell-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": h.size * STEPS_PER_RUN / v * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "bubble resolution 2048 (2048 x 4096 cells), 10,000 steps, fluid defaults, "
-                                   "dt 1e-3 s; reference CPU path (DrainageSimulator::step) on a bounded sample"},
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(world),
             "cpu_baseline": {**vals[-1], "value": v},
             "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -601,6 +665,137 @@ def spectral_section(sbs, synthetic, torch):
     return out
 
 
+def profile_traffic(name: str):
+    """`traffic_bytes_per_launch:` of a committed ncu summary under profiles/ (or None)."""
+    try:
+        for line in open(os.path.join(ROOT, "profiles", name)):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(float(line.split(":", 1)[1]))
+    except OSError:
+        pass
+    return None
+
+
+def cpu_semantics_section(sbs, torch, h0, peak, cpu_seconds):
+    """The reference's own solver (DrainageSimulator::step with pole means and fronts) at 2048 x 4096
+    on the GPU, compensated f32x2 (the default) and plain f32, timed over 2000 steps after 512
+    (fronts active from step 500), with its roofline and the f64 restatement on all host cores."""
+    from soap_bubble_simulation_gb300 import _native as N
+
+    cells = h0.size
+    out = {}
+    for prec, bpc in (("f32x2", 16), ("f32", 8)):
+        cfg = sbs.SimulationConfig()
+        cfg.resolution = RES
+        c = cfg.to_c()
+        hh = ctypes.c_void_p()
+        N.call("sbs_drainage_create_ex", ctypes.byref(c), N.DRAIN_F32X2 if prec == "f32x2" else N.DRAIN_F32,
+               ctypes.byref(hh))
+        sim = sbs.DrainageSimulator.__new__(sbs.DrainageSimulator)
+        sbs.drainage._Handle.__init__(sim)
+        sim._h = hh
+        sim._config = cfg
+        kb = ctypes.c_int()
+        N.call("sbs_drainage_time_blocking", sim.handle, ctypes.byref(kb))
+        sim.set_thickness_array(h0)
+        sim.step_n(0.001, 512)
+        st = torch.cuda.ExternalStream(sim.stream())
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n = 2000
+        torch.cuda.synchronize()
+        a.record(st)
+        sim.step_n(0.001, n)
+        b.record(st)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        sim.close()
+        rate = cells * n / (ms * 1e-3)
+        gbs = bpc * rate / 1e9
+        out[prec] = {"value": rate, "unit": "cell-steps/s", "us_per_step": ms * 1e3 / n, "steps_per_launch": kb.value,
+                     "roofline": {"bound": "hbm", "bytes_per_cell_step": bpc, "achieved": gbs, "peak": peak,
+                                  "unit": "GB/s", "frac": gbs / peak,
+                                  "frac_at_8B_per_cell_step": 8 * rate / 1e9 / peak,
+                                  "traffic": profile_traffic("drain_wtbc_cpu_c1.md") if prec == "f32x2" else None,
+                                  "kernel": f"wtbc_kernel<{kb.value}, {'compensated' if prec == 'f32x2' else 'f32'}>"}}
+    base = cpu_baseline_f64(h0, cpu_seconds, os.cpu_count() or 1)
+    out["cpu_baseline"] = base
+    out["vs_cpu_baseline"] = out["f32x2"]["value"] / base["value"]
+    return out
+
+
+def res4096_section(sbs, synthetic, torch, peak):
+    """The WGSL step at resolution 4096 (4096 x 8192 cells, a 537 MB working set: 4 x the 129 MB
+    L2), where the temporally blocked kernel's fields cannot stay in L2 between launches."""
+    h, c = synthetic.bubble_c1(4096)
+    nt, np_ = h.shape
+    sim = sbs.GPUDrainageSimulator(None, 550e-9, np_, nt)
+    sim.set_thickness_array(h)
+    sim.set_concentration_array(c)
+    sim.run(40)
+    st = torch.cuda.ExternalStream(sim.stream())
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n = 400
+    torch.cuda.synchronize()
+    a.record(st)
+    sim.run(n)
+    b.record(st)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    sim.close()
+    rate = h.size * n / (ms * 1e-3)
+    launch_us = ms * 1e3 / n * 4
+    dram = 511_542_272  # ncu DRAM bytes per 4-step launch at this size (profiles/drain_wtb_wgsl_c1.md)
+    return {"value": rate, "unit": "cell-steps/s", "cells": int(h.size), "steps": n, "launch_us": launch_us,
+            "roofline": {"bound": "hbm", "achieved": 16 * rate / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": 16 * rate / 1e9 / peak, "traffic": dram,
+                         "dram_frac": dram / (launch_us * 1e-6) / 1e9 / peak}}
+
+
+def _r(x, n=3):
+    """Rounds to n significant digits (compact summary)."""
+    if x is None or not isinstance(x, (int, float)) or x == 0 or not np.isfinite(x):
+        return x
+    return float(f"{x:.{n}g}")
+
+
+def summary(line: dict) -> dict:
+    """The headline figures of every section, rounded, for the end of the JSON line."""
+    g = lambda d, *k: (None if d is None else (d.get(k[0]) if len(k) == 1 else g(d.get(k[0]), *k[1:])))
+    out = {"c1": {"value": _r(line["value"]), "e2e": _r(line["e2e"]["value"]),
+                  "frac_alg": _r(line["roofline"]["frac"]), "dram_frac": _r(line["roofline"].get("dram_frac")),
+                  "vs_cpu": _r(line["value"] / line["cpu_baseline"]["value"]) if line.get("cpu_baseline") else None,
+                  "vs_cpu_1core": _r(line["value"] / line["cpu_baseline_single_thread"]["value"])
+                  if line.get("cpu_baseline_single_thread") else None}}
+    par = line.get("parity")
+    if par:
+        out["parity"] = {"steps": par["steps"], "bitdiff_kernel_order_100": par["kernel_order_cells_differing_after_100"],
+                         "rel": _r(par["rel_linf"], 2), "rel_cfl": _r(par["rel_linf_cfl_rows"], 2),
+                         "rel_stable": _r(par["rel_linf_stable_rows_margin8"], 2),
+                         "rel_sin02": _r(par["rel_linf_sin_ge_0.2"], 2)}
+    cs = line.get("cpu_semantics")
+    if cs:
+        out["cpu_sem"] = {"value": _r(cs["f32x2"]["value"]), "frac16": _r(cs["f32x2"]["roofline"]["frac"]),
+                          "frac8": _r(cs["f32x2"]["roofline"]["frac_at_8B_per_cell_step"]),
+                          "f32_frac8": _r(cs["f32"]["roofline"]["frac"]), "vs_cpu_f64": _r(cs["vs_cpu_baseline"])}
+    if line.get("res4096"):
+        out["res4096"] = {"value": _r(line["res4096"]["value"]), "frac_alg": _r(line["res4096"]["roofline"]["frac"]),
+                          "dram_frac": _r(line["res4096"]["roofline"]["dram_frac"])}
+    if line.get("foam"):
+        out["foam"] = {"value": _r(line["foam"]["value"]), "gbs_alg": _r(line["foam"]["algorithmic_gbs"])}
+    sp = line.get("spectral")
+    if sp:
+        out["spectral"] = {k: _r(g(sp, k, "value")) for k in sp if isinstance(sp.get(k), dict) and "value" in sp[k]}
+    for key in ("surrogate", "surrogate_hswish"):
+        su = line.get(key)
+        if su:
+            out[key] = {"x_plain": _r(su["speedup_vs_plain"]), "err": _r(su["masked_rel_linf_vs_plain"], 2),
+                        "id_err": _r(su["identity_rel_linf_vs_plain"], 2), "tc_frac": _r(su["tensor"]["frac"])}
+    for key in ("shading", "caustics", "branched_flow", "foam_dynamics"):
+        if line.get(key):
+            out[key] = _r(line[key]["value"])
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -695,24 +890,11 @@ def main():
     (e2e_s,) = max_over_ranks(e2e_s)
     e2e_value = world * cells * STEPS_PER_RUN * e2e_steps / e2e_s
 
-    # ---- the reference's CPU semantics on the GPU, for context (compensated f32x2) --------------
-    cfg = sbs.SimulationConfig()
-    cfg.resolution = RES
-    cpu_sem = sbs.DrainageSimulator(cfg)
-    cpu_sem.set_thickness_array(h0)
-    cpu_sem.step_n(0.001, 200)
-    torch.cuda.synchronize()
-    cs = torch.cuda.ExternalStream(cpu_sem.stream())
-    a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a_ev.record(cs)
-    cpu_sem.step_n(0.001, 2000)
-    b_ev.record(cs)
-    torch.cuda.synchronize()
-    cpu_sem_ms = a_ev.elapsed_time(b_ev)
-    cpu_sem_rate = cells * 2000 / (cpu_sem_ms / 1e3)
-
-    surrogate = foam = spectral = small = shade = caus = bflow = fdyn = None
+    surrogate = foam = spectral = small = shade = caus = bflow = fdyn = cpu_sem = big = None
     if not args.skip_aux:
+        cpu_sem = cpu_semantics_section(sbs, torch, h0, peak,
+                                         min(args.cpu_seconds, 10.0) if rank == 0 and world == 1 else 0.5)
+        big = res4096_section(sbs, synthetic, torch, peak)
         small = c0_section(sbs, synthetic, torch)
         shade = shade_section(sbs, torch)
         caus = caustics_section(sbs, synthetic, torch, h0, c0)
@@ -723,39 +905,38 @@ def main():
         if rank == 0 and world == 1:
             fdyn = foam_dynamics_section(sbs, min(args.cpu_seconds, 10.0))
 
-    base = base1 = None
+    base = base1 = par = None
     if rank == 0 and world == 1 and not args.skip_aux:
-        base = cpu_baseline(h0, args.cpu_seconds, os.cpu_count() or 1)
-        # the reference's own CPU path is single-threaded: the same restatement on one core
-        base1 = cpu_baseline(h0, min(args.cpu_seconds, 8.0), 1)
+        base, sample = cpu_baseline(h0, c0, args.cpu_seconds, os.cpu_count() or 1)
+        par = parity_section(sbs, sample, h0, c0)
+        # one host core: the reference's own CPU code is single-threaded
+        base1, _ = cpu_baseline(h0, c0, min(args.cpu_seconds, 6.0), 1)
 
     if rank == 0:
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_kind": peak_kind, "bytes_per_launch": BYTES_PER_CELL_STEP * cells * k_block,
+                "steps_per_launch": k_block, "launch_us": launch_us,
+                "dram_frac": traffic / (launch_us * 1e-6) / 1e9 / peak if traffic else None,
+                "kernel": f"wtb_wgsl_kernel<{k_block}> (temporally blocked WGSL step)",
+                "note": "algorithmic bytes: 16 B per cell-step; temporal blocking keeps k steps on chip, so achieved "
+                        "can exceed the copy peak; traffic is ncu DRAM bytes per launch (L2 holds part of the 128 MB "
+                        "working set at this size; see res4096 for a size L2 cannot hold)"}
         line = {
             "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "bubble resolution 2048 (2048 theta x 4096 phi = 8.4M cells), h 550 nm + 16 "
-                                   "seeded modes, surfactant 0.5+-0.1, fluid defaults, dt 1e-3 s, 10,000 steps of "
-                                   "GPUDrainageSimulator semantics per bench step, FP64 volume check every 100 steps",
-                       "cells": cells, "drainage_steps_per_bench_step": STEPS_PER_RUN, "check_every": CHECK_EVERY,
-                       "l2": "512 MB write before every bench step (working set 128 MB)",
-                       "replicas": world},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "peak_kind": peak_kind,
-                         "bytes_per_launch": BYTES_PER_CELL_STEP * cells * k_block,
-                         "steps_per_launch": k_block, "launch_us": launch_us,
-                         "kernel": f"wtb_wgsl_kernel<{k_block}> (temporally blocked WGSL step)",
-                         "note": "algorithmic bytes: 16 B per cell-step; temporal blocking keeps k steps on chip, "
-                                 "so achieved can exceed the copy peak and traffic is ~1/k of the algorithmic bytes"},
+            "config": workload_config(world),
+            "roofline": roof,
             "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": 2 * cells * 4,
                     "d2h_bytes_per_step": 2 * cells * 4 + 8 * (STEPS_PER_RUN // CHECK_EVERY)},
             "gpu_launches": args.steps * launches,
             "clocks": clk.summary(),
-            "volume_rel_drift_per_run": vol_drift,
-            "cpu_semantics": {"value": cpu_sem_rate, "unit": "cell-steps/s", "storage": "f32x2 (16 B/cell-step)",
-                              "frac_hbm": BYTES_PER_CELL_STEP * cells * 2000 / (cpu_sem_ms / 1e3) / 1e9 / peak},
             "cpu_baseline": base,
             "cpu_baseline_single_thread": base1,
+            "parity": par,
+            "volume_rel_drift_per_run": vol_drift,
+            "cpu_semantics": cpu_sem,
+            "res4096": big,
             "surrogate": surrogate and surrogate["gelu"],
             "surrogate_hswish": surrogate and surrogate["hswish"],
             "foam": foam,
@@ -766,6 +947,7 @@ def main():
             "branched_flow": bflow,
             "foam_dynamics": fdyn,
         }
+        line["summary"] = summary(line)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -70,3 +70,9 @@ def test_reference_arm_under_torchrun_two_ranks():
     line = lines[0]
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
+    # the same workload description as the GPU arm, and the same semantics (drainage.wgsl, f32)
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert line["config"] == bench.workload_config(2)
+    assert line["dtype"] == "f32" and "drainage.wgsl" in line["cpu_baseline"]["sample"]
