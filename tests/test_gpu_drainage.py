@@ -138,7 +138,7 @@ def test_cpu_time_blocking_needs_even_resolution(sbs):
         set_cpu_blocking(sbs, sim, 4)
     set_cpu_blocking(sbs, sim, 1)
     sim.step_n(0.001, 5)
-    small = make_sim(sbs, 8)  # fewer than 2 (K + 1) rows
+    small = make_sim(sbs, 4)  # fewer than 2 (K + 1) rows for any K
     assert cpu_blocking(sbs, small) == 1
     with pytest.raises(sbs.SbsError):
         set_cpu_blocking(sbs, small, 4)
