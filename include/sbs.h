@@ -65,6 +65,28 @@ const char *sbs_version(void);
 /* Number of CUDA devices visible, or a negative code. */
 int sbs_device_count(int *out);
 
+/* Bounded device-side waits (no reference counterpart). Every wait inside this
+ * library's kernels - the foam batch's grid barrier, the mbarrier waits of the
+ * tensor-core spectral contraction and of the fused surrogate kernel - gives up
+ * after `cycles` SM clock cycles (default 2e9, about one second): the kernel
+ * records the timeout, finishes its outstanding tensor-core work, frees its
+ * tensor memory and exits, and the call returns SBS_E_TIMEOUT; the context and
+ * the handles stay usable. The limit is process-wide and applies to launches
+ * made after the call (handles rebuild their captured CUDA graphs). */
+int sbs_set_wait_limit(uint64_t cycles);
+int sbs_wait_limit(uint64_t *out);
+
+/* Test switch for the timeout path (no reference counterpart): makes the
+ * bounded waits of later launches unsatisfiable without faulting anything.
+ * SBS_STALL_TENSOR_COMMITS: the tensor-core kernels issue neither their MMAs
+ * nor the commits that signal them, so nothing asynchronous is in flight when
+ * the waits expire. SBS_STALL_GRID_BARRIER: the foam kernel's grid barrier
+ * expects one arrival more than the grid has. 0 (the default) turns both off.
+ * Process-wide; meant for tests, which set a short wait limit first. */
+#define SBS_STALL_TENSOR_COMMITS 1
+#define SBS_STALL_GRID_BARRIER 2
+int sbs_set_stall_injection(int flags);
+
 /* ------------------------------------------------------------------ */
 /* Configuration: SimulationConfig (config.rs:283-302) and its         */
 /* defaults (config.rs:26-35, 56-66, 93-103, 305-316).                 */

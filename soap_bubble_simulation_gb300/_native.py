@@ -38,6 +38,8 @@ NN_PARAMS = 23425
 NN_ACT_GELU = 0
 NN_ACT_HSWISH = 1
 NN_STEPS = 64
+STALL_TENSOR_COMMITS = 1
+STALL_GRID_BARRIER = 2
 
 _ERR_NAMES = {
     SBS_E_INVALID: "SBS_E_INVALID",
@@ -165,6 +167,9 @@ SIGNATURES: dict[str, list] = {
     "sbs_gpu_drainage_set_marangoni_params": [_P, _F, _F, _F, _F],
     "sbs_gpu_drainage_set_time_blocking": [_P, _I],
     "sbs_gpu_drainage_time_blocking": [_P, _IP],
+    "sbs_set_wait_limit": [C.c_uint64],
+    "sbs_wait_limit": [C.POINTER(C.c_uint64)],
+    "sbs_set_stall_injection": [_I],
     "sbs_drainage_set_time_blocking": [_P, _I],
     "sbs_drainage_time_blocking": [_P, _IP],
     "sbs_gpu_drainage_set_enabled": [_P, _I],

@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 
+#include <atomic>
 #include <map>
 #include <mutex>
 
@@ -65,9 +66,47 @@ cudaError_t scratch_alloc(void **p, size_t bytes, cudaStream_t s) {
     return cudaMallocFromPoolAsync(p, bytes, pool, s);
 }
 
+namespace {
+std::atomic<long long> g_wait_cycles{kDefaultWaitCycles};
+std::atomic<int> g_stall{0};
+std::atomic<unsigned> g_wait_epoch{0};
+}  // namespace
+
+WaitConfig wait_config() {
+    WaitConfig w;
+    w.cycles = g_wait_cycles.load();
+    w.stall = g_stall.load();
+    w.epoch = g_wait_epoch.load();
+    return w;
+}
+
 }  // namespace sbs
 
 extern "C" {
+
+int sbs_set_wait_limit(uint64_t cycles) {
+    sbs::clear_error();
+    SBS_CHECK_ARG(cycles >= 1000 && cycles <= (uint64_t)1 << 40, "wait limit must be 1e3 .. 2^40 cycles (got %llu)",
+                  (unsigned long long)cycles);
+    sbs::g_wait_cycles.store((long long)cycles);
+    sbs::g_wait_epoch.fetch_add(1);
+    return SBS_OK;
+}
+
+int sbs_wait_limit(uint64_t *out) {
+    SBS_CHECK_ARG(out != nullptr, "out is null");
+    *out = (uint64_t)sbs::g_wait_cycles.load();
+    return SBS_OK;
+}
+
+int sbs_set_stall_injection(int flags) {
+    sbs::clear_error();
+    SBS_CHECK_ARG((flags & ~(SBS_STALL_TENSOR_COMMITS | SBS_STALL_GRID_BARRIER)) == 0, "unknown stall flags %d",
+                  flags);
+    sbs::g_stall.store(flags);
+    sbs::g_wait_epoch.fetch_add(1);
+    return SBS_OK;
+}
 
 const char *sbs_last_error(void) { return sbs::g_last_error; }
 

@@ -28,7 +28,6 @@ namespace {
 
 constexpr int kWarps = 4;
 constexpr int kSeg = 120;                          // output columns per warp item
-constexpr long long kBarrierCycles = 4000000000LL;  // ~2 s: bound on a grid-barrier wait
 
 struct FoamBubble {
     float *h[2], *c[2];
@@ -47,23 +46,27 @@ struct FoamArgs {
     int nitems, nphases, parity0, rbmax;
     float dt, crit;
     unsigned *bar;  // [0] arrival count, [1] generation, [2] status (bit 1: barrier timeout)
+    long long wait_cycles;  // bound on one barrier wait
+    unsigned extra;         // arrivals the barrier expects beyond the grid (1: the timeout test)
 };
 
-// Grid-wide barrier for a cooperative (all-resident) grid; false if the wait timed out.
-__device__ bool grid_barrier(unsigned *bar, unsigned nblocks, int *s_timeout) {
+// Grid-wide barrier for a cooperative (all-resident) grid of `nblocks` blocks, completed by
+// nblocks + extra arrivals (extra is 0 except in the timeout test, where nothing completes it);
+// false if the wait ran past `limit` cycles.
+__device__ bool grid_barrier(unsigned *bar, unsigned nblocks, unsigned extra, long long limit, int *s_timeout) {
     __syncthreads();
     if (threadIdx.x == 0) {
         *s_timeout = 0;
         const unsigned gen = atomicAdd(bar + 1, 0u);
         __threadfence();
-        if (atomicAdd(bar, 1u) + 1 == nblocks) {
+        if (atomicAdd(bar, 1u) + 1 == nblocks + extra) {
             atomicExch(bar, 0u);
             __threadfence();
             atomicAdd(bar + 1, 1u);
         } else {
             const long long t0 = clock64();
             while (atomicAdd(bar + 1, 0u) == gen) {
-                if (clock64() - t0 > kBarrierCycles) {
+                if (clock64() - t0 > limit) {
                     atomicOr(bar + 2, 2u);
                     *s_timeout = 1;
                     break;
@@ -141,7 +144,7 @@ __global__ void __launch_bounds__(kWarps * 32) foam_kernel(const FoamArgs a) {
                 if (t + 2 < t1) wtb_iter<K, 2, false, MAR, true>(w, t + 2, wh, wc, ph4, pc4, vacc);
             }
         }
-        if (ph + 1 < a.nphases && !grid_barrier(a.bar, gridDim.x, &s_timeout)) return;
+        if (ph + 1 < a.nphases && !grid_barrier(a.bar, gridDim.x, a.extra, a.wait_cycles, &s_timeout)) return;
     }
 }
 
@@ -174,6 +177,7 @@ struct sbs_foam {
     cudaStream_t stream = nullptr;
     sbs_drainage_params params{};
     bool graphs_ok = true;
+    unsigned wait_epoch = 0;  // the wait settings the captured graphs were made with
     std::map<long long, cudaGraphExec_t> graphs;
 };
 
@@ -235,6 +239,9 @@ int launch_phases(sbs_foam *f, int k, int phases) {
     a.dt = f->params.dt;
     a.crit = f->params.critical_thickness;
     a.bar = f->bar;
+    const WaitConfig w = wait_config();
+    a.wait_cycles = w.cycles;
+    a.extra = (w.stall & SBS_STALL_GRID_BARRIER) ? 1u : 0u;
     void *args[] = {(void *)&a};
     const dim3 grid((unsigned)(per_sm * sms)), block(kWarps * 32);
     SBS_CUDA_TRY(cudaLaunchCooperativeKernel(fn, grid, block, args, smem, f->stream));
@@ -264,6 +271,12 @@ int check_status(sbs_foam *f) {
 
 int run_steps(sbs_foam *f, uint32_t steps) {
     if (steps == 0) return SBS_OK;
+    const unsigned epoch = wait_config().epoch;
+    if (epoch != f->wait_epoch) {  // the launches carry the wait settings: capture them again
+        SBS_CUDA_TRY(cudaStreamSynchronize(f->stream));
+        foam_destroy_graphs(f);
+        f->wait_epoch = epoch;
+    }
     const long long key = ((long long)steps << 1) | f->cur;
     auto it = f->graphs.find(key);
     if (it != f->graphs.end()) {

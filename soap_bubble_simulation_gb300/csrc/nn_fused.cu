@@ -114,7 +114,6 @@ constexpr uint32_t kOffPrev = (kOffBar + 8 * (kNumBars + 1) + 64 + 15) / 16 * 16
 constexpr uint32_t kSmem = kOffPrev + kDepth4 * kLanes * 4;
 constexpr int kMaxTileRows = 256;
 static_assert(kSmem <= 227 * 1024, "shared memory per CTA");
-constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at 2 GHz
 // try_wait may suspend the thread until the phase completes or this many ns pass (waiting warps
 // then take no issue slots from the working ones)
 constexpr uint32_t kSuspendNs = 1000000;
@@ -164,10 +163,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     return ok != 0;
 }
 
-__device__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+// Bounded wait on an mbarrier phase; false after `limit` cycles (sbs_set_wait_limit).
+__device__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, long long limit) {
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > kWaitCycles) return false;
+        if (clock64() - t0 > limit) return false;
     return true;
 }
 
@@ -209,6 +209,8 @@ struct FusedArgs {
     int nf, nstrips, nrb, rows_per_block, ntiles;
     int act;  // SBS_NN_ACT_*
     unsigned *err;
+    long long wait_cycles;  // bound on every mbarrier wait
+    int stall;              // 1 (the timeout test): the MMA warps issue neither MMAs nor commits
 };
 
 // MMAs of layer l (1-based) for input row s into the layer's accumulator ring (or, for the pole
@@ -364,9 +366,10 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
 struct Waiter {
     volatile int *fail;
     unsigned *err;
+    long long limit;
     __device__ __forceinline__ void wait(uint32_t bar, uint32_t count) {
         if (*fail) return;
-        if (!mbar_wait_bounded(bar, count & 1u)) {
+        if (!mbar_wait_bounded(bar, count & 1u, limit)) {
             atomicOr(err, 1u);
             *fail = 1;
         }
@@ -459,7 +462,7 @@ __device__ void mma_agent(const int L, const FusedArgs &a, const Bars &bars, uin
             const int c = slot(s - 1);
             const uint64_t ad0 = adb + (uint64_t)((uint32_t)b * row_step);
             const bool top = s == 1 && top_ok, bot = s == nt - 2 && bot_ok;
-            if (!*s_fail) {
+            if (!*s_fail && !a.stall) {
                 const uint32_t xe = bars.xempty(L, b), af = bars.afull(L, c);
                 switch (L) {
                     case 1: issue_row<1>(dacc, ad0, bd0, c, sbase, top, bot, oslot, xe, af); break;
@@ -471,7 +474,7 @@ __device__ void mma_agent(const int L, const FusedArgs &a, const Bars &bars, uin
             __syncwarp();
         }
         // rows H-1 and H are complete with the last row's MMAs
-        if (!*s_fail && elect_one()) {
+        if (!*s_fail && !a.stall && elect_one()) {
             commit(bars.afull(L, slot(H - 1)));
             commit(bars.afull(L, slot(H)));
         }
@@ -681,7 +684,7 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(FusedArgs a) {
         }
         wait_st();
     }
-    Waiter wt{s_fail, a.err};
+    Waiter wt{s_fail, a.err, a.wait_cycles};
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -700,7 +703,7 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(FusedArgs a) {
     }
     __syncthreads();
     // no MMA may still write the accumulators when the columns are released
-    if (tid == 0 && !mbar_wait_bounded(drain, 0u)) atomicOr(a.err, 1u);
+    if (tid == 0 && !mbar_wait_bounded(drain, 0u, a.wait_cycles)) atomicOr(a.err, 1u);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -813,6 +816,9 @@ int fused_forward(sbs_surrogate *s, const Fields &fields, int nf, const GridTab 
     a.nstrips = (g.np + kOut - 1) / kOut;
     a.act = act_of(s);
     a.err = st->err;
+    const WaitConfig w = wait_config();
+    a.wait_cycles = w.cycles;
+    a.stall = (w.stall & SBS_STALL_TENSOR_COMMITS) ? 1 : 0;
     // rows per block: the smallest block count whose tile count fills the grid evenly (>= 16 rows)
     const int sms = std::max(1, sms_of(s));
     const int per_field = a.nstrips;

@@ -35,6 +35,18 @@ void clear_error();
 // Makes sure a CUDA device exists and the runtime is usable; fails with SBS_E_CUDA otherwise.
 int require_device();
 
+// Bounded device-side waits: every spin or mbarrier wait of a kernel gives up after `cycles` SM
+// clock cycles, records the timeout in a device flag and lets the kernel exit; the host reports
+// SBS_E_TIMEOUT. `stall` holds the SBS_STALL_* test switches (sbs_set_stall_injection); `epoch`
+// changes with every setting, so handles that captured launches in CUDA graphs rebuild them.
+constexpr long long kDefaultWaitCycles = 2000000000LL;  // ~1 s at 2 GHz
+struct WaitConfig {
+    long long cycles;
+    int stall;
+    unsigned epoch;
+};
+WaitConfig wait_config();
+
 // Stream-ordered scratch for one call (release it with cudaFreeAsync on the same stream). Blocks of
 // up to 64 MB come from a per-device pool that keeps freed memory for the next call (the default
 // pool returns it to the system at every synchronisation, and mapping it again costs ~100 us);

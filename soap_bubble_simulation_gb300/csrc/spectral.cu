@@ -7,8 +7,9 @@
 // memory (K-major, 8 x 16-byte core matrices, no swizzle); one thread issues K/16
 // tcgen05.mma.kind::f16 instructions against the colour-matching B tile (16 x K, channels 3..15
 // zero) with the FP32 accumulator D (128 x 16) in tensor memory, and commits them to an mbarrier;
-// each warp then reads its 32 rows of D with tcgen05.ld. Every wait is bounded: on timeout the CTA
-// records the failure in a device flag, frees its tensor memory and returns.
+// each warp then reads its 32 rows of D with tcgen05.ld. Every wait is bounded (sbs_set_wait_limit):
+// on timeout the CTA records the failure in a device flag, waits (bounded) for contractions still
+// in flight, frees its tensor memory and returns.
 //
 // FP32 mode: the same spectra in FP32 contracted with FP32 FMAs (the precision reference for the
 // BF16 contraction).
@@ -34,7 +35,6 @@ namespace {
 constexpr int kTileM = 128;
 constexpr int kNPad = 16;         // MMA N (channels 0..2 used)
 constexpr int kMaxLambda = 128;   // K padded to a multiple of 16, at most 128
-constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz: bound on every mbarrier wait
 
 // The BF16 CMF^T tile (B operand) passed by value in the kernel parameters: no per-call device
 // buffer, no upload.
@@ -128,11 +128,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait on an mbarrier phase; returns false on timeout.
-__device__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+// Bounded wait on an mbarrier phase; returns false after `limit` cycles.
+__device__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, long long limit) {
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > kWaitCycles) return false;
+        if (clock64() - t0 > limit) return false;
     return true;
 }
 
@@ -167,7 +167,8 @@ __global__ void __launch_bounds__(kTileM) spectral_tc_kernel(const float *__rest
                                                             const float *__restrict__ cos_i,
                                                             const float *__restrict__ n_film, size_t n,
                                                             const BTile b_tile, const SpecConsts c,
-                                                            float *__restrict__ rgb, unsigned *err) {
+                                                            float *__restrict__ rgb, unsigned *err,
+                                                            long long wait_cycles, int stall) {
     constexpr uint32_t SBO = (KPAD / 8) * 128;
     constexpr uint32_t A_BYTES = kTileM * KPAD * 2;
     constexpr uint32_t B_BYTES = kNPad * KPAD * 2;
@@ -204,7 +205,7 @@ __global__ void __launch_bounds__(kTileM) spectral_tc_kernel(const float *__rest
 
     // waits for the contraction of `tile` (buffer b) and writes its colours; false on timeout
     auto finish = [&](size_t tile, int b) -> bool {
-        if (tid == 0 && !mbar_wait_bounded(smem_u32(bar + b), (phases >> b) & 1u)) {
+        if (tid == 0 && !mbar_wait_bounded(smem_u32(bar + b), (phases >> b) & 1u, wait_cycles)) {
             atomicOr(err, 1u);
             *s_fail = 1;
         }
@@ -244,7 +245,7 @@ __global__ void __launch_bounds__(kTileM) spectral_tc_kernel(const float *__rest
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
-        if (tid == 0) {
+        if (tid == 0 && !stall) {  // stall (the timeout test): neither MMAs nor their commit
             const uint32_t a_base = smem_u32(sA);
 #pragma unroll
             for (int kk = 0; kk < KPAD / 16; ++kk) {
@@ -270,8 +271,8 @@ __global__ void __launch_bounds__(kTileM) spectral_tc_kernel(const float *__rest
     if (NBUF == 2 && ok && it > 0) ok = finish(prev, (it - 1) & 1);
     if (!ok && tid == 0) {
         // contractions may still be in flight: give each barrier one more bounded wait before freeing
-        mbar_wait_bounded(smem_u32(bar), phases & 1u);
-        mbar_wait_bounded(smem_u32(bar + 1), (phases >> 1) & 1u);
+        mbar_wait_bounded(smem_u32(bar), phases & 1u, wait_cycles);
+        mbar_wait_bounded(smem_u32(bar + 1), (phases >> 1) & 1u, wait_cycles);
     }
     tc_fence_before();
     __syncthreads();
@@ -331,7 +332,9 @@ cudaError_t launch_tc(const float *t, const float *ci, const float *nf, size_t n
     const size_t ntiles = (n + kTileM - 1) / kTileM;
     size_t grid = (size_t)per_sm * sms;
     if (grid > ntiles) grid = ntiles;
-    spectral_tc_kernel<KPAD, NBUF><<<(unsigned)grid, kTileM, smem, s>>>(t, ci, nf, n, btile, c, rgb, err);
+    const WaitConfig w = wait_config();
+    spectral_tc_kernel<KPAD, NBUF><<<(unsigned)grid, kTileM, smem, s>>>(
+        t, ci, nf, n, btile, c, rgb, err, w.cycles, (w.stall & SBS_STALL_TENSOR_COMMITS) ? 1 : 0);
     return cudaGetLastError();
 }
 
