@@ -301,8 +301,11 @@ int sbs_film_volume_device(const float *h, uint32_t num_theta, uint32_t num_phi,
  * Rules:
  *  - num_theta <= 16384 (the rows whose weights fit in the array); larger
  *    grids are rejected with SBS_E_INVALID.
- *  - The first call on each device looks up the array's device address; make
- *    that first call before any stream capture on that device.
+ *  - Each call looks up the array's device address in the current device's
+ *    context (so a cudaDeviceReset, after which the array lives at a new
+ *    address, is followed); the first call on a device also loads the
+ *    library's device code there: make that first call before any stream
+ *    capture on that device.
  *  - Every call uses the same array, which keeps the previous call's contents
  *    (the call clears its own counter). Calls whose work overlaps on the GPU,
  *    from different streams or threads, race and can return wrong sums:

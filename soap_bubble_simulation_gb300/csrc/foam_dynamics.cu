@@ -52,7 +52,9 @@ constexpr int kThreads = 256;
 constexpr uint32_t kNone = 0xffffffffu;
 constexpr unsigned long long kNoPair = ~0ull;
 
-enum Fault : uint32_t { kFaultNone = 0, kFaultCapacity = 1, kFaultDense = 2 };
+// kFaultWalk: a bubble's candidate walk collected a different number of entries than its count
+// pass (the two passes make the same decisions, so this means a fault of the build itself).
+enum Fault : uint32_t { kFaultNone = 0, kFaultCapacity = 1, kFaultDense = 2, kFaultWalk = 3 };
 
 // Device-side control block.
 struct Ctl {
@@ -520,6 +522,10 @@ __global__ void __launch_bounds__(kListWarps * 32) list_walk_kernel(ListArgs a) 
             if (ok && slot < mk) col[(size_t)slot * 32] = a.bitems[i];
             m += __popc(bal);
         });
+        // a column the walk did not fill exactly would be sorted with stale entries: stop the
+        // list build and every later pass of the call instead
+        if (m != mk && lane == 0)
+            atomicCAS(const_cast<uint32_t *>(&c->fault), (uint32_t)kFaultNone, (uint32_t)kFaultWalk);
     }
 }
 
@@ -1137,6 +1143,7 @@ int rebuild_now(sbs_foam_sim *s, float skin) {
             return set_error(SBS_E_INVALID,
                              "foam too dense: bubble %u has %u neighbours within 3 (r_a + r_b) + skin (limit %d)",
                              h.dense_bubble, h.dense_count, kMaxCand);
+        if (h.fault == kFaultWalk) return set_error(SBS_E_STATE, "foam neighbour list: walk and count passes disagree");
         if (h.fault == kFaultNone) {
             s->list_invalid = false;
             return SBS_OK;
@@ -1332,6 +1339,7 @@ int sbs_foam_sim_step(sbs_foam_sim *s, float dt, uint32_t steps) {
         if ((rc = read_ctl(s, &h))) return rc;
         s->stepped = true;
         if (h.fault == kFaultNone) break;
+        if (h.fault == kFaultWalk) return set_error(SBS_E_STATE, "foam neighbour list: walk and count passes disagree");
         // The list outgrew its storage at a rebuild: the steps from there on did nothing. Restore
         // the buffer parities of the last completed step, grow the list and continue.
         done += h.steps_done;

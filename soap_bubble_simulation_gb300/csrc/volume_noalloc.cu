@@ -8,8 +8,6 @@
 // cause.
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 #include "sbs_internal.h"
 
 namespace sbs {
@@ -27,25 +25,16 @@ constexpr size_t kScratchDoubles = kOffCounter + 1;  // 19,460 doubles = 155,680
 // must use the address cudaGetSymbolAddress returns for it (see scratch_on_current_device).
 static __device__ __align__(256) double g_volume_scratch[kScratchDoubles];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-double *g_scratch_ptr[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device, looked up once per device.
+// Device address of the scratch array in the current device's context. It is looked up on every
+// call (a lookup allocates nothing and costs ~a microsecond): a cached address would outlive a
+// cudaDeviceReset, after which the library's module, and the array with it, is loaded again at a
+// new address. The first lookup on a device loads the module.
 int scratch_on_current_device(double **out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return set_error(SBS_E_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return set_error(SBS_E_CUDA, "device %d out of range", dev);
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (g_scratch_ptr[dev] == nullptr) {
-        double *p = nullptr;
-        e = cudaGetSymbolAddress((void **)&p, g_volume_scratch);
-        if (e != cudaSuccess)
-            return set_error(SBS_E_CUDA, "cudaGetSymbolAddress(volume scratch): %s", cudaGetErrorString(e));
-        g_scratch_ptr[dev] = p;
-    }
-    *out = g_scratch_ptr[dev];
+    double *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress((void **)&p, g_volume_scratch);
+    if (e != cudaSuccess)
+        return set_error(SBS_E_CUDA, "cudaGetSymbolAddress(volume scratch): %s", cudaGetErrorString(e));
+    *out = p;
     return SBS_OK;
 }
 
