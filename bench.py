@@ -788,8 +788,10 @@ def summary(line: dict) -> dict:
     for key in ("surrogate", "surrogate_hswish"):
         su = line.get(key)
         if su:
+            ho = su.get("heldout_256") or {}
             out[key] = {"x_plain": _r(su["speedup_vs_plain"]), "err": _r(su["masked_rel_linf_vs_plain"], 2),
-                        "id_err": _r(su["identity_rel_linf_vs_plain"], 2), "tc_frac": _r(su["tensor"]["frac"])}
+                        "id_err": _r(su["identity_rel_linf_vs_plain"], 2), "tc_frac": _r(su["tensor"]["frac"]),
+                        "held": _r(ho.get("rel_linf"), 2), "held_id": _r(ho.get("rel_linf_identity"), 2)}
     for key in ("shading", "caustics", "branched_flow", "foam_dynamics"):
         if line.get(key):
             out[key] = _r(line[key]["value"])

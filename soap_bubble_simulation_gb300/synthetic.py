@@ -65,9 +65,11 @@ def smooth_modes_window(full_nt: int, full_np: int, r0: int, c0: int, nt: int, n
 def surrogate_trajectories(count: int = 512, seed: int = 21, resolution: int = 256, fine: int = 2048):
     """Initial states of the surrogate's training trajectories on a resolution x 2 resolution grid.
 
-    Even k: a config-1 field at `resolution` (bubble_c1). Odd k: a resolution x 2 resolution window
-    of a config-1 field at `fine` (the cell-scale content - kinks where the clamp to [100, 1000] nm
-    bites, nearly flat smooth modes - that a `fine` field shows the network). Viscosity is
+    Even k: a config-1 field at `resolution` (bubble_c1). Odd k: a resolution x resolution window
+    of a config-1 field at `fine`, followed by its mirror image in phi, so the film is continuous
+    across the periodic phi seam (a plain window of a non-periodic patch would have a jump there
+    that no film on a sphere has); this shows the network the cell-scale content of a `fine`
+    field - kinks where the clamp to [100, 1000] nm bites, nearly flat smooth modes. Viscosity is
     log-uniform in [1e-4, 1e-2] Pa s and the diameter log-uniform in [3, 80] mm; the small end gives,
     at `resolution`, the per-cell diffusion numbers of 25-40 mm bubbles at `fine`.
     Yields (h f32, c f32, viscosity, radius)."""
@@ -82,7 +84,8 @@ def surrogate_trajectories(count: int = 512, seed: int = 21, resolution: int = 2
         else:
             r0 = int(g.integers(0, fine - nt + 1))
             c0 = int(g.integers(0, 2 * fine))
-            h = smooth_modes_window(fine, 2 * fine, r0, c0, nt, np_, seed=s).astype(np.float32)
+            w = smooth_modes_window(fine, 2 * fine, r0, c0, nt, np_ // 2, seed=s)
+            h = np.concatenate([w, w[:, ::-1]], axis=1).astype(np.float32)
         c = surfactant_noise(nt, np_, seed=s + 1)
         yield h, c, visc, radius
 

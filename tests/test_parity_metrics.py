@@ -41,3 +41,16 @@ def test_report_keys():
     r = parity.report(a, a, a)
     assert r["rel_linf"] == 0.0 and r["stable_rows"] == 30 and r["rows"] == 30
     assert set(r) >= {"rel_linf_cfl_rows", "rel_linf_stable_rows", "rel_linf_stable_rows_margin8", "rel_linf_sin_ge_0.2"}
+
+
+def test_surrogate_training_fields_are_continuous_across_the_phi_seam():
+    """Every training film is periodic in phi without a jump at the seam: a film on a sphere has
+    none, and a step there is a discontinuity that a 64-pass interval diffuses faster than the
+    network's 4-cell receptive field can follow."""
+    from soap_bubble_simulation_gb300 import synthetic
+
+    for k, (h, c, visc, rad) in enumerate(synthetic.surrogate_trajectories(6)):
+        seam = np.abs(h[:, 0].astype(np.float64) - h[:, -1]).max()
+        inner = np.abs(np.diff(h.astype(np.float64), axis=1)).max()
+        assert seam <= inner + 1e-15, (k, seam, inner)
+        assert h.shape == (256, 512) and 1e-4 <= visc <= 1e-2 and 0.0015 <= rad <= 0.04
