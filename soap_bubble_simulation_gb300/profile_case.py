@@ -34,7 +34,8 @@ def main(argv=None) -> None:
     p.add_argument("--points", type=int, default=1 << 20, help="spectral cases: number of points")
     p.add_argument("--res", type=int, default=2048)
     p.add_argument("--steps", type=int, default=20)
-    p.add_argument("--blocking", type=int, default=-1, help="WGSL steps per launch (default: library choice)")
+    p.add_argument("--blocking", type=int, default=-1,
+                   help="steps per launch, both semantics (default: library choice; 1 = single steps)")
     p.add_argument("--bubbles", type=int, default=4096, help="foam case: number of bubbles")
     p.add_argument("--activation", default="gelu", choices=["gelu", "hswish"], help="surrogate cases: activation")
     a = p.parse_args(argv)
@@ -134,6 +135,8 @@ def main(argv=None) -> None:
         sim = DrainageSimulator.__new__(DrainageSimulator)
         _Handle.__init__(sim)
         sim._h = hh
+        if a.blocking >= 0:
+            N.call("sbs_drainage_set_time_blocking", sim.handle, a.blocking)
         sim.set_thickness_array(h)
         sim.step_n(cfg.dt, a.steps)
     sim.close()

@@ -131,6 +131,34 @@ def test_cpu_time_blocking_bit_identical(sbs, orc, precision, res):
     assert results[0][2] == ref.active_tfe_count() >= 1
 
 
+@pytest.mark.parametrize("precision", ["f32x2", "f32"])
+@pytest.mark.parametrize("res", [1024, 1500])
+def test_cpu_single_steps_many_column_blocks(sbs, orc, precision, res):
+    """Single steps (K = 1) on grids of 2048 and 3000 columns (many column blocks, the last one
+    partly filled: 3000 = 5 x 512 + 440), the phi wrap at both ends, fronts active from step 50
+    (dt 0.01 s), volume checks: every cell equal to the kernel-order oracle."""
+    from soap_bubble_simulation_gb300 import synthetic
+
+    h0 = synthetic.smooth_modes(res, 2 * res, seed=res)
+    if precision == "f32":
+        h0 = h0.astype(np.float32).astype(np.float64)
+    sim = make_sim(sbs, res, precision)
+    set_cpu_blocking(sbs, sim, 1)
+    set64(sbs, sim, h0)
+    sim.step_n(0.01, 47)
+    vols = sim.run_checked(0.01, 16, 8)
+    ref = orc.CpuSim(resolution=res, precision=ORC_PREC[precision], threads=0)
+    ref.set_field(h0)
+    ref.step_n(0.01, 55)
+    v0 = orc.film_volume(ref.field(), 0.025)
+    ref.step_n(0.01, 8)
+    got, want = field64(sbs, sim), ref.field()
+    assert sim.active_tfe_count() == ref.active_tfe_count() >= 1
+    np.testing.assert_array_equal(got, want)
+    assert vols[0] == pytest.approx(v0, rel=1e-12)
+    assert vols[1] == pytest.approx(orc.film_volume(want, 0.025), rel=1e-12)
+
+
 def test_cpu_time_blocking_needs_even_resolution(sbs):
     sim = make_sim(sbs, 33)  # 66 columns: not a multiple of 4
     assert cpu_blocking(sbs, sim) == 1
