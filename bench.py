@@ -279,16 +279,23 @@ def launches_per_run(k: int) -> int:
 
 
 def surrogate_section(sbs, synthetic, h0, c0, torch, activations=("gelu", "hswish")):
-    """C4: train on 512 plain trajectories at 256 x 512, then the checked 10,000-step rollout, once per
-    activation (GELU, the network's default, and hard-swish) from the same initial weights and data."""
+    """C4: train on 480 plain trajectories at 256 x 512 (config-1 fields, mirrored and step windows of
+    2048-resolution fields), evaluate on 24 held-out continuous and 8 held-out step trajectories, then
+    the checked 10,000-step rollout, once per activation (GELU, the network's default, and hard-swish)
+    from the same initial weights and data."""
     nt, np_ = h0.shape
     cells = h0.size
     s = sbs.DrainageSurrogate(seed=7)
     theta0 = s.params
     t0 = time.perf_counter()
-    ntraj = 512
-    for h, c, visc, rad in synthetic.surrogate_trajectories(ntraj):
-        s.add_trajectory(h, c, sbs.field_params(256, 512, viscosity=visc, bubble_radius=rad), pairs=4)
+    ntrain, nheld, nstep = 480, 24, 8
+    ntraj = ntrain + nheld + nstep
+    # training trajectories of every kind, then held-out continuous films (config-1 fields and
+    # mirrored windows) and held-out step windows, each a contiguous block for evaluate()
+    sets = ((ntrain, 21, synthetic.SURROGATE_KINDS), (nheld, 22, ("c1", "mirror")), (nstep, 23, ("step",)))
+    for count, seed, kinds in sets:
+        for h, c, visc, rad in synthetic.surrogate_trajectories(count, seed=seed, kinds=kinds):
+            s.add_trajectory(h, c, sbs.field_params(256, 512, viscosity=visc, bubble_radius=rad), pairs=4)
     data_s = time.perf_counter() - t0
     p = sbs.field_params(nt, np_, bubble_radius=0.025)
 
@@ -323,10 +330,11 @@ def surrogate_section(sbs, synthetic, h0, c0, torch, activations=("gelu", "hswis
         s.activation = act
         s.params = theta0  # same start for every activation (also resets the optimiser state)
         t1 = time.perf_counter()
-        losses = s.train(ntraj - 32, iters, batch=8, lr=2e-3, seed=5)
+        losses = s.train(ntrain, iters, batch=8, lr=2e-3, seed=5)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
-        ev = s.evaluate(ntraj - 32, 32, mode="fused")
+        ev = s.evaluate(ntrain, nheld, mode="fused")
+        ev_step = s.evaluate(ntrain + nheld, nstep, mode="fused")
         # fused forward pass alone (one 64-pass interval)
         sim = fresh()
         for _ in range(3):
@@ -358,10 +366,12 @@ def surrogate_section(sbs, synthetic, h0, c0, torch, activations=("gelu", "hswis
             "fused_interval_cell_steps_per_s": cells * 64 / (fused_ms * 1e-3),
             "tensor": {"bound": "tensor", "achieved": tflops, "peak": tf_peak, "unit": "TFLOP/s",
                        "frac": tflops / tf_peak, "flop_per_cell": flop_cell, "peak_kind": "measured bf16 burst"},
-            "train": {"trajectories": ntraj, "grid": "256 x 512", "pairs_per_trajectory": 4, "iters": iters,
+            "train": {"trajectories": ntrain, "kinds": list(synthetic.SURROGATE_KINDS), "grid": "256 x 512",
+                      "pairs_per_trajectory": 4, "iters": iters,
                       "batch": 8, "data_s": data_s, "train_s": t2 - t1, "loss_first": float(losses[:10].mean()),
                       "loss_last": float(losses[-50:].mean())},
-            "heldout_256": ev}
+            "heldout_256": {**ev, "trajectories": nheld, "kinds": ["c1", "mirror"]},
+            "heldout_256_step": {**ev_step, "trajectories": nstep, "kinds": ["step"]}}
     s.close()
     return results
 
@@ -791,7 +801,8 @@ def summary(line: dict) -> dict:
             ho = su.get("heldout_256") or {}
             out[key] = {"x_plain": _r(su["speedup_vs_plain"]), "err": _r(su["masked_rel_linf_vs_plain"], 2),
                         "id_err": _r(su["identity_rel_linf_vs_plain"], 2), "tc_frac": _r(su["tensor"]["frac"]),
-                        "held": _r(ho.get("rel_linf"), 2), "held_id": _r(ho.get("rel_linf_identity"), 2)}
+                        "held": _r(ho.get("rel_linf"), 2), "held_id": _r(ho.get("rel_linf_identity"), 2),
+                        "fail": (su.get("stats") or {}).get("failed_checks")}
     for key in ("shading", "caustics", "branched_flow", "foam_dynamics"):
         if line.get(key):
             out[key] = _r(line[key]["value"])

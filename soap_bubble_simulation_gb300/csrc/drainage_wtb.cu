@@ -41,9 +41,10 @@ __device__ __forceinline__ double wtb_block_sum(double v, double *smem) {
     return t;
 }
 
-// At least three blocks per SM: caps the K = 4 pipeline at 168 registers. Measured at 2048 x 4096
-// (4000 steps): 13.95 us per step against 14.98 with the compiler's own 166-register allocation;
-// four blocks (128 registers, spills) 15.49.
+// At least three blocks per SM: caps the K = 4 pipeline at 168 registers (164-168 used, 12 warps
+// per SM). Left to itself the compiler allocates 188-198 registers, two blocks per SM fit, and the
+// 2048 x 4096 step takes 14.84 us against 13.84 (median of 7 x 2048 steps, measured A/B/A in one
+// process each); four blocks (128 registers, spills) 15.49.
 constexpr int kMinBlocksPerSm = 3;
 
 template <int K, bool VOL, bool MAR>

@@ -62,30 +62,50 @@ def smooth_modes_window(full_nt: int, full_np: int, r0: int, c0: int, nt: int, n
     return np.clip(h, kw.get("lo", 100e-9), kw.get("hi", 1000e-9))
 
 
-def surrogate_trajectories(count: int = 512, seed: int = 21, resolution: int = 256, fine: int = 2048):
+SURROGATE_KINDS = ("c1", "step", "c1", "mirror")
+
+
+def surrogate_trajectories(count: int = 512, seed: int = 21, resolution: int = 256, fine: int = 2048,
+                           kinds: tuple[str, ...] = SURROGATE_KINDS):
     """Initial states of the surrogate's training trajectories on a resolution x 2 resolution grid.
 
-    Even k: a config-1 field at `resolution` (bubble_c1). Odd k: a resolution x resolution window
-    of a config-1 field at `fine`, followed by its mirror image in phi, so the film is continuous
-    across the periodic phi seam (a plain window of a non-periodic patch would have a jump there
-    that no film on a sphere has); this shows the network the cell-scale content of a `fine`
-    field - kinks where the clamp to [100, 1000] nm bites, nearly flat smooth modes. Viscosity is
-    log-uniform in [1e-4, 1e-2] Pa s and the diameter log-uniform in [3, 80] mm; the small end gives,
-    at `resolution`, the per-cell diffusion numbers of 25-40 mm bubbles at `fine`.
+    Trajectory k is of kind kinds[k % len(kinds)]:
+    * "c1": a config-1 field at `resolution` (bubble_c1);
+    * "mirror": a resolution x resolution window of a config-1 field at `fine`, followed by its
+      mirror image in phi, so the film is continuous across the periodic phi seam; this shows the
+      network the cell-scale content of a `fine` field - kinks where the clamp to [100, 1000] nm
+      bites, nearly flat smooth modes;
+    * "step": a resolution x 2 resolution window of a config-1 field at `fine`, whose two ends meet
+      at the phi seam with a jump of up to a few hundred nm. No film on a sphere has such a step;
+      it is the largest gradient in the data and teaches the network the response to a sharp
+      feature. A network trained without it under-predicts the drainage at the clamp kinks of the
+      2048 x 4096 field: in the 10,000-step checked rollout there 4-9 of 20 checks fail (largest
+      check error 3e-3 - 1e-2), against none (largest 6e-5) with it. A 64-pass interval diffuses
+      the step itself further than the network's 4-cell receptive field reaches, so held-out error
+      is reported for step and continuous trajectories apart.
+    Viscosity is log-uniform in [1e-4, 1e-2] Pa s and the diameter log-uniform in [3, 80] mm; the
+    small end gives, at `resolution`, the per-cell diffusion numbers of 25-40 mm bubbles at `fine`.
     Yields (h f32, c f32, viscosity, radius)."""
+    for kind in kinds:
+        if kind not in ("c1", "mirror", "step"):
+            raise ValueError(f"unknown trajectory kind {kind!r}")
     g = rng(seed)
     nt, np_ = resolution, 2 * resolution
     for k in range(count):
+        kind = kinds[k % len(kinds)]
         visc = float(10 ** g.uniform(-4.0, -2.0))
         radius = float(0.5 * 10 ** g.uniform(math.log10(0.003), math.log10(0.08)))
         s = int(g.integers(0, 2**31 - 1))
-        if k % 2 == 0:
+        if kind == "c1":
             h = smooth_modes(nt, np_, seed=s).astype(np.float32)
         else:
             r0 = int(g.integers(0, fine - nt + 1))
             c0 = int(g.integers(0, 2 * fine))
-            w = smooth_modes_window(fine, 2 * fine, r0, c0, nt, np_ // 2, seed=s)
-            h = np.concatenate([w, w[:, ::-1]], axis=1).astype(np.float32)
+            if kind == "mirror":
+                w = smooth_modes_window(fine, 2 * fine, r0, c0, nt, np_ // 2, seed=s)
+                h = np.concatenate([w, w[:, ::-1]], axis=1).astype(np.float32)
+            else:
+                h = smooth_modes_window(fine, 2 * fine, r0, c0, nt, np_, seed=s).astype(np.float32)
         c = surfactant_noise(nt, np_, seed=s + 1)
         yield h, c, visc, radius
 

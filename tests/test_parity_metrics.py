@@ -2,6 +2,7 @@
 import math
 
 import numpy as np
+import pytest
 
 
 def test_rel_linf_and_masks():
@@ -43,14 +44,22 @@ def test_report_keys():
     assert set(r) >= {"rel_linf_cfl_rows", "rel_linf_stable_rows", "rel_linf_stable_rows_margin8", "rel_linf_sin_ge_0.2"}
 
 
-def test_surrogate_training_fields_are_continuous_across_the_phi_seam():
-    """Every training film is periodic in phi without a jump at the seam: a film on a sphere has
-    none, and a step there is a discontinuity that a 64-pass interval diffuses faster than the
-    network's 4-cell receptive field can follow."""
+def test_surrogate_training_kinds():
+    """Config-1 fields and mirrored windows are periodic in phi without a jump at the seam (a film
+    on a sphere has none); step windows keep the jump where their two ends meet."""
     from soap_bubble_simulation_gb300 import synthetic
 
-    for k, (h, c, visc, rad) in enumerate(synthetic.surrogate_trajectories(6)):
+    kinds = synthetic.SURROGATE_KINDS
+    assert set(kinds) == {"c1", "mirror", "step"}
+    for k, (h, c, visc, rad) in enumerate(synthetic.surrogate_trajectories(8)):
         seam = np.abs(h[:, 0].astype(np.float64) - h[:, -1]).max()
         inner = np.abs(np.diff(h.astype(np.float64), axis=1)).max()
-        assert seam <= inner + 1e-15, (k, seam, inner)
+        if kinds[k % len(kinds)] == "step":
+            assert seam > 4 * inner, (k, seam, inner)
+        else:
+            assert seam <= inner + 1e-15, (k, seam, inner)
         assert h.shape == (256, 512) and 1e-4 <= visc <= 1e-2 and 0.0015 <= rad <= 0.04
+    for h, *_ in synthetic.surrogate_trajectories(3, seed=5, kinds=("mirror",)):
+        assert np.array_equal(h[:, :256], h[:, 256:][:, ::-1])
+    with pytest.raises(ValueError):
+        next(synthetic.surrogate_trajectories(1, kinds=("ring",)))
