@@ -66,8 +66,9 @@ const char *sbs_version(void);
 int sbs_device_count(int *out);
 
 /* Bounded device-side waits (no reference counterpart). Every wait inside this
- * library's kernels - the foam batch's grid barrier, the mbarrier waits of the
- * tensor-core spectral contraction and of the fused surrogate kernel - gives up
+ * library's kernels - the foam batch's grid barrier, the pole-ring barrier of the
+ * blocked DrainageSimulator step, the mbarrier waits of the tensor-core spectral
+ * contraction and of the fused surrogate kernel - gives up
  * after `cycles` SM clock cycles (default 2e9, about one second): the kernel
  * records the timeout, finishes its outstanding tensor-core work, frees its
  * tensor memory and exits, and the call returns SBS_E_TIMEOUT; the context and
@@ -80,8 +81,9 @@ int sbs_wait_limit(uint64_t *out);
  * bounded waits of later launches unsatisfiable without faulting anything.
  * SBS_STALL_TENSOR_COMMITS: the tensor-core kernels issue neither their MMAs
  * nor the commits that signal them, so nothing asynchronous is in flight when
- * the waits expire. SBS_STALL_GRID_BARRIER: the foam kernel's grid barrier
- * expects one arrival more than the grid has. 0 (the default) turns both off.
+ * the waits expire. SBS_STALL_GRID_BARRIER: the foam kernel's grid barrier and
+ * the pole-ring barrier of the blocked DrainageSimulator step expect one arrival
+ * more than there are blocks. 0 (the default) turns both off.
  * Process-wide; meant for tests, which set a short wait limit first. */
 #define SBS_STALL_TENSOR_COMMITS 1
 #define SBS_STALL_GRID_BARRIER 2
@@ -267,11 +269,12 @@ int sbs_gpu_drainage_set_time_blocking(sbs_drainage *h, int steps_per_launch);
 int sbs_gpu_drainage_time_blocking(const sbs_drainage *h, int *out);
 /* The same for a handle of either semantics (no reference counterpart). For the
  * DrainageSimulator semantics 2..4 steps per launch advance the stencil, the
- * pole-ring means and the marginal-regeneration fronts K steps at a time (each
- * row strip one thread-block cluster spanning the ring); it needs an even
- * resolution and at least 2 (K + 1) theta rows. Results are bit-identical to
- * single steps. Default where supported: 2 for the compensated f32x2 storage,
- * 4 for plain f32 (WGSL semantics: 4). */
+ * pole-ring means and the marginal-regeneration fronts K steps at a time (row
+ * strips of blocks spanning the ring, all resident at once; the two polar
+ * strips meet at a bounded barrier per ring mean, see sbs_set_wait_limit); it
+ * needs an even resolution and at least 2 (K + 1) theta rows. Results are
+ * bit-identical to single steps. Default where supported: 3 for the
+ * compensated f32x2 storage, 4 for plain f32 (WGSL semantics: 4). */
 int sbs_drainage_set_time_blocking(sbs_drainage *h, int steps_per_launch);
 int sbs_drainage_time_blocking(const sbs_drainage *h, int *out);
 

@@ -168,19 +168,85 @@ void stencil_f32k(orc_sim *s, double dt) {
     }
 }
 
-// Compensated (TwoSum) summation in f64 of a ring's values.
-double ring_sum(const orc_sim *s, uint32_t row) {
-    double sum = 0.0, comp = 0.0;
-    for (uint32_t j = 0; j < s->np; ++j) {
-        double x = (double)s->hf[(size_t)row * s->np + j];
-        if (s->precision == 2) x += (double)s->lf[(size_t)row * s->np + j];
-        double t = sum + x;
-        double bb = t - sum;
-        double e = (sum - (t - bb)) + (x - bb);
-        sum = t;
-        comp += e;
+// Kernel order of a ring sum: every f32 word (the thickness, plus the low word in the
+// compensated storage) as a two's-complement integer in units of 2^-96 m, truncated toward
+// zero, summed exactly in 256 bits (wide enough for any finite f32 word); the total rounded to
+// the nearest double (ties to even). An infinite or NaN word makes the sum NaN. Integer addition
+// does not depend on the order, so this equals the kernels' per-lane / per-warp / per-block
+// groupings bit for bit.
+struct Wide {
+    unsigned __int128 lo = 0, hi = 0;  // two's complement, 256 bits
+};
+
+void wide_add(Wide &a, unsigned __int128 lo, unsigned __int128 hi) {
+    const unsigned __int128 s = a.lo + lo;
+    a.hi = a.hi + hi + (s < lo ? 1 : 0);
+    a.lo = s;
+}
+
+bool fix_word(float x, Wide &acc) {
+    if (!std::isfinite(x)) return false;
+    if (x == 0.0f) return true;
+    int e = 0;
+    const float fr = std::frexp(x, &e);                        // x = fr 2^e, 0.5 <= |fr| < 1
+    const long long m = (long long)std::ldexp((double)fr, 24); // exact: 24 significant bits
+    const int sh = e - 24 + 96;                                // x = m 2^(sh - 96)
+    const unsigned __int128 mag = (unsigned __int128)(m < 0 ? -m : m);
+    unsigned __int128 lo = 0, hi = 0;
+    if (sh < 0)
+        lo = sh <= -64 ? 0 : mag >> -sh;
+    else if (sh < 128) {
+        lo = mag << sh;
+        hi = sh > 104 ? mag >> (128 - sh) : 0;
+    } else {
+        hi = mag << (sh - 128);
     }
-    return sum + comp;
+    if (m < 0) {
+        lo = ~lo + 1;
+        hi = ~hi + (lo == 0 ? 1 : 0);
+    }
+    wide_add(acc, lo, hi);
+    return true;
+}
+
+bool wide_bit(const Wide &v, int i) { return i < 128 ? ((v.lo >> i) & 1) != 0 : ((v.hi >> (i - 128)) & 1) != 0; }
+
+double fix_total_to_double(Wide v) {
+    const bool neg = (v.hi >> 127) != 0;
+    if (neg) {
+        v.lo = ~v.lo + 1;
+        v.hi = ~v.hi + (v.lo == 0 ? 1 : 0);
+    }
+    int nbits = 0;
+    for (int i = 255; i >= 0; --i)
+        if (wide_bit(v, i)) {
+            nbits = i + 1;
+            break;
+        }
+    unsigned long long q = 0;
+    int drop = 0;
+    if (nbits <= 53) {
+        q = (unsigned long long)v.lo;
+    } else {
+        drop = nbits - 53;
+        for (int i = nbits - 1; i >= drop; --i) q = (q << 1) | (wide_bit(v, i) ? 1ull : 0ull);
+        const bool round = wide_bit(v, drop - 1);
+        bool sticky = false;
+        for (int i = drop - 2; i >= 0 && !sticky; --i) sticky = wide_bit(v, i);
+        if (round && (sticky || (q & 1))) q += 1;  // round half to even
+    }
+    const double d = std::ldexp((double)q, drop - 96);
+    return neg ? -d : d;
+}
+
+double ring_sum(const orc_sim *s, uint32_t row) {
+    Wide tot;
+    bool ok = true;
+    for (uint32_t j = 0; j < s->np; ++j) {
+        if (!fix_word(s->hf[(size_t)row * s->np + j], tot)) ok = false;
+        if (s->precision == 2 && !fix_word(s->lf[(size_t)row * s->np + j], tot)) ok = false;
+    }
+    return ok ? fix_total_to_double(tot) : std::nan("");
 }
 
 // update_poles (drainage.rs:480-503): ring means in f64, sequential order.
@@ -195,7 +261,7 @@ void update_poles(orc_sim *s) {
         double ba = bot / (double)np;
         for (uint32_t j = 0; j < np; ++j) s->h[(size_t)last * np + j] = ba;
     } else {
-        // kernel order: compensated ring sums, mean in f64, stored rounded (f32) or split (f32x2)
+        // kernel order: exact fixed-point ring sums, mean in f64, stored rounded (f32) or split (f32x2)
         const double mt = ring_sum(s, 1) / (double)np;
         const double mb = ring_sum(s, last - 1) / (double)np;
         const float th = (float)mt, bh = (float)mb;
@@ -397,6 +463,15 @@ double orc_sim_get_thickness(const orc_sim *s, double theta, double phi) {
 }
 
 double orc_sim_current_time(const orc_sim *s) { return s->current_time; }
+
+// The kernels' exact ring mean of n f32 words (kernel-order pole means) over a ring of np cells.
+double orc_fix_ring_mean(const float *words, size_t n, uint32_t np) {
+    Wide tot;
+    bool ok = true;
+    for (size_t j = 0; j < n; ++j)
+        if (!fix_word(words[j], tot)) ok = false;
+    return ok ? fix_total_to_double(tot) / (double)np : std::nan("");
+}
 
 double orc_sim_min_thickness(const orc_sim *s) {
     double m = INFINITY;

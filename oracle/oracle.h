@@ -65,6 +65,7 @@ double orc_sim_get_thickness(const orc_sim *s, double theta, double phi);
 double orc_sim_current_time(const orc_sim *s);
 int orc_sim_has_critical_region(const orc_sim *s);
 double orc_sim_min_thickness(const orc_sim *s);
+double orc_fix_ring_mean(const float *words, size_t n, uint32_t np);
 double orc_sim_max_thickness(const orc_sim *s);
 void orc_sim_reset(orc_sim *s, double h0);
 void orc_sim_set_marginal_regeneration(orc_sim *s, int enabled);

@@ -74,6 +74,7 @@ _SIGS = {
     "orc_sim_current_time": ([_P], _D),
     "orc_sim_has_critical_region": ([_P], _I),
     "orc_sim_min_thickness": ([_P], _D),
+    "orc_fix_ring_mean": ([_P, C.c_size_t, C.c_uint32], _D),
     "orc_sim_max_thickness": ([_P], _D),
     "orc_sim_reset": ([_P, _D], None),
     "orc_sim_set_marginal_regeneration": ([_P, _I], None),
@@ -570,3 +571,9 @@ def foam_step(physics, dt: float, steps: int, position, radius, velocity=None, t
 FOAM_CONNECTION = np.dtype([("bubble_a", np.uint32), ("bubble_b", np.uint32), ("contact_point", np.float32, 3),
                             ("contact_normal", np.float32, 3), ("wall_curvature_radius", np.float32),
                             ("wall_thickness_nm", np.float32)])
+
+
+def fix_ring_mean(words, np_):
+    """The kernels' exact pole-ring mean of f32 words over a ring of np_ cells."""
+    a = np.ascontiguousarray(words, dtype=np.float32).reshape(-1)
+    return lib().orc_fix_ring_mean(_p(a), a.size, int(np_))

@@ -239,15 +239,15 @@ int allocate(sbs_drainage *h) {
         h->wgeom = wtb_geometry(h->nt, h->np, h->wtb_k);
     }
     if (h->sem == SBS_CPU_SEMANTICS) {
-        // steps per launch measured fastest at 2048 x 4096: 2 for the compensated storage (its
-        // register windows grow with K and cost warps), 4 for plain f32
-        const int k = h->x2 ? 2 : 4;
+        // steps per launch measured fastest at 2048 x 4096: 3 for the compensated storage (19.7 us
+        // per step; K = 2 20.2, K = 4 spills), 4 for plain f32 (10.7 us)
+        const int k = h->x2 ? 3 : 4;
         h->cgeom = wtbc_geometry(h->nt, h->np, k, h->x2);
         if (h->cgeom.nby > 0) h->cpu_k = k;
     }
     for (int i = 0; i < 2; ++i) {
-        SBS_CUDA_TRY(cudaMalloc(&h->part[i], sizeof(double) * 4 * h->geom.nbx));
-        SBS_CUDA_TRY(cudaMemset(h->part[i], 0, sizeof(double) * 4 * h->geom.nbx));
+        SBS_CUDA_TRY(cudaMalloc(&h->part[i], sizeof(FixSum) * 2 * h->geom.nbx));
+        SBS_CUDA_TRY(cudaMemset(h->part[i], 0, sizeof(FixSum) * 2 * h->geom.nbx));
     }
     SBS_CUDA_TRY(cudaMalloc(&h->rows, sizeof(float4) * h->nt));
     SBS_CUDA_TRY(cudaMalloc(&h->vol_w, sizeof(double) * h->nt));
@@ -258,11 +258,21 @@ int allocate(sbs_drainage *h) {
             const StepGeom g = wtb_geometry(h->nt, h->np, k);
             vol_blocks = std::max(vol_blocks, (size_t)g.nbx * g.nby);
         }
-    if (h->sem == SBS_CPU_SEMANTICS)
+    if (h->sem == SBS_CPU_SEMANTICS) {
+        size_t parts = 1;
         for (int k = 2; k <= 4; ++k) {
             const StepGeom g = wtbc_geometry(h->nt, h->np, k, h->x2);
             vol_blocks = std::max(vol_blocks, (size_t)g.nbx * g.nby);
+            parts = std::max(parts, (size_t)wtbc_ring_parts(g));
         }
+        SBS_CUDA_TRY(cudaMalloc(&h->ring_part, sizeof(FixSum) * 2 * 4 * parts));
+        SBS_CUDA_TRY(cudaMalloc(&h->ring_bar, sizeof(unsigned) * kWtbcBarWords));
+        SBS_CUDA_TRY(cudaMemset(h->ring_bar, 0, sizeof(unsigned) * kWtbcBarWords));
+        SBS_CUDA_TRY(cudaHostAlloc(&h->ring_status, sizeof(unsigned), cudaHostAllocMapped));
+        *h->ring_status = 0u;
+        SBS_CUDA_TRY(cudaHostGetDevicePointer(&h->ring_status_dev, h->ring_status, 0));
+        h->wait_epoch = wait_config().epoch;
+    }
     SBS_CUDA_TRY(cudaMalloc(&h->vol_partials, sizeof(double) * vol_blocks));
     SBS_CUDA_TRY(cudaMalloc(&h->vol_counter, sizeof(unsigned) * 2));
     SBS_CUDA_TRY(cudaMemset(h->vol_counter, 0, sizeof(unsigned) * 2));
@@ -303,6 +313,9 @@ void release(sbs_drainage *h) {
     cudaFree(h->red_out);
     cudaFree(h->sched_dev);
     cudaFree(h->qbuf);
+    cudaFree(h->ring_part);
+    cudaFree(h->ring_bar);
+    if (h->ring_status) cudaFreeHost(h->ring_status);
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -350,6 +363,15 @@ int enqueue_steps(sbs_drainage *h, int start, int count, float dt, bool vol_last
             a.b = k.b;
             a.DR2 = k.DR2;
             a.dt = dt;
+            a.prow = h->cgeom.prow;
+            a.ring_part = h->ring_part;
+            a.ring_bar = h->ring_bar;
+            a.status_host = h->ring_status_dev;
+            {
+                const WaitConfig wc = wait_config();
+                a.wait_cycles = wc.cycles;
+                a.extra = (wc.stall & SBS_STALL_GRID_BARRIER) ? 1u : 0u;
+            }
             if (blocked)
                 SBS_CUDA_TRY(launch_wtbc(K, h->x2, a, h->cgeom, h->stream));
             else
@@ -493,9 +515,27 @@ int run_chunk(sbs_drainage *h, int count, double dt, bool vol_last, bool last_si
     return SBS_OK;
 }
 
+// After the stream has drained: a timed-out ring barrier of the blocked CPU-semantics step turns
+// into SBS_E_TIMEOUT, and the barrier words are cleared for the next call.
+int check_ring_status(sbs_drainage *h) {
+    if (!h->ring_status || *(volatile unsigned *)h->ring_status == 0u) return SBS_OK;
+    *(volatile unsigned *)h->ring_status = 0u;
+    SBS_CUDA_TRY(cudaMemsetAsync(h->ring_bar, 0, sizeof(unsigned) * kWtbcBarWords, h->stream));
+    SBS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return set_error(SBS_E_TIMEOUT, "drainage: a pole-ring barrier wait timed out");
+}
+
 // Advances n steps in chunks; a volume check follows every check_every-th step (0 = none).
 int run_steps(sbs_drainage *h, double dt, uint64_t n, uint32_t check_every) {
     if (h->tfe.error) return set_error(SBS_E_STATE, "TFE front columns are not one interval");
+    if (h->ring_bar) {
+        const unsigned epoch = wait_config().epoch;
+        if (epoch != h->wait_epoch) {  // the launches carry the wait settings: capture them again
+            SBS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+            destroy_graphs(h);
+            h->wait_epoch = epoch;
+        }
+    }
     uint64_t done = 0;
     while (done < n) {
         uint64_t g = std::min<uint64_t>(kMaxChunk, n - done);
@@ -703,7 +743,7 @@ int sbs_drainage_step_n(sbs_drainage *h, double dt, uint32_t n) {
     int rc = run_steps(h, dt, n, 0);
     if (rc) return rc;
     SBS_CUDA_TRY(cudaStreamSynchronize(h->stream));
-    return SBS_OK;
+    return check_ring_status(h);
 }
 
 int sbs_gpu_drainage_step(sbs_drainage *h, float frame_dt) {
@@ -753,7 +793,7 @@ int sbs_drainage_run_checked(sbs_drainage *h, double dt, uint32_t n, uint32_t ch
         SBS_CUDA_TRY(cudaMemcpyAsync(volumes_out, h->vol_out, sizeof(double) * nchecks, cudaMemcpyDeviceToHost,
                                      h->stream));
     SBS_CUDA_TRY(cudaStreamSynchronize(h->stream));
-    return SBS_OK;
+    return check_ring_status(h);
 }
 
 int sbs_drainage_set_thickness(sbs_drainage *h, const float *src, size_t n, int mem) {

@@ -54,20 +54,6 @@ __device__ __forceinline__ void setk(float4 &v, int k, float x) {
         v.w = x;
 }
 
-// Error-free sum of two doubles (Knuth TwoSum): a + b == s + e exactly.
-__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e) {
-    s = a + b;
-    const double bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
-
-// Compensated accumulation: (s, c) += x.
-__device__ __forceinline__ void comp_add(double &s, double &c, double x) {
-    double e;
-    two_sum(s, x, s, e);
-    c += e;
-}
-
 // Sum of a double over the block, deterministic order; result valid in thread 0.
 __device__ double block_sum(double v, double *smem) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -82,43 +68,27 @@ __device__ double block_sum(double v, double *smem) {
     return t;
 }
 
-// Compensated sum (s, c) over the block; result valid in thread 0.
-__device__ void block_comp_sum(double &s, double &c, double *smem /*2*32*/) {
+// Exact fixed-point sum over the block (fixsum.cuh); result valid in thread 0.
+__device__ void block_fix_sum(FixSum &a, FixSum *smem /*32*/) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const double s2 = __shfl_xor_sync(kFull, s, o), c2 = __shfl_xor_sync(kFull, c, o);
-        double e;
-        two_sum(s, s2, s, e);
-        c = c + c2 + e;
-    }
-    if (lane == 0) {
-        smem[2 * warp] = s;
-        smem[2 * warp + 1] = c;
-    }
+    fix_warp(a);
+    if (lane == 0) smem[warp] = a;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double ts = 0.0, tc = 0.0;
-        for (int i = 0; i < nw; ++i) {
-            double e;
-            two_sum(ts, smem[2 * i], ts, e);
-            tc = tc + smem[2 * i + 1] + e;
-        }
-        s = ts;
-        c = tc;
+        FixSum t = fix_zero();
+        for (int i = 0; i < nw; ++i) fix_add(t, smem[i]);
+        a = t;
     }
     __syncthreads();
 }
 
-// Mean of a pole ring from its per-block compensated partial sums (s, c pairs, fixed order).
-__device__ __forceinline__ double ring_mean(const double *part, int nbx, int np) {
-    double s = 0.0, c = 0.0;
+// Mean of a pole ring from its per-block partial sums.
+__device__ __forceinline__ double ring_mean(const FixSum *part, int nbx, int np) {
+    FixSum t = fix_zero();
     for (int b = 0; b < nbx; ++b) {
-        double e;
-        two_sum(s, __ldcg(part + 2 * b), s, e);
-        c = c + __ldcg(part + 2 * b + 1) + e;
+        fix_add(t, fix_ldcg(part + b));
     }
-    return (s + c) / (double)np;
+    return fix_to_double(t) / (double)np;
 }
 
 // Phi neighbours of the four cells c..c+3 of row `rowp` whose values are v (all lanes call).
@@ -141,6 +111,7 @@ __device__ __forceinline__ void phi_neighbors(const float *rowp, const float4 &v
 template <int SEM, int X2, bool VOL, bool MAR = false>
 __global__ void __launch_bounds__(kBlockThreadsMax) drain_step_kernel(const StepArgs a) {
     __shared__ double s_red[64];
+    __shared__ FixSum s_fix[32];
     __shared__ TfeStep s_tfe;
     __shared__ int s_last;
     constexpr bool CPU = SEM == SBS_CPU_SEMANTICS;
@@ -173,7 +144,7 @@ __global__ void __launch_bounds__(kBlockThreadsMax) drain_step_kernel(const Step
             ptop_lo = (float)(m - (double)ptop);
         }
         if (r1 == nt - 1) {
-            const double m = ring_mean(a.pin + 2 * nbx, nbx, np);
+            const double m = ring_mean(a.pin + nbx, nbx, np);
             pbot = (float)m;
             pbot_lo = (float)(m - (double)pbot);
         }
@@ -235,7 +206,7 @@ __global__ void __launch_bounds__(kBlockThreadsMax) drain_step_kernel(const Step
                 if (r >= s_tfe.fr[f].x && r <= s_tfe.fr[f].y) fmask |= 1u << f;
 
         float4 outh, outl = splat4(0.f), outc = splat4(0.f);
-        double ring_s = 0.0, ring_c = 0.0;
+        FixSum ring = fix_zero();
         float4 wh4, wc4;
         if (WGSL)
             wgsl_cell4<MAR>(hc, hp, hn, hpm, hpp, cc, cp, cn, cpm, cpp, co, b, DR2, a.DsR2, a.Gt, a.M, dt, crit, wh4,
@@ -250,7 +221,10 @@ __global__ void __launch_bounds__(kBlockThreadsMax) drain_step_kernel(const Step
             if (WGSL) vc = getk(wc4, k);
             if (X2) vl = getk(wc4, k);
             if (CPU) {
-                if (ring_row && valid) comp_add(ring_s, ring_c, (double)vh + (double)vl);
+                if (ring_row && valid) {
+                    fix_add_float(ring, vh);
+                    if (X2) fix_add_float(ring, vl);
+                }
                 if (fmask) {
                     const int col = c + k;
                     for (int f = 0; f < nf; ++f) {
@@ -287,16 +261,10 @@ __global__ void __launch_bounds__(kBlockThreadsMax) drain_step_kernel(const Step
         }
         if (CPU && (r == 1 || r == nt - 2)) {
             // block-uniform branch: every thread of the block walks the same rows
-            block_comp_sum(ring_s, ring_c, s_red);
+            block_fix_sum(ring, s_fix);
             if (threadIdx.x == 0) {
-                if (r == 1) {
-                    a.pout[2 * blockIdx.x] = ring_s;
-                    a.pout[2 * blockIdx.x + 1] = ring_c;
-                }
-                if (r == nt - 2) {
-                    a.pout[2 * (gridDim.x + blockIdx.x)] = ring_s;
-                    a.pout[2 * (gridDim.x + blockIdx.x) + 1] = ring_c;
-                }
+                if (r == 1) a.pout[blockIdx.x] = ring;
+                if (r == nt - 2) a.pout[gridDim.x + blockIdx.x] = ring;
             }
         }
         hp = hc;
@@ -342,7 +310,7 @@ __global__ void __launch_bounds__(kBlockThreadsMax) drain_step_kernel(const Step
             if (threadIdx.x == 0) {
                 if (CPU) {
                     const double mt = ring_mean(a.pout, gridDim.x, np);
-                    const double mb = ring_mean(a.pout + 2 * gridDim.x, gridDim.x, np);
+                    const double mb = ring_mean(a.pout + gridDim.x, gridDim.x, np);
                     const float mth = (float)mt, mbh = (float)mb;
                     // the pole rows hold the split (or rounded) means
                     const double vt = X2 ? (double)mth + (double)(float)(mt - (double)mth) : (double)mth;
@@ -359,11 +327,11 @@ __global__ void __launch_bounds__(kBlockThreadsMax) drain_step_kernel(const Step
     }
 }
 
-__global__ void finalize_poles_kernel(float *h, float *hl, const double *part, int nbx, int nt, int np, int pitch) {
+__global__ void finalize_poles_kernel(float *h, float *hl, const FixSum *part, int nbx, int nt, int np, int pitch) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= np) return;
     const double mt = ring_mean(part, nbx, np);
-    const double mb = ring_mean(part + 2 * nbx, nbx, np);
+    const double mb = ring_mean(part + nbx, nbx, np);
     const float th = (float)mt, bh = (float)mb;
     h[j] = th;
     h[(size_t)(nt - 1) * pitch + j] = bh;
@@ -615,7 +583,7 @@ cudaError_t launch_step(int semantics, int x2, const StepArgs &a, const StepGeom
     return cudaGetLastError();
 }
 
-cudaError_t launch_finalize_poles(float *h, float *hl, const double *part, int nbx, int nt, int np, int pitch,
+cudaError_t launch_finalize_poles(float *h, float *hl, const FixSum *part, int nbx, int nt, int np, int pitch,
                                   cudaStream_t s) {
     finalize_poles_kernel<<<(np + 255) / 256, 256, 0, s>>>(h, hl, part, nbx, nt, np, pitch);
     return cudaGetLastError();

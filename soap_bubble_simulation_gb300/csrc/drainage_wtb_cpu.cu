@@ -8,13 +8,22 @@
 //
 // What the WGSL kernel does not have are the poles: after every step, row 0 becomes the mean of
 // the whole of ring 1 and row N-1 the mean of ring N-2 (update_poles, drainage.rs:480-503), and
-// the next step's ring-1 update reads it. So every row strip is one thread-block cluster whose
-// warps together cover the full ring (cluster rank r holds segments r W .. r W + W - 1). When a
-// strip's pipeline produces ring 1 or ring N-2 at some step, its warps form compensated (TwoSum)
-// partial sums of the ring, publish them in shared memory, meet at a cluster barrier, and every
-// warp gathers all partials through distributed shared memory in the same fixed order, so all
-// of them hold the same mean. Interior strips never reach a ring row (strips are at least K + 1
-// rows, so their dependency cones stop short of rows 1 and N-2) and never synchronise.
+// the next step's ring-1 update reads it. A row strip is C blocks of W warps that together cover
+// the full ring (block b holds segments b W .. b W + W - 1). When a polar strip's pipeline
+// produces ring 1 or ring N-2 at some step, its warps form compensated (TwoSum) partial sums of
+// the ring, publish them in global memory, meet at a barrier of the strip's C blocks, and every
+// warp gathers all partials in the same fixed order, so all of them hold the same mean. The
+// launch is cooperative (every block resident at once), so the barrier cannot wait for a block
+// that is not running; its wait is bounded all the same. Interior strips never reach a ring row
+// (strips are at least K + 1 rows, so their dependency cones stop short of rows 1 and N-2) and
+// never synchronise.
+//
+// An earlier form made every strip one thread-block cluster and gathered the partials through
+// distributed shared memory. Clusters of C = 9 blocks are placed whole on one GPC, which at
+// 2048 x 4096 left some SMs without a block and the average SM busy 56 % of the launch (33.5 us
+// per step); the plain grid keeps every SM at its four blocks. The ring sums are exact integer
+// sums (fixsum.cuh): the compensated double sums before them kept the polar strips' warps on
+// the FP64 pipe for ~10 us per ring mean.
 //
 // Order within one step is the reference's: stencil (rows 1..N-2), the pole means from the
 // stencil's ring values, then the fronts thin their cells. In the skewed pipeline the top pole
@@ -25,13 +34,11 @@
 // The per-cell arithmetic is cpu_cell4() (cell.cuh) and the front factor the double-float
 // product of the single-step kernel, so K single steps and one launch of this give the same bits
 // (the ring sums are compensated, which makes them independent of the summation order).
-#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "cell.cuh"
+#include "fixsum.cuh"
 #include "sbs_internal.h"
-
-namespace cg = cooperative_groups;
 
 namespace sbs {
 namespace {
@@ -39,36 +46,40 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kSegStride = 120;  // output columns per warp
 constexpr int kMaxWarps = 8;      // warps per block
-// Registers per thread. The pipeline is latency-bound at the few warps a wave of ring-wide
-// clusters leaves per SM, so more warps beat fewer spills: at 2048 x 4096, compensated K = 2
-// measured 32.8 us per step capped at 128 registers and 36-38 us with its own ~138; K = 4,
-// which needs ~180, 37.7 us at 128 and 50.3 uncapped; plain f32 K = 4 19.7 us either way.
+// Registers per thread: 128 lets four blocks of four warps share an SM. The pipeline needs more
+// warps more than fewer spills (an earlier, cluster-launched form at 2048 x 4096: compensated
+// K = 2 32.8 us per step capped at 128 registers against 36-38 us with its own ~138).
 constexpr int kMaxRegs = 128;
-constexpr int kMaxCluster = 16;  // blocks per cluster (above 8 needs the non-portable opt-in)
 constexpr int kMaxK = 4;
+// Rows in flight per lane. Row t + kDepth is requested while row t is consumed, through a
+// per-warp ring of kDepth + 1 row slots (hi and lo words) in shared memory filled by per-thread
+// 16-byte cp.async copies: each lane waits only for its own copies (cp.async.wait_group), so no
+// handshake between warps is needed and the rows in flight cost no registers. Depths 2 to 6
+// measured within 2 % of each other.
+constexpr int kDepth = 3;
+constexpr int kSlots = kDepth + 1;
+
+__device__ __forceinline__ void cp_async16(float4 *smem, const float *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
 
 __device__ __forceinline__ float4 splat4(float v) { return make_float4(v, v, v, v); }
 
-__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e) {
-    s = a + b;
-    const double bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
-
-// (s, c) += (s2, c2): compensated combination; the same bits whichever operand comes first.
-__device__ __forceinline__ void comp_merge(double &s, double &c, double s2, double c2) {
-    double e;
-    two_sum(s, s2, s, e);
-    c = c + c2 + e;
-}
-
-__device__ __forceinline__ void comp_warp(double &s, double &c) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const double s2 = __shfl_xor_sync(kFull, s, o), c2 = __shfl_xor_sync(kFull, c, o);
-        comp_merge(s, c, s2, c2);
-    }
-}
+// Where a polar strip's blocks exchange their ring partials.
+struct RingX {
+    FixSum *part;            // [2][kMaxK][nparts] warp partials in global memory (top, bottom)
+    unsigned *bar;           // [2][kMaxK] barrier words (arrivals, generation), then the status word
+    unsigned *status_host;   // host-mapped copy of the status word
+    long long limit;         // barrier wait limit, SM cycles
+    unsigned narrive;        // arrivals a barrier waits for (C, plus one in the timeout test)
+    int nparts;              // warp partials per ring = C W
+};
 
 struct Ctx {
     const float *hin, *lin;  // column-offset input pointers of this lane
@@ -80,42 +91,92 @@ struct Ctx {
     bool keep;               // lane owns kept, valid columns (stores and ring sums)
     float b, DR2, dt, crit;
     const double *vol_w;
-    double2 *red;            // [2][K][W] ring partials in shared memory (top, bottom)
-    int W, C;
+    RingX x;                 // the polar strips' ring exchange
     unsigned colbits[kMaxK]; // per step: 4 bits per front, the lane's columns inside it
     const TfeStep *tfe;      // the K steps' front records in shared memory
     bool fronts;             // some step of the launch has a front
+    float4 *ring;            // this lane's row slots: ring[(slot * 2 + word) * 32]
 };
 
-// Mean of a ring row over the cluster: compensated sums per lane, per warp, then every warp
-// gathers the nparts warp partials (all blocks' slots `mine`, rank-major) in the same order.
-// All threads of the cluster call this.
+// Requests row r (hi and lo words) into its ring slot and closes the copy group; rows outside
+// [0, nt) and past the strip's span are not fetched (the group is then empty).
 template <bool X2>
-__device__ __noinline__ double ring_mean(float4 oh, float4 ol, bool keep, double2 *mine, int W, int nparts, int np) {
+__device__ __forceinline__ void request_row(const Ctx &w, int r) {
+    if (r >= 0 && r < w.nt && r < w.t0 + w.span) {
+        float4 *slot = w.ring + ((r - w.t0) % kSlots) * 64;
+        cp_async16(slot, w.hin + (size_t)r * w.pitch);
+        if (X2) cp_async16(slot + 32, w.lin + (size_t)r * w.pitch);
+    }
+    cp_async_commit();
+}
+
+// Barrier of the C blocks of one polar strip. All threads of the block call it. Bounded: after
+// `limit` cycles it records a timeout in the status words and returns; once a timeout is
+// recorded, later barriers of the launch do not wait.
+__device__ __forceinline__ void strip_barrier(unsigned *b, unsigned *status, unsigned *status_host, long long limit,
+                                              unsigned narrive) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned gen = atomicAdd(b + 1, 0u);
+        __threadfence();
+        if (atomicAdd(b, 1u) + 1 == narrive) {
+            atomicExch(b, 0u);
+            __threadfence();
+            atomicAdd(b + 1, 1u);
+        } else if (atomicAdd(status, 0u) == 0u) {
+            const long long t0 = clock64();
+            while (atomicAdd(b + 1, 0u) == gen) {
+                if (clock64() - t0 > limit) {
+                    atomicOr(status, 1u);
+                    *(volatile unsigned *)status_host = 1u;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+// Mean of a ring row over the strip: exact fixed-point sums (fixsum.cuh) per lane and per warp,
+// published per warp; every warp then adds all nparts partials, so all of them hold the same
+// mean. All threads of the strip's blocks call this; slot = side * kMaxK + level - 1. Scalar
+// arguments keep the caller's context in registers.
+template <bool X2>
+__device__ __noinline__ double ring_mean(float4 oh, float4 ol, bool keep, FixSum *part_all, unsigned *bar,
+                                         unsigned *status_host, long long limit, unsigned narrive, int nparts, int np,
+                                         int slot) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double s = 0.0, c = 0.0;
+    FixSum acc = fix_zero();
     if (keep) {
-        double e;
-        const float hv[4] = {oh.x, oh.y, oh.z, oh.w}, lv[4] = {ol.x, ol.y, ol.z, ol.w};
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const double x = X2 ? (double)hv[k] + (double)lv[k] : (double)hv[k];
-            two_sum(s, x, s, e);
-            c += e;
+        fix_add_float(acc, oh.x);
+        fix_add_float(acc, oh.y);
+        fix_add_float(acc, oh.z);
+        fix_add_float(acc, oh.w);
+        if (X2) {
+            fix_add_float(acc, ol.x);
+            fix_add_float(acc, ol.y);
+            fix_add_float(acc, ol.z);
+            fix_add_float(acc, ol.w);
         }
     }
-    comp_warp(s, c);
-    if (lane == 0) mine[warp] = make_double2(s, c);
-    cg::cluster_group cl = cg::this_cluster();
-    cl.sync();
-    double S = 0.0, Cc = 0.0;
+    fix_warp(acc);
+    FixSum *part = part_all + (size_t)slot * nparts;
+    if (lane == 0) part[blockIdx.x * (blockDim.x >> 5) + warp] = acc;
+    strip_barrier(bar + 2 * slot, bar + 4 * kMaxK, status_host, limit, narrive);
+    FixSum tot = fix_zero();
     for (int j = lane; j < nparts; j += 32) {
-        const double2 *rp = cl.map_shared_rank(mine, (unsigned)(j / W));
-        const double2 v = rp[j % W];
-        comp_merge(S, Cc, v.x, v.y);
+        fix_add(tot, fix_ldcg(part + j));
     }
-    comp_warp(S, Cc);
-    return (S + Cc) / (double)np;
+    fix_warp(tot);
+    return fix_to_double(tot) / (double)np;
+}
+
+template <bool X2>
+__device__ __forceinline__ double ring_mean_of(const Ctx &w, float4 oh, float4 ol, int slot) {
+    return ring_mean<X2>(oh, ol, w.keep, w.x.part, w.x.bar, w.x.status_host, w.x.limit, w.x.narrive, w.x.nparts,
+                         w.np, slot);
 }
 
 // Thins the cells of one row of step l that lie inside a front of that step (drainage.rs:425-460).
@@ -160,31 +221,31 @@ __device__ __forceinline__ void store_row(const Ctx &w, int i, float4 oh, float4
     }
 }
 
-// One pipeline iteration: receive level-0 row t (prefetched), request row t + 1, then level l of
-// row t - l for l = 1..K. Slot P holds each level's newest row.
+// One pipeline iteration: receive level-0 row t from the ring, request row t + kDepth, then level l
+// of row t - l for l = 1..K. Slot P holds each level's newest row.
 // Poles: row 0 of step l is written into its slot (CUR, the previous iteration's) when ring 1 of
 // step l is reduced; row N-1 of step l is written into the slot it will occupy in the next
 // iteration (UP, free once level l + 1 of this iteration has read it) when ring N-2 is reduced.
 // Step K's pole rows are stored at the reduction.
 template <int K, int P, bool X2, bool VOL, bool POLAR>
-__device__ __forceinline__ void iter(const Ctx &w, int t, float4 (&wh)[K][3], float4 (&wl)[K][3], float4 &ph,
-                                     float4 &pl, double &vacc) {
+__device__ __forceinline__ void iter(const Ctx &w, int t, float4 (&wh)[K][3], float4 (&wl)[K][3], double &vacc) {
     constexpr int CUR = (P + 2) % 3, UP = (P + 1) % 3;
-    const int tl = t + 1;
+    cp_async_wait<kDepth - 1>();  // the groups of rows <= t have landed
     float4 nh = splat4(0.f), nl = nh;
-    if (tl >= 0 && tl < w.nt && tl < w.t0 + w.span) {
-        nh = __ldg(reinterpret_cast<const float4 *>(w.hin + (size_t)tl * w.pitch));
-        if (X2) nl = __ldg(reinterpret_cast<const float4 *>(w.lin + (size_t)tl * w.pitch));
+    if (t >= 0 && t < w.nt) {  // t < t0 + span always
+        const float4 *slot = w.ring + ((t - w.t0) % kSlots) * 64;
+        nh = slot[0];
+        if (X2) nl = slot[32];
     }
-    wh[0][P] = ph;
-    if (X2) wl[0][P] = pl;
-    ph = nh;
-    pl = nl;
+    wh[0][P] = nh;
+    if (X2) wl[0][P] = nl;
+    // the slot of row t + kDepth last held row t - 1, read one iteration ago
+    request_row<X2>(w, t + kDepth);
     double mbot = 0.0;  // ring N-2 mean of the level reduced in this iteration
 #pragma unroll
     for (int l = 1; l <= K; ++l) {
         const int i = t - l;
-        // cluster-uniform: every thread of the strip walks the same rows
+        // strip-uniform: every thread of the strip walks the same rows
         const bool need = i >= w.r0 - (K - l) && i < w.r1 + (K - l) && i >= 0 && i < w.nt;
         float4 oh = splat4(0.f), ol = oh;
         if (POLAR && need && i == w.nt - 1 && l < K) {  // the bottom pole, written one iteration ago
@@ -211,7 +272,7 @@ __device__ __forceinline__ void iter(const Ctx &w, int t, float4 (&wh)[K][3], fl
             if (POLAR && (i == 1 || i == w.nt - 2)) {
                 // pole means of this step from the ring's stencil values (before the fronts)
                 if (i == 1) {
-                    const double m = ring_mean<X2>(oh, ol, w.keep, w.red + (l - 1) * w.W, w.W, w.W * w.C, w.np);
+                    const double m = ring_mean_of<X2>(w, oh, ol, l - 1);
                     const float mh = (float)m;
                     const float4 ph4 = splat4(mh), pl4 = splat4(X2 ? (float)(m - (double)mh) : 0.f);
                     if (l < K) {
@@ -222,7 +283,7 @@ __device__ __forceinline__ void iter(const Ctx &w, int t, float4 (&wh)[K][3], fl
                     }
                 }
                 if (i == w.nt - 2) {
-                    mbot = ring_mean<X2>(oh, ol, w.keep, w.red + (K + l - 1) * w.W, w.W, w.W * w.C, w.np);
+                    mbot = ring_mean_of<X2>(w, oh, ol, kMaxK + l - 1);
                     if (l == K && w.r1 == w.nt && w.keep) {
                         const float mh = (float)mbot;
                         store_row<VOL>(w, w.nt - 1, splat4(mh), splat4(X2 ? (float)(mbot - (double)mh) : 0.f), X2,
@@ -246,6 +307,25 @@ __device__ __forceinline__ void iter(const Ctx &w, int t, float4 (&wh)[K][3], fl
     }
 }
 
+// Rows [r0, r1) of strip `by` of `ns`: the two polar strips have prow rows each, the interior
+// strips share the rest evenly. prow = 0: all strips even.
+__host__ __device__ inline void strip_rows(int by, int ns, int nt, int prow, int &r0, int &r1) {
+    if (prow <= 0 || ns < 3) {
+        r0 = (int)((long long)by * nt / ns);
+        r1 = (int)((long long)(by + 1) * nt / ns);
+    } else if (by == 0) {
+        r0 = 0;
+        r1 = prow;
+    } else if (by == ns - 1) {
+        r0 = nt - prow;
+        r1 = nt;
+    } else {
+        const long long rest = nt - 2 * prow;
+        r0 = prow + (int)((by - 1) * rest / (ns - 2));
+        r1 = prow + (int)(by * rest / (ns - 2));
+    }
+}
+
 __device__ __forceinline__ double block_sum(double v, double *smem) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
@@ -261,11 +341,10 @@ __device__ __forceinline__ double block_sum(double v, double *smem) {
 
 template <int K, bool X2, bool VOL>
 __global__ void __maxnreg__(kMaxRegs) wtbc_kernel(const StepArgs a) {
-    __shared__ double2 s_red[2 * kMaxK * kMaxWarps];
     __shared__ TfeStep s_tfe[kMaxK];
     __shared__ double s_vred[32];
     __shared__ int s_last;
-    extern __shared__ float4 s_dyn[];  // coefficients of rows [t0, t1), then the front table
+    extern __shared__ float4 s_dyn[];  // row rings of the warps, coefficients of rows [t0, t1), front table
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
     const int np = a.np, nt = a.nt;
@@ -273,8 +352,8 @@ __global__ void __maxnreg__(kMaxRegs) wtbc_kernel(const StepArgs a) {
     const int seg = blockIdx.x * W + warp;
     const int c_unwrapped = seg * kSegStride - 4 + 4 * lane;
     const int col = ((c_unwrapped % np) + np) % np;
-    const int ns = gridDim.y;
-    const int r0 = (int)((long long)blockIdx.y * nt / ns), r1 = (int)((long long)(blockIdx.y + 1) * nt / ns);
+    int r0, r1;
+    strip_rows(blockIdx.y, gridDim.y, nt, a.prow, r0, r1);
 
     Ctx w;
     w.hin = a.hin + col;
@@ -294,11 +373,15 @@ __global__ void __maxnreg__(kMaxRegs) wtbc_kernel(const StepArgs a) {
     w.dt = a.dt;
     w.crit = a.crit;
     w.vol_w = a.vol_w;
-    w.red = s_red;
-    w.W = W;
-    w.C = gridDim.x;
-    float4 *sco = s_dyn;
-    unsigned *fsel = reinterpret_cast<unsigned *>(s_dyn + w.span);
+    w.x.part = a.ring_part;
+    w.x.bar = a.ring_bar;
+    w.x.status_host = a.status_host;
+    w.x.limit = a.wait_cycles;
+    w.x.narrive = gridDim.x + a.extra;
+    w.x.nparts = gridDim.x * W;
+    w.ring = s_dyn + (size_t)warp * kSlots * 64 + lane;
+    float4 *sco = s_dyn + (size_t)W * kSlots * 64;
+    unsigned *fsel = reinterpret_cast<unsigned *>(sco + w.span);
     w.sco = sco;
     w.fsel = fsel;
     w.tfe = s_tfe;
@@ -347,26 +430,22 @@ __global__ void __maxnreg__(kMaxRegs) wtbc_kernel(const StepArgs a) {
 
     double vacc = 0.0;
     const int t0 = w.t0, t1 = w.t0 + w.span;
-    float4 ph = splat4(0.f), pl = ph;
-    if (t0 >= 0) {
-        ph = __ldg(reinterpret_cast<const float4 *>(w.hin + (size_t)t0 * w.pitch));
-        if (X2) pl = __ldg(reinterpret_cast<const float4 *>(w.lin + (size_t)t0 * w.pitch));
-    }
-    if (r0 == 0 || r1 == nt) {  // a polar strip (cluster-uniform)
+#pragma unroll
+    for (int j = 0; j < kDepth; ++j) request_row<X2>(w, t0 + j);
+    if (r0 == 0 || r1 == nt) {  // a polar strip (block-uniform)
         for (int t = t0; t < t1; t += 3) {
-            iter<K, 0, X2, VOL, true>(w, t, wh, wl, ph, pl, vacc);
-            if (t + 1 < t1) iter<K, 1, X2, VOL, true>(w, t + 1, wh, wl, ph, pl, vacc);
-            if (t + 2 < t1) iter<K, 2, X2, VOL, true>(w, t + 2, wh, wl, ph, pl, vacc);
+            iter<K, 0, X2, VOL, true>(w, t, wh, wl, vacc);
+            if (t + 1 < t1) iter<K, 1, X2, VOL, true>(w, t + 1, wh, wl, vacc);
+            if (t + 2 < t1) iter<K, 2, X2, VOL, true>(w, t + 2, wh, wl, vacc);
         }
     } else {
         for (int t = t0; t < t1; t += 3) {
-            iter<K, 0, X2, VOL, false>(w, t, wh, wl, ph, pl, vacc);
-            if (t + 1 < t1) iter<K, 1, X2, VOL, false>(w, t + 1, wh, wl, ph, pl, vacc);
-            if (t + 2 < t1) iter<K, 2, X2, VOL, false>(w, t + 2, wh, wl, ph, pl, vacc);
+            iter<K, 0, X2, VOL, false>(w, t, wh, wl, vacc);
+            if (t + 1 < t1) iter<K, 1, X2, VOL, false>(w, t + 1, wh, wl, vacc);
+            if (t + 2 < t1) iter<K, 2, X2, VOL, false>(w, t + 2, wh, wl, vacc);
         }
     }
-    // no block may leave while a cluster peer can still read its ring partials
-    cg::this_cluster().sync();
+    cp_async_wait<0>();  // every copy was consumed; nothing may still be landing at exit
 
     if (VOL) {
         const double s = block_sum(vacc, s_vred);
@@ -413,91 +492,81 @@ const void *wtbc_fn(int K, bool x2, bool vol) {
     }
 }
 
-size_t dyn_smem(int span, int K) { return sizeof(float4) * (size_t)span + sizeof(unsigned) * (size_t)K * span; }
+size_t dyn_smem(int W, int span, int K) {
+    return sizeof(float4) * ((size_t)W * kSlots * 64 + span) + sizeof(unsigned) * (size_t)K * span;
+}
 
 }  // namespace
 
-// Geometry of the blocked CPU-semantics step: W warps per block and C = ceil(segments / W)
-// blocks per cluster cover the ring's 120-column segments (C <= 16). A launch is one wave of
-// clusters, one per row strip, so the W that lets the most clusters be resident at once wins
-// (the strips are then shortest); ties go to fewer idle warps, then W nearest 4. Strips have at
-// least K + 1 rows. nby = 0: unsupported.
+// Geometry of the blocked CPU-semantics step: blocks of W = 4 warps (fewer on narrow grids), C =
+// ceil(segments / W) blocks per strip across the ring's 120-column segments, and as many strips
+// as fit one wave (the cooperative launch needs every block resident). The two polar strips get
+// K + 1 rows, the fewest the pipeline allows: their blocks also meet at a barrier for every
+// ring mean, and with equal strips they finished last (2048 x 4096, compensated K = 2: 28.6 us per
+// step with equal strips, 20.2 with polar strips of K + 1 rows). Interior strips have at least
+// K + 1 rows. nby = 0: unsupported.
 StepGeom wtbc_geometry(int nt, int np, int K, int x2) {
     StepGeom g{};
     if (K < 2 || K > kMaxK || np % 4 != 0 || np < 8 || nt < 2 * (K + 1)) return g;
     const int segs = (np + kSegStride - 1) / kSegStride;
-    int dev = 0, sms = 148;
+    int dev = 0, sms = 148, coop = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int span_guess = (nt + sms - 1) / sms + 2 * K + 64;
-    int bestW = 0, bestC = 0, bestN = 0, bestWaste = 1 << 30, bestD = 1 << 30;
-    for (int W = 1; W <= kMaxWarps; ++W) {
-        const int C = (segs + W - 1) / W;
-        if (C > kMaxCluster) continue;
-        if (C > 8) {
-            bool ok = true;
-            for (int v = 0; v < 2; ++v)
-                ok = ok && cudaFuncSetAttribute(wtbc_fn(K, x2 != 0, v == 1),
-                                                cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
-            if (!ok) {
-                cudaGetLastError();
-                continue;
-            }
-        }
-        cudaLaunchConfig_t cfg{};
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = C;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.gridDim = dim3(C, 1);
-        cfg.blockDim = dim3(32 * W);
-        cfg.dynamicSmemBytes = dyn_smem(span_guess, K);
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        int n = 0;
-        if (cudaOccupancyMaxActiveClusters(&n, wtbc_fn(K, x2 != 0, true), &cfg) != cudaSuccess) {
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (!coop) return g;
+    for (int v = 0; v < 2; ++v)  // the rings alone take up to 32 KB a block
+        if (cudaFuncSetAttribute(wtbc_fn(K, x2 != 0, v == 1), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 160 * 1024) != cudaSuccess) {
             cudaGetLastError();
-            n = 0;
+            return g;
         }
-        if (n < 1) continue;
-        const int waste = C * W - segs, d = W > 4 ? W - 4 : 4 - W;
-        if (n > bestN || (n == bestN && (waste < bestWaste || (waste == bestWaste && d < bestD)))) {
-            bestW = W;
-            bestC = C;
-            bestN = n;
-            bestWaste = waste;
-            bestD = d;
+    const int W = segs < 4 ? segs : 4, C = (segs + W - 1) / W;
+    // strips that fit one wave: shrink until the blocks of the real strip height fit
+    int ns = nt / (K + 1);
+    for (int it = 0; it < 8 && ns >= 1; ++it) {
+        int prow = 0, rmax = 0;
+        if (ns >= 3) {
+            prow = K + 1;
+            if ((nt - 2 * prow) / (ns - 2) < K + 1) prow = 0;
         }
+        for (int by = 0; by < ns; ++by) {
+            int r0, r1;
+            strip_rows(by, ns, nt, prow, r0, r1);
+            rmax = r1 - r0 > rmax ? r1 - r0 : rmax;
+        }
+        int per_sm = 0;
+        for (int v = 0; v < 2; ++v) {
+            int n = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wtbc_fn(K, x2 != 0, v == 1), 32 * W,
+                                                              dyn_smem(W, rmax + 2 * K, K)) != cudaSuccess) {
+                cudaGetLastError();
+                n = 0;
+            }
+            per_sm = v == 0 || n < per_sm ? n : per_sm;
+        }
+        const int fit = per_sm * sms / C;
+        if (fit >= ns) {
+            if (dyn_smem(W, rmax + 2 * K, K) > 160 * 1024) return g;
+            g.wx = W;
+            g.nbx = C;
+            g.nby = ns;
+            g.rb = rmax;
+            g.prow = prow;
+            return g;
+        }
+        ns = fit;
     }
-    if (bestW == 0) return g;
-    int ns = bestN < nt / (K + 1) ? bestN : nt / (K + 1);
-    if (ns < 1) ns = 1;
-    g.wx = bestW;
-    g.nbx = bestC;
-    g.nby = ns;
-    g.rb = (nt + ns - 1) / ns;
     return g;
 }
 
+int wtbc_ring_parts(const StepGeom &g) { return g.nbx * g.wx; }
+
 cudaError_t launch_wtbc(int K, int x2, const StepArgs &a, const StepGeom &g, cudaStream_t s) {
     const void *fn = wtbc_fn(K, x2 != 0, a.vol_w != nullptr);
-    if (fn == nullptr || g.nby < 1) return cudaErrorInvalidValue;
+    if (fn == nullptr || g.nby < 1 || a.ring_part == nullptr || a.ring_bar == nullptr) return cudaErrorInvalidValue;
     const int span = g.rb + 2 * K;
-    cudaLaunchConfig_t cfg{};
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = g.nbx;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3(g.nbx, g.nby);
-    cfg.blockDim = dim3(32 * g.wx);
-    cfg.dynamicSmemBytes = dyn_smem(span, K);
-    cfg.stream = s;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
     void *args[] = {(void *)&a};
-    return cudaLaunchKernelExC(&cfg, fn, args);
+    return cudaLaunchCooperativeKernel(fn, dim3(g.nbx, g.nby), dim3(32 * g.wx), args, dyn_smem(g.wx, span, K), s);
 }
 
 }  // namespace sbs

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/sbs.h"
+#include "fixsum.cuh"
 
 namespace sbs {
 
@@ -88,8 +89,8 @@ struct StepArgs {
     const float *lin;  // low-order thickness words (compensated f32x2 mode)
     float *lout;
     const float4 *rows;    // per theta row: A = -rho g/(3 eta) sin, E = cot/(2 dth), F = 1/(ss^2 dphi^2), G
-    const double *pin;     // pole-ring partial sums (s, c pairs) of the input field (CPU semantics)
-    double *pout;          // pole-ring partial sums written by this step
+    const FixSum *pin;     // pole-ring partial sums (ring 1 per block, then ring N-2) of the input field
+    FixSum *pout;          // pole-ring partial sums written by this step (CPU semantics)
     const TfeStep *tfe;    // fronts of this step (nullptr = none)
     const double *vol_w;   // per-row volume weights R^2 sin dth dphi (nullptr = no volume check)
     double *vol_partials;  // one per block
@@ -101,13 +102,21 @@ struct StepArgs {
     int poles_virtual;  // 1: pole rows of hin are the means of pin, not memory
     int marangoni;
     float crit, b, DR2, DsR2, Gt, M, dt;
+    // blocked CPU-semantics step only: the polar strips' ring exchange
+    FixSum *ring_part;      // [2][4][C W] warp partials of ring 1 / ring N-2 per step of the launch
+    unsigned *ring_bar;     // [2][4] barrier words (arrivals, generation), then the status word
+    unsigned *status_host;  // host-mapped status word (nonzero: a barrier wait timed out)
+    long long wait_cycles;  // barrier wait limit
+    unsigned extra;         // arrivals beyond the strip's blocks (1 only in the timeout test)
+    int prow;               // rows of each polar strip (0: all strips even)
 };
 
 struct StepGeom {
     int wx;   // warps per block along phi
     int nbx;  // column blocks
     int nby;  // row strips
-    int rb;
+    int rb;   // rows of the tallest strip
+    int prow; // blocked CPU-semantics step: rows of each polar strip (0: all strips even)
 };
 
 StepGeom step_geometry(int nt, int np, int semantics, int x2);
@@ -116,14 +125,18 @@ bool wtb_supported(int nt, int np);
 StepGeom wtb_geometry(int nt, int np, int K);
 cudaError_t launch_wtb(int K, const StepArgs &a, const StepGeom &g, cudaStream_t s);
 // Temporally blocked CPU-semantics step (K = 2..4 steps per launch, pole means and fronts
-// included), drainage_wtb_cpu.cu. Each row strip is one cluster of nbx blocks of wx warps that
-// spans the ring; nby strips of at most rb rows. nby == 0: the grid is not supported.
+// included), drainage_wtb_cpu.cu. Each row strip is nbx blocks of wx warps that span the ring;
+// nby strips of at most rb rows, all resident at once (cooperative launch). nby == 0: the grid
+// is not supported. The ring exchange needs 2 x 4 x wtbc_ring_parts(g) FixSum partials and
+// kWtbcBarWords barrier words (zeroed before first use and after a timeout).
+constexpr int kWtbcBarWords = 17;
 StepGeom wtbc_geometry(int nt, int np, int K, int x2);
+int wtbc_ring_parts(const StepGeom &g);
 cudaError_t launch_wtbc(int K, int x2, const StepArgs &a, const StepGeom &g, cudaStream_t s);
 // x2: compensated f32x2 thickness (hi + lo words); CPU semantics only.
 cudaError_t launch_step(int semantics, int x2, const StepArgs &a, const StepGeom &g, cudaStream_t s);
 // Writes the pole rows of `h` (and `hl`, if not null) from the ring partials of the last step.
-cudaError_t launch_finalize_poles(float *h, float *hl, const double *part, int nbx, int nt, int np,
+cudaError_t launch_finalize_poles(float *h, float *hl, const FixSum *part, int nbx, int nt, int np,
                                   int pitch, cudaStream_t s);
 
 // Field reductions: min, max and FP64 volume sum of a pitched field (valid columns only).
@@ -202,7 +215,7 @@ struct sbs_drainage {
     int x2 = 0;                          // 1: compensated f32x2 thickness
     int cur = 0;   // buffer index holding the newest field
     int prev = 1;  // buffer holding the field one pass older (WGSL quirk accessor)
-    double *part[2] = {nullptr, nullptr};
+    sbs::FixSum *part[2] = {nullptr, nullptr};  // per-block pole-ring partials (single-step kernel)
     float4 *rows = nullptr;
     double *vol_w = nullptr;
     double *vol_partials = nullptr;
@@ -225,6 +238,11 @@ struct sbs_drainage {
     sbs::StepGeom wgeom{};
     int cpu_k = 0;  // steps per temporally blocked launch (CPU semantics; 0 = single steps only)
     sbs::StepGeom cgeom{};
+    sbs::FixSum *ring_part = nullptr;  // the blocked step's ring exchange (CPU semantics)
+    unsigned *ring_bar = nullptr;
+    unsigned *ring_status = nullptr;   // host-mapped timeout word
+    unsigned *ring_status_dev = nullptr;
+    unsigned wait_epoch = 0;           // the wait settings the captured graphs were made with
 
     // CPU semantics parameters (from sbs_config)
     sbs_config cfg{};

@@ -98,9 +98,9 @@ def cpu_blocking(sbs, sim):
 @pytest.mark.parametrize("res", [10, 12, 64, 130, 256])
 def test_cpu_time_blocking_bit_identical(sbs, orc, precision, res):
     """K = 1..4 steps per launch (the blocked kernel's polar strips form each step's ring means
-    as a cluster reduction): the same bits as single steps and as the kernel-order oracle, with
-    fronts active (first spawn at step 50), a frozen critical patch, volume checks and chunk
-    ends at every K."""
+    as exact integer sums across their blocks): the same bits as single steps and as the
+    kernel-order oracle, with fronts active (first spawn at step 50), a frozen critical patch,
+    volume checks and chunk ends at every K."""
     from soap_bubble_simulation_gb300 import synthetic
 
     h0 = synthetic.bubble_c0(res, seed=res + 1)
@@ -110,7 +110,7 @@ def test_cpu_time_blocking_bit_identical(sbs, orc, precision, res):
     results = []
     for k in (1, 2, 3, 4):
         sim = make_sim(sbs, res, precision)
-        assert cpu_blocking(sbs, sim) == (2 if precision == "f32x2" else 4)  # the defaults
+        assert cpu_blocking(sbs, sim) == (3 if precision == "f32x2" else 4)  # the defaults
         set_cpu_blocking(sbs, sim, k)
         assert cpu_blocking(sbs, sim) == k
         set64(sbs, sim, h0)

@@ -5,7 +5,8 @@ handle or function computes the right result.
 Nothing is faulted or hung: a host switch (sbs_set_stall_injection) makes the waits
 unsatisfiable - the tensor-core kernels issue neither their MMAs nor the commits that would
 signal them, so no asynchronous operation is outstanding when a wait expires, and the foam
-kernel's grid barrier expects one arrival more than the grid has - and a short wait limit
+kernel's grid barrier and the pole-ring barrier of the blocked DrainageSimulator step expect one
+arrival more than there are blocks - and a short wait limit
 (sbs_set_wait_limit, 2e5 cycles, ~0.1 ms) bounds every wait.
 """
 import ctypes
@@ -106,3 +107,38 @@ def test_fused_surrogate_wait_times_out_then_recovers(sbs, orc, short_waits):
     want = orc.nn_forward(net.params, x)
     assert np.abs(y - want).max() / np.abs(want).max() <= 1e-2
     net.close()
+
+
+def test_blocked_drainage_pole_ring_barrier_times_out_then_recovers(sbs, short_waits):
+    """The polar strips of the blocked DrainageSimulator step meet at a barrier per step; with it
+    unsatisfiable the call reports the timeout, and afterwards the handle steps like a fresh one."""
+    from soap_bubble_simulation_gb300 import synthetic
+
+    N = short_waits
+    cfg = sbs.SimulationConfig()
+    cfg.resolution = 64
+    h0 = np.ascontiguousarray(synthetic.bubble_c0(64, seed=2))
+
+    def load(sim):
+        N.call("sbs_drainage_set_thickness_f64", sim.handle, N.dptr(h0), h0.size)
+
+    def field(sim):
+        out = np.empty(h0.size)
+        N.call("sbs_drainage_get_thickness_field_f64", sim.handle, N.dptr(out), out.size)
+        return out
+
+    sim, fresh = sbs.DrainageSimulator(cfg), sbs.DrainageSimulator(cfg)
+    kb = ctypes.c_int()
+    N.call("sbs_drainage_time_blocking", sim.handle, ctypes.byref(kb))
+    assert kb.value > 1
+    load(sim)
+    N.call("sbs_set_stall_injection", N.STALL_GRID_BARRIER)
+    with pytest.raises(sbs.SbsError) as e:
+        sim.step_n(0.001, 4 * kb.value)
+    assert e.value.code == N.SBS_E_TIMEOUT
+    N.call("sbs_set_stall_injection", 0)
+    fresh.step_n(0.001, 4 * kb.value)  # the same clock (fronts depend on it)
+    for s in (sim, fresh):
+        load(s)
+        s.step_n(0.001, 16)
+    np.testing.assert_array_equal(field(sim), field(fresh))

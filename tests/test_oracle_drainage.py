@@ -270,3 +270,57 @@ def test_wgsl_kernel_order_close_to_wgsl_order(orc):
         np.testing.assert_array_equal(hN[0], h[0])
         np.testing.assert_array_equal(hN[-1], h[-1])
         np.testing.assert_array_equal(cK[-1], c[-1])
+
+
+def _exact_ring_mean(words, np_):
+    """The kernels' ring mean from first principles: each f32 word truncated toward zero to a
+    multiple of 2^-96, summed exactly, rounded to the nearest double, divided by the ring length."""
+    from fractions import Fraction
+
+    tot = 0
+    for w in np.asarray(words, dtype=np.float32).ravel():
+        q = Fraction(float(w)) * 2**96
+        tot += int(q)  # int() truncates toward zero
+    return float(Fraction(tot, 2**96)) / np_
+
+
+@pytest.mark.parametrize("precision", ["f32k", "f32x2"])
+def test_kernel_order_pole_means_are_exact_ring_sums(orc, precision):
+    """The pole rows after one kernel-order step are the exact ring-1 / ring-(N-2) sums of the
+    stencil's words (drainage.rs:480-503 restated with order-free integer sums)."""
+    res = 24
+    g = np.random.default_rng(4)
+    h = 500e-9 * (1.0 + 0.2 * g.uniform(-1, 1, size=(res, 2 * res)))
+    h[1, ::5] *= 3.0  # spread the magnitudes, so low words carry many bits
+    sim = orc.CpuSim(resolution=res, precision=precision)
+    sim.set_field(h)
+    sim.step(0.001)
+    f = sim.field()
+    hi = f.astype(np.float32)
+    lo = (f - hi.astype(np.float64)).astype(np.float32) if precision == "f32x2" else np.zeros_like(hi)
+    for ring, pole in ((1, 0), (res - 2, res - 1)):
+        words = np.concatenate([hi[ring], lo[ring]])
+        m = _exact_ring_mean(words, 2 * res)
+        mh = np.float32(m)
+        assert np.all(hi[pole] == mh), (ring, hi[pole][0], mh)
+        if precision == "f32x2":
+            assert np.all(lo[pole] == np.float32(m - float(mh)))
+
+
+def test_exact_ring_mean_across_the_f32_range(orc):
+    """Words from denormals to 1e38 m, both signs, in rings of up to 65,536 cells: the oracle's
+    256-bit integer sum rounds like the exact rational sum; non-finite words give NaN."""
+    g = np.random.default_rng(12)
+    cases = [
+        np.float32([1e-45, -1e-45, 3e-39, 1e-30]),
+        np.float32([3.4e38, 3.4e38, -1.0, 5e-7]),
+        np.float32([1e4, 2.5e-7, -1e4, 1e-20]),
+        (500e-9 * (1 + 0.1 * g.uniform(-1, 1, 65536))).astype(np.float32),
+        np.concatenate([g.uniform(0, 1e-6, 2000), g.uniform(-1e-20, 1e-20, 2000), [7e15, -7e15]]).astype(np.float32),
+        (g.standard_normal(4096) * 10.0 ** g.integers(-40, 38, 4096)).astype(np.float32),
+    ]
+    for w in cases:
+        np_ = max(2, w.size // 2)
+        assert orc.fix_ring_mean(w, np_) == _exact_ring_mean(w, np_), w[:4]
+    assert np.isnan(orc.fix_ring_mean(np.float32([1.0, np.inf]), 2))
+    assert np.isnan(orc.fix_ring_mean(np.float32([np.nan, 1.0]), 2))
