@@ -492,7 +492,9 @@ def shade_section(sbs, torch):
 
 def caustics_section(sbs, synthetic, torch, h0, c0):
     """The caustic pass over the 2048 x 4096 field after a drainage run, on the simulator's own
-    device field (no copy): 8 algorithmic bytes per cell (read h, write the map)."""
+    device field (no copy): 8 algorithmic bytes per cell (read h, write the map); then runs of 10
+    and 100 passes with the map of the buffer the renderer binds, separate pass against the map
+    written by the run's final blocked launch."""
     from soap_bubble_simulation_gb300.caustics import CausticParams
 
     N = sbs._native
@@ -519,6 +521,36 @@ def caustics_section(sbs, synthetic, torch, h0, c0):
     b.record(st)
     torch.cuda.synchronize()
     ms = a.elapsed_time(b) / reps
+
+    # a run of drainage passes and the map of the buffer the renderer binds: run() then the separate
+    # pass, against run_caustics (the map written by the run's final blocked launch)
+    pp = ctypes.cast(ctypes.byref(p), ctypes.c_void_p)
+    outp = ctypes.c_void_p(out.data_ptr())
+
+    def frame(fused, passes):
+        if fused:
+            N.call("sbs_gpu_drainage_run_caustics", sim.handle, passes, pp, outp, N.MEM_DEVICE)
+        else:
+            N.call("sbs_gpu_drainage_run", sim.handle, passes)
+            N.call("sbs_gpu_drainage_caustics", sim.handle, pp, 1, outp, N.MEM_DEVICE)
+
+    fused_runs = {}
+    for passes in (10, 100):
+        res = {}
+        for fused in (False, True):
+            for _ in range(3):
+                frame(fused, passes)
+            n = 20
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(st)
+            for _ in range(n):
+                frame(fused, passes)
+            e1.record(st)
+            torch.cuda.synchronize()
+            res["fused_us" if fused else "separate_us"] = e0.elapsed_time(e1) / n * 1e3
+        res["saved_us"] = res["separate_us"] - res["fused_us"]
+        fused_runs[f"passes_{passes}"] = res
     sim.close()
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
@@ -526,7 +558,8 @@ def caustics_section(sbs, synthetic, torch, h0, c0):
     gbs = 8.0 * h0.size / (ms * 1e-3) / 1e9
     return {"value": h0.size / (ms * 1e-3), "unit": "cells/s", "us_per_map": ms * 1e3, "grid": f"{nt} x {np_}",
             "hbm": {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
-                    "bytes_per_cell": 8}}
+                    "bytes_per_cell": 8},
+            "run_and_map": fused_runs}
 
 
 def branched_section(sbs, synthetic, torch):
@@ -806,6 +839,10 @@ def summary(line: dict) -> dict:
     for key in ("shading", "caustics", "branched_flow", "foam_dynamics"):
         if line.get(key):
             out[key] = _r(line[key]["value"])
+    ca = (line.get("caustics") or {}).get("run_and_map") or {}
+    if ca.get("passes_10"):
+        out["caustics_frame10_us"] = {"separate": _r(ca["passes_10"]["separate_us"]),
+                                      "fused": _r(ca["passes_10"]["fused_us"])}
     return out
 
 

@@ -512,6 +512,19 @@ int sbs_caustics(const sbs_caustic_params *p, const float *thickness, size_t pit
  * field; p's grid must equal the handle's. caustic_map per mem (host: the call
  * returns when the map is there; device: ordered on the handle's stream). */
 int sbs_gpu_drainage_caustics(sbs_drainage *h, const sbs_caustic_params *p, int which, float *caustic_map, int mem);
+/* sbs_gpu_drainage_run(h, passes) followed by sbs_gpu_drainage_caustics(h, p, 1,
+ * caustic_map, mem) - the map of the field one pass behind the newest, the
+ * buffer the renderer binds - with the same results, but the map is written by
+ * the run's final blocked launch from the field it holds on chip, so the field
+ * is not read again (runs of fewer than 4 passes, or with time blocking off,
+ * use the separate pass). The map's device destination and p are part of the
+ * captured graph: a caller that reuses them runs without recapture. */
+int sbs_gpu_drainage_run_caustics(sbs_drainage *h, uint32_t passes, const sbs_caustic_params *p, float *caustic_map,
+                                  int mem);
+/* sbs_gpu_drainage_step(h, frame_dt) (steps_per_frame passes, none when
+ * disabled; the frame-dt clock) followed by the caustic map as above. */
+int sbs_gpu_drainage_step_caustics(sbs_drainage *h, float frame_dt, const sbs_caustic_params *p, float *caustic_map,
+                                   int mem);
 
 /* ------------------------------------------------------------------ */
 /* Branched flow of light through the film (ray tracing)               */

@@ -205,6 +205,8 @@ SIGNATURES: dict[str, list] = {
     "sbs_caustic_params_default": [_P],
     "sbs_caustics": [_P, _P, _SZ, _P, _I, _P],
     "sbs_gpu_drainage_caustics": [_P, _P, _I, _P, _I],
+    "sbs_gpu_drainage_run_caustics": [_P, C.c_uint32, _P, _P, _I],
+    "sbs_gpu_drainage_step_caustics": [_P, C.c_float, _P, _P, _I],
     "sbs_branched_params_default": [_P],
     "sbs_branched_scatterers": [_P, _U32, _F, _P],
     "sbs_branched_flow": [_P, _P, _U32, _U32, _SZ, _P, _P, _I, _I, _P],

@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "caustics.cuh"
 #include "sbs_internal.h"
 
 namespace sbs {
@@ -21,52 +22,6 @@ namespace {
 
 constexpr int kCols = 128;  // threads (columns) per block
 constexpr int kRows = 16;   // rows a thread walks down
-
-struct Row {
-    float l, c, r;
-};
-
-// pow(x, y) for x > 0 through the special-function unit: 2^(y log2 x) with the hardware base-2
-// logarithm and exponential (each ~2^-22 relative), i.e. well below 1e-6 relative for the
-// exponents and magnitudes of this pass.
-__device__ __forceinline__ float pow_sfu(float x, float y) {
-    float l, r;
-    asm("lg2.approx.f32 %0, %1;" : "=f"(l) : "f"(x));
-    const float e = y * l;
-    asm("ex2.approx.f32 %0, %1;" : "=f"(r) : "f"(e));
-    return r;
-}
-
-__device__ __forceinline__ Row load_row(const float *__restrict__ h, size_t pitch, int H, int y, int xl, int x,
-                                        int xr) {
-    const float *p = h + (size_t)min(max(y, 0), H - 1) * pitch;  // theta clamped
-    return Row{__ldg(p + xl), __ldg(p + x), __ldg(p + xr)};
-}
-
-// compute_caustic_intensity (caustics_compute.wgsl:87-111) from the 3 x 3 neighbourhood:
-// a = row above (y - 1), b = the cell's row, c = row below (y + 1)
-__device__ __forceinline__ float intensity(const sbs_caustic_params &p, Row a, Row b, Row c) {
-    const float center = b.c, left = b.l, right = b.r, up = a.c, down = c.c;
-    const float ul = a.l, ur = a.r, dl = c.l, dr = c.r;
-    // thickness_gradient (h = 1)
-    const float gx = (right - left) / 2.0f, gy = (down - up) / 2.0f;
-    // thickness_laplacian
-    const float lap = (left + right + up + down - 4.0f * center) / 1.0f;
-    // thickness_hessian_det
-    const float d2x = (left + right - 2.0f * center) / 1.0f;
-    const float d2y = (up + down - 2.0f * center) / 1.0f;
-    const float dxy = (dr - dl - ur + ul) / 4.0f;
-    const float hdet = d2x * d2y - dxy * dxy;
-    const float curvature = -lap * p.focal_length;
-    const float focusing = 1.0f / fmaxf(fabsf(1.0f - curvature), 0.01f);
-    const float branch = hdet < -p.branch_threshold ? 1.5f : 1.0f;
-    const float gmag = sqrtf(gx * gx + gy * gy);
-    const float refraction = 1.0f + gmag * 0.5f;
-    float it = focusing * branch * refraction;
-    it = pow_sfu(it, p.caustic_sharpness);  // it >= 0.01 (the focusing clamp keeps it positive)
-    it *= p.caustic_intensity;
-    return fminf(fmaxf(it, 0.0f), 10.0f);
-}
 
 // One thread per column, walking kRows rows with the three-row window in registers.
 __global__ void __launch_bounds__(kCols) caustics_kernel(sbs_caustic_params p, const float *__restrict__ h,
@@ -76,12 +31,13 @@ __global__ void __launch_bounds__(kCols) caustics_kernel(sbs_caustic_params p, c
     if (x >= W) return;
     const int xl = x == 0 ? W - 1 : x - 1, xr = x + 1 == W ? 0 : x + 1;  // phi wrapped
     const int y0 = blockIdx.y * kRows, y1 = min(H, y0 + kRows);
-    Row a = load_row(h, pitch, H, y0 - 1, xl, x, xr);
-    Row b = load_row(h, pitch, H, y0, xl, x, xr);
+    CausticRow a = caustic_load_row(h, pitch, H, y0 - 1, xl, x, xr);
+    CausticRow b = caustic_load_row(h, pitch, H, y0, xl, x, xr);
 #pragma unroll 4
     for (int y = y0; y < y1; ++y) {
-        const Row c = load_row(h, pitch, H, y + 1, xl, x, xr);
-        out[(size_t)y * W + x] = intensity(p, a, b, c);
+        const CausticRow c = caustic_load_row(h, pitch, H, y + 1, xl, x, xr);
+        out[(size_t)y * W + x] =
+            caustic_intensity(p.focal_length, p.caustic_intensity, p.caustic_sharpness, p.branch_threshold, a, b, c);
         a = b;
         b = c;
     }

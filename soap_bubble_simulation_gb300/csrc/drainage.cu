@@ -237,6 +237,7 @@ int allocate(sbs_drainage *h) {
     if (h->sem == SBS_WGSL_SEMANTICS && wtb_supported(h->nt, h->np)) {
         h->wtb_k = 4;
         h->wgeom = wtb_geometry(h->nt, h->np, h->wtb_k);
+        h->cau_geom = wtb_geometry(h->nt, h->np, kWtbCausticK);
     }
     if (h->sem == SBS_CPU_SEMANTICS) {
         // steps per launch measured fastest at 2048 x 4096: 3 for the compensated storage (19.7 us
@@ -315,16 +316,27 @@ void release(sbs_drainage *h) {
     cudaFree(h->qbuf);
     cudaFree(h->ring_part);
     cudaFree(h->ring_bar);
+    cudaFree(h->cau_buf);
     if (h->ring_status) cudaFreeHost(h->ring_status);
     if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+// Whether a chunk of `count` WGSL passes ends with the launch that also writes the caustic map:
+// the final chunk of a run that asked for the map, blocked, with three passes before the final
+// single pass (the map is of the field one pass behind the newest, the buffer the renderer binds).
+bool cau_plan(const sbs_drainage *h, int count, bool last_single) {
+    return h->cau_on && h->sem == SBS_WGSL_SEMANTICS && h->wtb_k > 1 && last_single && h->cau_geom.nby > 0 &&
+           count - 1 >= kWtbCausticK;
 }
 
 // Enqueues `count` steps starting from buffer `start`; returns the buffer holding the result.
 // CPU semantics: step i reads pole rows from memory when i == 0 (the chunk starts from a
 // materialised field) and from the ring partials of step i-1 otherwise; the chunk ends by
 // materialising the pole rows. WGSL semantics: runs of wtb_k steps go through the temporally
-// blocked kernel; with last_single the final step is a single-step launch, so the other buffer
-// ends one pass behind the newest (what the reference's current_buffer() returns).
+// blocked kernel, a remainder of 2 or 3 through one shorter blocked launch; with last_single the
+// final step is a single-step launch, so the other buffer ends one pass behind the newest (what
+// the reference's current_buffer() returns). A run that asks for the caustic map ends
+// [..., blocked launch of kWtbCausticK passes that writes the map of its result, single pass].
 int enqueue_steps(sbs_drainage *h, int start, int count, float dt, bool vol_last, bool use_sched, bool last_single,
                   int *end) {
     const Consts &k = consts_of(h);
@@ -385,14 +397,20 @@ int enqueue_steps(sbs_drainage *h, int start, int count, float dt, bool vol_last
         *end = cur;
         return SBS_OK;
     }
-    std::vector<int> plan;  // steps per launch
+    std::vector<int> plan;  // steps per launch; -kWtbCausticK: the launch that also writes the map
     if (h->sem == SBS_WGSL_SEMANTICS && h->wtb_k > 1) {
-        int rem = count - (last_single && count > 0 ? 1 : 0);
+        const bool cau = cau_plan(h, count, last_single);
+        int rem = count - (last_single && count > 0 ? 1 : 0) - (cau ? kWtbCausticK : 0);
         while (rem >= h->wtb_k) {
             plan.push_back(h->wtb_k);
             rem -= h->wtb_k;
         }
+        if (rem >= 2) {  // a remainder of 2 or 3 passes in one shorter blocked launch
+            plan.push_back(rem);
+            rem = 0;
+        }
         for (; rem > 0; --rem) plan.push_back(1);
+        if (cau) plan.push_back(-kWtbCausticK);
         if (last_single && count > 0) plan.push_back(1);
     } else {
         plan.assign(count, 1);
@@ -419,7 +437,16 @@ int enqueue_steps(sbs_drainage *h, int start, int count, float dt, bool vol_last
         a.nt = h->nt;
         a.np = h->np;
         a.pitch = (int)h->pitch;
-        a.rb = plan[i] > 1 ? h->wgeom.rb : h->geom.rb;
+        const bool cau_launch = plan[i] < 0;
+        const int steps = cau_launch ? -plan[i] : plan[i];
+        a.rb = cau_launch ? h->cau_geom.rb : steps > 1 ? h->wgeom.rb : h->geom.rb;
+        if (cau_launch) {
+            a.cau_out = h->cau_out;
+            a.cau_focal = h->cau_p[0];
+            a.cau_scale = h->cau_p[1];
+            a.cau_sharp = h->cau_p[2];
+            a.cau_branch = h->cau_p[3];
+        }
         a.poles_virtual = i > 0 ? 1 : 0;
         a.marangoni = h->params.marangoni_enabled ? 1 : 0;
         a.crit = k.crit;
@@ -429,8 +456,8 @@ int enqueue_steps(sbs_drainage *h, int start, int count, float dt, bool vol_last
         a.Gt = k.Gt;
         a.M = k.M;
         a.dt = dt;
-        if (plan[i] > 1)
-            SBS_CUDA_TRY(launch_wtb(plan[i], a, h->wgeom, h->stream));
+        if (steps > 1)
+            SBS_CUDA_TRY(launch_wtb(steps, a, cau_launch ? h->cau_geom : h->wgeom, h->stream));
         else
             SBS_CUDA_TRY(launch_step(h->sem, h->x2, a, h->geom, h->stream));
         cur ^= 1;
@@ -447,8 +474,10 @@ int launches_in(const sbs_drainage *h, int count, bool last_single) {
     if (h->sem == SBS_CPU_SEMANTICS) return h->cpu_k > 1 ? count / h->cpu_k + count % h->cpu_k : count;
     if (!(h->sem == SBS_WGSL_SEMANTICS && h->wtb_k > 1)) return count;
     const int tail = last_single && count > 0 ? 1 : 0;
-    const int body = count - tail;
-    return body / h->wtb_k + body % h->wtb_k + tail;
+    const int cau = cau_plan(h, count, last_single) ? 1 : 0;
+    const int body = count - tail - cau * kWtbCausticK;
+    const int rem = body % h->wtb_k;
+    return body / h->wtb_k + (rem >= 2 ? 1 : rem) + cau + tail;
 }
 
 // Runs one chunk (count <= kMaxChunk) through a cached CUDA graph (or directly when short).
@@ -488,6 +517,12 @@ int run_chunk(sbs_drainage *h, int count, double dt, bool vol_last, bool last_si
                           ":" + std::to_string(use_sched) + ":" + std::to_string(bits) + ":" +
                           std::to_string(last_single) + ":" + std::to_string(h->wtb_k) + ":" +
                           std::to_string(h->cpu_k);
+        if (cau_plan(h, count, last_single)) {  // the map's destination and parameters are in the graph
+            uint32_t pb[4];
+            std::memcpy(pb, h->cau_p, sizeof(pb));
+            key += ":cau:" + std::to_string((uintptr_t)h->cau_out);
+            for (uint32_t v : pb) key += ":" + std::to_string(v);
+        }
         auto it = h->graphs.find(key);
         cudaGraphExec_t exec = nullptr;
         if (it == h->graphs.end()) {
@@ -510,6 +545,7 @@ int run_chunk(sbs_drainage *h, int count, double dt, bool vol_last, bool last_si
         end = h->cur ^ (launches_in(h, count, last_single) & 1);
         SBS_CUDA_TRY(cudaGraphLaunch(exec, h->stream));
     }
+    if (last_single && h->cau_on) h->cau_fused = cau_plan(h, count, last_single);
     h->cur = end;
     h->prev = end ^ 1;
     return SBS_OK;
@@ -552,6 +588,36 @@ int run_steps(sbs_drainage *h, double dt, uint64_t n, uint32_t check_every) {
         done += g;
     }
     if (h->tfe.error) return set_error(SBS_E_STATE, "TFE front columns are not one interval");
+    return SBS_OK;
+}
+
+// `passes` WGSL passes, then the caustic map of the field one pass behind the newest (the buffer
+// the reference's caustic renderer binds) into `map` (device or host memory): the final blocked
+// launch writes the map of its result, so the field is not read again; runs too short for that
+// launch use the standalone caustic pass.
+int run_with_caustics(sbs_drainage *h, uint32_t passes, const sbs_caustic_params *p, float *map, int mem) {
+    const size_t bytes = sizeof(float) * (size_t)h->np * (size_t)h->nt;
+    float *dst = map;
+    if (mem == SBS_MEM_HOST) {
+        if (!h->cau_buf) SBS_CUDA_TRY(cudaMalloc(&h->cau_buf, bytes));
+        dst = h->cau_buf;
+    }
+    h->cau_on = true;
+    h->cau_fused = false;
+    h->cau_out = dst;
+    h->cau_p[0] = p->focal_length;
+    h->cau_p[1] = p->caustic_intensity;
+    h->cau_p[2] = p->caustic_sharpness;
+    h->cau_p[3] = p->branch_threshold;
+    int rc = run_steps(h, 0.0, passes, 0);
+    h->cau_on = false;
+    if (rc) return rc;
+    if (!h->cau_fused) {
+        rc = sbs_caustics(p, h->h[h->prev], h->pitch, dst, SBS_MEM_DEVICE, h->stream);
+        if (rc) return rc;
+    }
+    if (mem == SBS_MEM_HOST) SBS_CUDA_TRY(cudaMemcpyAsync(map, dst, bytes, cudaMemcpyDeviceToHost, h->stream));
+    SBS_CUDA_TRY(cudaStreamSynchronize(h->stream));
     return SBS_OK;
 }
 
@@ -769,6 +835,37 @@ int sbs_gpu_drainage_run(sbs_drainage *h, uint32_t passes) {
     int rc = run_steps(h, 0.0, passes, 0);
     if (rc) return rc;
     SBS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return SBS_OK;
+}
+
+int sbs_gpu_drainage_run_caustics(sbs_drainage *h, uint32_t passes, const sbs_caustic_params *p, float *caustic_map,
+                                  int mem) {
+    clear_error();
+    CHECK_HANDLE(h);
+    REQUIRE_SEM(h, SBS_WGSL_SEMANTICS);
+    SBS_CHECK_ARG(p != nullptr && caustic_map != nullptr, "null argument");
+    SBS_CHECK_ARG(mem == SBS_MEM_HOST || mem == SBS_MEM_DEVICE, "bad mem flag %d", mem);
+    SBS_CHECK_ARG(p->grid_width == (uint32_t)h->np && p->grid_height == (uint32_t)h->nt,
+                  "caustic grid %ux%u differs from the handle's %dx%d", p->grid_width, p->grid_height, h->np, h->nt);
+    return run_with_caustics(h, passes, p, caustic_map, mem);
+}
+
+int sbs_gpu_drainage_step_caustics(sbs_drainage *h, float frame_dt, const sbs_caustic_params *p, float *caustic_map,
+                                   int mem) {
+    clear_error();
+    CHECK_HANDLE(h);
+    REQUIRE_SEM(h, SBS_WGSL_SEMANTICS);
+    SBS_CHECK_ARG(p != nullptr && caustic_map != nullptr, "null argument");
+    SBS_CHECK_ARG(mem == SBS_MEM_HOST || mem == SBS_MEM_DEVICE, "bad mem flag %d", mem);
+    SBS_CHECK_ARG(p->grid_width == (uint32_t)h->np && p->grid_height == (uint32_t)h->nt,
+                  "caustic grid %ux%u differs from the handle's %dx%d", p->grid_width, p->grid_height, h->np, h->nt);
+    const uint32_t passes = h->enabled ? h->steps_per_frame : 0u;  // gpu_drainage.rs:339-341
+    const float step_dt = frame_dt * h->time_scale / (float)h->steps_per_frame;
+    const double t0 = h->current_time;
+    int rc = run_with_caustics(h, passes, p, caustic_map, mem);
+    if (rc) return rc;
+    h->current_time = t0;
+    for (uint32_t i = 0; i < passes; ++i) h->current_time += (double)step_dt;
     return SBS_OK;
 }
 

@@ -47,11 +47,13 @@ __device__ __forceinline__ double wtb_block_sum(double v, double *smem) {
 // process each); four blocks (128 registers, spills) 15.49.
 constexpr int kMinBlocksPerSm = 3;
 
-template <int K, bool VOL, bool MAR>
+// CAU: the launch also writes the caustic map of its result (wtb_iter); K must be kWtbCausticK.
+template <int K, bool VOL, bool MAR, bool CAU = false>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, kMinBlocksPerSm) wtb_wgsl_kernel(const StepArgs a) {
+    constexpr int E = CAU ? 1 : 0;  // extra final rows on each side of the strip
     __shared__ double s_red[32];
     __shared__ int s_last;
-    extern __shared__ float4 s_co[];  // coefficient rows [r0 - K, r1 + K) of this strip
+    extern __shared__ float4 s_co[];  // coefficient rows [r0 - K - E, r1 + K + E) of this strip
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int np = a.np;
     const int seg = blockIdx.x * kWarpsPerBlock + warp;
@@ -77,9 +79,17 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kMinBlocksPerSm) wtb_wgsl
     w.dt = a.dt;
     w.crit = a.crit;
     w.vol_w = a.vol_w;
-    w.sco_base = w.r0 - K;
+    w.cau_out = CAU ? a.cau_out + col : nullptr;
+    w.cau_stride = np;
+    w.cau_j0 = w.r0 == 1 ? 0 : w.r0;
+    w.cau_j1 = w.r1 == a.nt - 1 ? a.nt : w.r1;
+    w.cau_focal = a.cau_focal;
+    w.cau_scale = a.cau_scale;
+    w.cau_sharp = a.cau_sharp;
+    w.cau_branch = a.cau_branch;
+    w.sco_base = w.r0 - K - E;
     w.sco = s_co;
-    for (int i = threadIdx.x; i < a.rb + 2 * K; i += blockDim.x) {
+    for (int i = threadIdx.x; i < a.rb + 2 * (K + E); i += blockDim.x) {
         const int r = w.sco_base + i;
         s_co[i] = (r >= 0 && r < a.nt) ? __ldg(a.rows + r) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
@@ -94,17 +104,21 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kMinBlocksPerSm) wtb_wgsl
             wc[l][s] = wh[l][s];
         }
 
+    float4 wk[3];  // the last three final rows (CAU)
+#pragma unroll
+    for (int s = 0; s < 3; ++s) wk[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+
     double vacc = 0.0;
-    const int t0 = w.r0 - K, t1 = w.r1 + K;  // level-0 rows [t0, t1)
+    const int t0 = w.r0 - K - E, t1 = w.r1 + K + E;  // level-0 rows [t0, t1)
     float4 ph = make_float4(0.f, 0.f, 0.f, 0.f), pc = ph;
     if (SBS_WTB_PREFETCH && t0 >= 0) {
         ph = __ldg(reinterpret_cast<const float4 *>(w.hin + (size_t)t0 * w.pitch));
         pc = __ldg(reinterpret_cast<const float4 *>(w.cin + (size_t)t0 * w.pitch));
     }
     for (int t = t0; t < t1; t += 3) {
-        wtb_iter<K, 0, VOL, MAR>(w, t, wh, wc, ph, pc, vacc);
-        if (t + 1 < t1) wtb_iter<K, 1, VOL, MAR>(w, t + 1, wh, wc, ph, pc, vacc);
-        if (t + 2 < t1) wtb_iter<K, 2, VOL, MAR>(w, t + 2, wh, wc, ph, pc, vacc);
+        wtb_iter<K, 0, VOL, MAR, false, CAU>(w, t, wh, wc, ph, pc, vacc, wk);
+        if (t + 1 < t1) wtb_iter<K, 1, VOL, MAR, false, CAU>(w, t + 1, wh, wc, ph, pc, vacc, wk);
+        if (t + 2 < t1) wtb_iter<K, 2, VOL, MAR, false, CAU>(w, t + 2, wh, wc, ph, pc, vacc, wk);
     }
 
     if (VOL) {
@@ -146,7 +160,12 @@ const void *wtb_fn(bool vol, bool mar) {
     return mar ? (const void *)wtb_wgsl_kernel<K, false, true> : (const void *)wtb_wgsl_kernel<K, false, false>;
 }
 
-const void *wtb_kernel(int K, bool vol, bool mar) {
+const void *wtb_kernel(int K, bool vol, bool mar, bool cau = false) {
+    if (cau) {
+        if (K != kWtbCausticK || vol) return nullptr;
+        return mar ? (const void *)wtb_wgsl_kernel<kWtbCausticK, false, true, true>
+                   : (const void *)wtb_wgsl_kernel<kWtbCausticK, false, false, true>;
+    }
     switch (K) {
         case 2:
             return wtb_fn<2>(vol, mar);
@@ -185,11 +204,12 @@ StepGeom wtb_geometry(int nt, int np, int K) {
 }
 
 cudaError_t launch_wtb(int K, const StepArgs &a, const StepGeom &g, cudaStream_t s) {
-    const void *fn = wtb_kernel(K, a.vol_w != nullptr, a.marangoni != 0);
+    const bool cau = a.cau_out != nullptr;
+    const void *fn = wtb_kernel(K, a.vol_w != nullptr, a.marangoni != 0, cau);
     if (fn == nullptr) return cudaErrorInvalidValue;
     dim3 grid(g.nbx, g.nby), block(kWarpsPerBlock * 32);
     void *args[] = {(void *)&a};
-    return cudaLaunchKernel(fn, grid, block, args, sizeof(float4) * (g.rb + 2 * K), s);
+    return cudaLaunchKernel(fn, grid, block, args, sizeof(float4) * (g.rb + 2 * (K + (cau ? 1 : 0))), s);
 }
 
 }  // namespace sbs

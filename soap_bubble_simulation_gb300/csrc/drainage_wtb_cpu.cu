@@ -45,7 +45,6 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kSegStride = 120;  // output columns per warp
-constexpr int kMaxWarps = 8;      // warps per block
 // Registers per thread: 128 lets four blocks of four warps share an SM. The pipeline needs more
 // warps more than fewer spills (an earlier, cluster-launched form at 2048 x 4096: compensated
 // K = 2 32.8 us per step capped at 128 registers against 36-38 us with its own ~138).

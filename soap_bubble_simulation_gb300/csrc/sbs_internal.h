@@ -109,6 +109,9 @@ struct StepArgs {
     long long wait_cycles;  // barrier wait limit
     unsigned extra;         // arrivals beyond the strip's blocks (1 only in the timeout test)
     int prow;               // rows of each polar strip (0: all strips even)
+    // blocked WGSL step only: the caustic map of the launch's result (nullptr: none)
+    float *cau_out;         // grid_width x grid_height floats, row stride np
+    float cau_focal, cau_scale, cau_sharp, cau_branch;
 };
 
 struct StepGeom {
@@ -124,6 +127,9 @@ StepGeom step_geometry(int nt, int np, int semantics, int x2);
 bool wtb_supported(int nt, int np);
 StepGeom wtb_geometry(int nt, int np, int K);
 cudaError_t launch_wtb(int K, const StepArgs &a, const StepGeom &g, cudaStream_t s);
+// K for a launch that also writes the caustic map of its result (a.cau_out): its final level must
+// leave one valid column beyond the kept 120 on each side of a warp's window.
+constexpr int kWtbCausticK = 3;
 // Temporally blocked CPU-semantics step (K = 2..4 steps per launch, pole means and fronts
 // included), drainage_wtb_cpu.cu. Each row strip is nbx blocks of wx warps that span the ring;
 // nby strips of at most rb rows, all resident at once (cooperative launch). nby == 0: the grid
@@ -243,6 +249,13 @@ struct sbs_drainage {
     unsigned *ring_status = nullptr;   // host-mapped timeout word
     unsigned *ring_status_dev = nullptr;
     unsigned wait_epoch = 0;           // the wait settings the captured graphs were made with
+    // caustic map written by the run in progress (sbs_gpu_drainage_run_caustics)
+    bool cau_on = false;
+    bool cau_fused = false;            // the final chunk of the last run wrote the map
+    float *cau_out = nullptr;          // device destination of the map
+    float cau_p[4] = {0.f, 0.f, 0.f, 0.f};  // focal length, intensity, sharpness, branch threshold
+    float *cau_buf = nullptr;          // device map for calls with host memory
+    sbs::StepGeom cau_geom{};          // geometry of the launch that writes the map
 
     // CPU semantics parameters (from sbs_config)
     sbs_config cfg{};

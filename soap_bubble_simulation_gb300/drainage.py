@@ -462,6 +462,29 @@ class GPUDrainageSimulator(_Handle):
                N.MEM_HOST)
         return out
 
+    def run_caustic_map(self, passes: int, params=None) -> np.ndarray:
+        """run(passes) followed by caustic_map(params, which=1), with the map written by the run's
+        final blocked launch (the field is not read again)."""
+        from .caustics import CausticParams
+
+        nt, np_ = self.grid()
+        p = params if params is not None else CausticParams.default(np_, nt)
+        out = np.empty((nt, np_), dtype=np.float32)
+        N.call("sbs_gpu_drainage_run_caustics", self.handle, int(passes), C.cast(C.byref(p), C.c_void_p), N.ptr(out),
+               N.MEM_HOST)
+        return out
+
+    def step_caustic_map(self, frame_dt: float, params=None) -> np.ndarray:
+        """step(frame_dt) followed by the caustic map of the buffer the renderer binds."""
+        from .caustics import CausticParams
+
+        nt, np_ = self.grid()
+        p = params if params is not None else CausticParams.default(np_, nt)
+        out = np.empty((nt, np_), dtype=np.float32)
+        N.call("sbs_gpu_drainage_step_caustics", self.handle, float(frame_dt), C.cast(C.byref(p), C.c_void_p),
+               N.ptr(out), N.MEM_HOST)
+        return out
+
     def concentration_buffer(self) -> DeviceField:
         """The reference's concentration_buffer() (gpu_drainage.rs:458-460), same indexing as
         current_buffer()."""
