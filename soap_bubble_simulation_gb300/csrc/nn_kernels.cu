@@ -1,16 +1,16 @@
 // Training-side kernels of the drainage surrogate (include/sbs_nn.h) and its layered forward
-// pass: features, 3x3 convolutions as implicit GEMMs on the tensor cores (mma.sync BF16 x BF16 ->
-// FP32), the one-channel output layer and its gradients on the FP32 pipe, loss, deterministic
-// gradient reduction, Adam, and weight packing.
+// pass: features, the weight gradients of the 3x3 convolutions (implicit GEMMs on warp-level
+// mma.sync BF16 x BF16 -> FP32), the one-channel output layer and its gradients on the FP32 pipe,
+// loss, deterministic gradient reduction, Adam, and weight packing. The convolutions themselves
+// (forward and transposed) run on tcgen05 (nn_conv_tc.cu).
 //
 // Layouts (channel-last, cells = fields x nt x np):
 //   features x        BF16 [cells][16]
 //   pre-activations y FP32 [cells][32]       activations a BF16 [cells][32]
 //   output y4 / gradient g4 FP32 [cells]     layer gradients g BF16 [cells][32]
-// A convolution tile is one row segment of kTileCols = 128 cells of one field: the block stages
-// the three input rows it reads (reflected in theta, periodic in phi) and the packed weights in
-// shared memory, and its four warps each compute 32 cells x 32 channels with m16n8k16 MMAs whose
-// A fragments are gathered by ldmatrix from the shifted rows (no im2col buffer).
+// A weight-gradient tile is one row segment of kTileCols = 128 cells of one field: the block
+// stages the three input rows it reads (reflected in theta, periodic in phi) in shared memory and
+// gathers MMA fragments with ldmatrix from the shifted rows (no im2col buffer).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -27,12 +27,6 @@ namespace nn {
 namespace {
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void ldsm_x4(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-                 : "r"(addr));
-}
 
 __device__ __forceinline__ void ldsm_x4_t(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
     asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0, %1, %2, %3}, [%4];"
@@ -82,156 +76,6 @@ __global__ void features_kernel(Fields fs, GridTab g, uint4 *x) {
     uint4 *o = x + (((size_t)b * nt + i) * np + j) * 2;
     o[0] = p0;
     o[1] = p1;
-}
-
-// ------------------------------------------------------------------ 3x3 convolution (mma.sync)
-// BWD = false: y = conv(x, W) + b, a = bf16(act(y))     (x: CIN channels, packed W [oc][tap*CIN+ic])
-// BWD = true : dX = conv^T(g, W), g_prev = bf16(dX * act'(y_prev))  (g: 32 channels, packed W
-//              [ic][tap*32+oc]); the transpose reads g at (i - dy, j - dx) with zero rows outside
-//              the grid, plus the reflected sources: row 1 also receives output row 0's dy = -1
-//              taps, row nt-2 output row nt-1's dy = +1 taps.
-struct ConvArgs {
-    const bf16 *in;
-    const bf16 *w;
-    const float *bias;
-    const float *yprev;
-    float *yout;
-    bf16 *aout;
-    int nt, np, tiles_x;
-    int act;  // SBS_NN_ACT_*
-};
-
-template <int CIN, bool BWD>
-__global__ void __launch_bounds__(128) conv_kernel(ConvArgs a) {
-    constexpr int KC = 9 * CIN / 8 + (CIN == 8 ? 1 : 0);  // 16-byte K chunks (padded to even)
-    constexpr int KS = KC / 2;                             // k16 steps
-    constexpr int KP = KC * 8;                             // packed K
-    constexpr int WS = KP + 8;                             // smem weight row stride (elements)
-    constexpr int CPC = CIN / 8;                           // chunks per cell
-    constexpr int CB = CIN * 2;                            // bytes per staged cell
-    constexpr int ROWB = kRowCells * CB;
-    extern __shared__ __align__(16) uint8_t smem[];
-    uint8_t *sIn = smem;                    // 4 row buffers
-    bf16 *sW = (bf16 *)(smem + 4 * ROWB);   // [32][WS]
-
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int tile = blockIdx.x;
-    const int tx = tile % a.tiles_x;
-    const int row_id = tile / a.tiles_x;  // field * nt + i
-    const int i = row_id % a.nt, b = row_id / a.nt;
-    const int nt = a.nt, np = a.np, j0 = tx * kTileCols;
-
-    // weights
-    for (int e = tid; e < 32 * KP / 8; e += 128) {
-        const int n = e / (KP / 8), k8 = e % (KP / 8);
-        *(uint4 *)(sW + n * WS + k8 * 8) = *(const uint4 *)(a.w + (size_t)n * KP + k8 * 8);
-    }
-    // source rows: buffer dy+1 holds the row read by taps with row offset dy; buffer 3 the extra
-    int src[4];
-    int extra_t0 = -1;
-    if (!BWD) {
-        src[0] = refl_row(i - 1, nt);
-        src[1] = i;
-        src[2] = refl_row(i + 1, nt);
-        src[3] = -1;
-    } else {
-        src[0] = i + 1 < nt ? i + 1 : -1;  // dy = -1 reads g at i + 1
-        src[1] = i;
-        src[2] = i - 1 >= 0 ? i - 1 : -1;  // dy = +1 reads g at i - 1
-        src[3] = -1;
-        if (i == 1) {
-            src[3] = 0;
-            extra_t0 = 0;  // taps (dy = -1, dx = -1..1)
-        } else if (i == nt - 2) {
-            src[3] = nt - 1;
-            extra_t0 = 6;  // taps (dy = +1, dx = -1..1)
-        }
-    }
-    const bf16 *base = a.in + (size_t)b * nt * np * CIN;
-    for (int e = tid; e < 4 * kRowCells * CPC; e += 128) {
-        const int rb = e / (kRowCells * CPC), r = e % (kRowCells * CPC);
-        const int q = r / CPC, ch = r % CPC;
-        int col = (j0 - 1 + q) % np;
-        col = col < 0 ? col + np : col;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (src[rb] >= 0) v = *(const uint4 *)(base + ((size_t)src[rb] * np + col) * CIN + ch * 8);
-        *(uint4 *)(sIn + rb * ROWB + cell_off<CIN>(q, ch)) = v;
-    }
-    __syncthreads();
-
-    float acc[2][4][4];
-#pragma unroll
-    for (int m = 0; m < 2; ++m)
-#pragma unroll
-        for (int n = 0; n < 4; ++n)
-#pragma unroll
-            for (int r = 0; r < 4; ++r) acc[m][n][r] = 0.f;
-
-    const uint32_t sIn_u = smem_addr(sIn), sW_u = smem_addr(sW);
-    const int q8 = lane >> 3, r8 = lane & 7;
-
-    auto kstep = [&](int c0, int buf_override) {
-        // A: two m-tiles
-        uint32_t af[2][4];
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt) {
-            const int rr = (q8 & 1) * 8 + r8;
-            int c = c0 + (q8 >> 1);
-            if (c >= 9 * CPC) c = 0;  // K padding chunk: finite data against zero weights
-            const int t = c / CPC, ch = c % CPC;
-            const int dy = t / 3 - 1, dx = t % 3 - 1;
-            const int buf = buf_override >= 0 ? buf_override : dy + 1;
-            const int q = 32 * warp + 16 * mt + rr + (BWD ? -dx : dx) + 1;
-            ldsm_x4(sIn_u + buf * ROWB + cell_off<CIN>(q, ch), af[mt][0], af[mt][1], af[mt][2], af[mt][3]);
-        }
-        // B: four n-tiles, two ldmatrix.x4
-#pragma unroll
-        for (int p = 0; p < 2; ++p) {
-            const int n = (2 * p + (q8 >> 1)) * 8 + r8;
-            const int k = c0 * 8 + (q8 & 1) * 8;
-            uint32_t b0, b1, b2, b3;
-            ldsm_x4(sW_u + (n * WS + k) * 2, b0, b1, b2, b3);
-#pragma unroll
-            for (int mt = 0; mt < 2; ++mt) {
-                mma16816(acc[mt][2 * p], af[mt], b0, b1);
-                mma16816(acc[mt][2 * p + 1], af[mt], b2, b3);
-            }
-        }
-    };
-
-#pragma unroll 2
-    for (int s = 0; s < KS; ++s) kstep(2 * s, -1);
-    if (BWD && extra_t0 >= 0) {
-        for (int s = 0; s < 3 * CPC / 2; ++s) kstep(extra_t0 * CPC + 2 * s, 3);
-    }
-
-    // epilogue
-    const int g = lane >> 2, q4 = lane & 3;
-    const size_t cell0 = ((size_t)b * nt + i) * np;
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt) {
-#pragma unroll
-        for (int hr = 0; hr < 2; ++hr) {
-            const int m = 32 * warp + 16 * mt + g + 8 * hr;
-            const int j = j0 + m;
-            if (j >= np) continue;
-            const size_t cell = cell0 + j;
-#pragma unroll
-            for (int nn = 0; nn < 4; ++nn) {
-                const int n = nn * 8 + 2 * q4;
-                const float v0 = acc[mt][nn][2 * hr], v1 = acc[mt][nn][2 * hr + 1];
-                if (!BWD) {
-                    const float y0 = __fadd_rn(v0, a.bias[n]), y1 = __fadd_rn(v1, a.bias[n + 1]);
-                    *(float2 *)(a.yout + cell * 32 + n) = make_float2(y0, y1);
-                    *(uint32_t *)(a.aout + cell * 32 + n) = pack2(act(a.act, y0), act(a.act, y1));
-                } else {
-                    const float2 yp = *(const float2 *)(a.yprev + cell * 32 + n);
-                    *(uint32_t *)(a.aout + cell * 32 + n) =
-                        pack2(__fmul_rn(v0, act_grad(a.act, yp.x)), __fmul_rn(v1, act_grad(a.act, yp.y)));
-                }
-            }
-        }
-    }
 }
 
 // ------------------------------------------------------- weight gradient of a 3x3 convolution
@@ -417,51 +261,72 @@ __global__ void out_kernel(OutArgs a) {
     }
 }
 
-// dW4[tap][ic] = sum g4[cell] a3[src(cell,tap)][ic], db4 = sum g4: 289 threads per block, each
-// block a contiguous chunk of cells; partial rows [block][289].
+// dW4[tap][ic] = sum g4[cell] a3[src(cell,tap)][ic], db4 = sum g4. Block b takes the rows
+// b, b + nblocks, ... of the batch; its 8 warps split each row into 32-column chunks, lane = ic,
+// nine accumulators per lane (one per tap); g4 of a chunk is loaded once and broadcast by shuffle.
+// One partial row [289] per block, warps summed in a fixed order.
 struct Wgrad4Args {
     const float *g4;
     const bf16 *a3;
     float *partial;
     GridTab g;
-    size_t cells, chunk;
+    int rows;  // fields x nt
 };
 
-__global__ void wgrad4_kernel(Wgrad4Args a) {
-    __shared__ float sg[256];
-    const int tid = threadIdx.x;
-    const int t = tid / 32, ic = tid % 32;
+constexpr int kW4Warps = 8;
+
+__global__ void __launch_bounds__(32 * kW4Warps) wgrad4_kernel(Wgrad4Args a) {
+    __shared__ float sp[kW4Warps][289];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nt = a.g.nt, np = a.g.np;
-    const int dy = t / 3 - 1, dx = t % 3 - 1;
-    const size_t c0 = (size_t)blockIdx.x * a.chunk;
-    const size_t c1 = min(a.cells, c0 + a.chunk);
-    float acc = 0.f;
-    for (size_t cb = c0; cb < c1; cb += 256) {
-        __syncthreads();
-        if (tid < 256) sg[tid] = cb + tid < c1 ? a.g4[cb + tid] : 0.f;
-        __syncthreads();
-        const int n = (int)min((size_t)256, c1 - cb);
-        if (tid < 288) {
-            for (int k = 0; k < n; ++k) {
-                const float gv = sg[k];
-                if (gv == 0.f) continue;
-                const size_t c = cb + k;
-                const int j = (int)(c % np), i = (int)((c / np) % nt);
-                const size_t fb = (c / ((size_t)np * nt)) * nt * np;
-                const int r = refl_row(i + dy, nt);
-                int q = j + dx;
-                q = q < 0 ? q + np : (q >= np ? q - np : q);
-                acc = __fmaf_rn(gv, __bfloat162float(a.a3[(fb + (size_t)r * np + q) * 32 + ic]), acc);
+    float acc[9];
+#pragma unroll
+    for (int t = 0; t < 9; ++t) acc[t] = 0.f;
+    float gsum = 0.f;
+    for (int row = blockIdx.x; row < a.rows; row += gridDim.x) {
+        const int i = row % nt;
+        const size_t fb = (size_t)(row / nt) * nt * np;
+        const bf16 *s0 = a.a3 + (fb + (size_t)refl_row(i - 1, nt) * np) * 32 + lane;  // taps dy = -1
+        const bf16 *s1 = a.a3 + (fb + (size_t)i * np) * 32 + lane;                       // dy = 0
+        const bf16 *s2 = a.a3 + (fb + (size_t)refl_row(i + 1, nt) * np) * 32 + lane;  // dy = +1
+        for (int j0 = 32 * warp; j0 < np; j0 += 32 * kW4Warps) {
+            const float gl = j0 + lane < np ? a.g4[fb + (size_t)i * np + j0 + lane] : 0.f;
+            gsum = __fadd_rn(gsum, gl);
+            const int n = min(32, np - j0);
+            for (int jj = 0; jj < n; ++jj) {
+                const float gv = __shfl_sync(0xffffffffu, gl, jj);
+                if (gv == 0.f) continue;  // masked rows
+                const int j = j0 + jj;
+                const int ql = j == 0 ? np - 1 : j - 1, qr = j + 1 == np ? 0 : j + 1;
+                const size_t ol = (size_t)ql * 32, oc = (size_t)j * 32, orr = (size_t)qr * 32;
+                acc[0] = __fmaf_rn(gv, __bfloat162float(s0[ol]), acc[0]);
+                acc[1] = __fmaf_rn(gv, __bfloat162float(s0[oc]), acc[1]);
+                acc[2] = __fmaf_rn(gv, __bfloat162float(s0[orr]), acc[2]);
+                acc[3] = __fmaf_rn(gv, __bfloat162float(s1[ol]), acc[3]);
+                acc[4] = __fmaf_rn(gv, __bfloat162float(s1[oc]), acc[4]);
+                acc[5] = __fmaf_rn(gv, __bfloat162float(s1[orr]), acc[5]);
+                acc[6] = __fmaf_rn(gv, __bfloat162float(s2[ol]), acc[6]);
+                acc[7] = __fmaf_rn(gv, __bfloat162float(s2[oc]), acc[7]);
+                acc[8] = __fmaf_rn(gv, __bfloat162float(s2[orr]), acc[8]);
             }
-        } else if (tid == 288) {
-            for (int k = 0; k < n; ++k) acc = __fadd_rn(acc, sg[k]);
         }
     }
-    if (tid < 289) a.partial[(size_t)blockIdx.x * 289 + tid] = acc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) gsum = __fadd_rn(gsum, __shfl_xor_sync(0xffffffffu, gsum, o));
+#pragma unroll
+    for (int t = 0; t < 9; ++t) sp[warp][t * 32 + lane] = acc[t];
+    if (lane == 0) sp[warp][288] = gsum;
+    __syncthreads();
+    for (int k = threadIdx.x; k < 289; k += blockDim.x) {
+        float v = 0.f;
+        for (int w = 0; w < kW4Warps; ++w) v = __fadd_rn(v, sp[w][k]);
+        a.partial[(size_t)blockIdx.x * 289 + k] = v;
+    }
 }
 
-// g3[cell][ic] = bf16( (sum over the taps that read `cell` of g4[out] W4[tap][ic]) * act'(y3) ),
-// one warp per cell, lane = ic.
+// g3[cell][ic] = bf16( (sum over the taps that read `cell` of g4[out] W4[tap][ic]) * act'(y3) ):
+// one thread per cell with its 32 channels in registers (taps in the order t = 0..8, each tap's
+// pole-reflection source right after its own term).
 struct Dgrad4Args {
     const float *g4;
     const float *w4;
@@ -472,24 +337,47 @@ struct Dgrad4Args {
     int act;  // SBS_NN_ACT_*
 };
 
-__global__ void dgrad4_kernel(Dgrad4Args a) {
-    const size_t c = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int ic = threadIdx.x & 31;
+__global__ void __launch_bounds__(256) dgrad4_kernel(Dgrad4Args a) {
+    __shared__ float sw[288];
+    for (int k = threadIdx.x; k < 288; k += blockDim.x) sw[k] = a.w4[k];
+    __syncthreads();
+    const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= a.cells) return;
     const int nt = a.g.nt, np = a.g.np;
     const int j = (int)(c % np), i = (int)((c / np) % nt);
     const size_t fb = (c / ((size_t)np * nt)) * nt * np;
-    float s = 0.f;
+    float s[32];
+#pragma unroll
+    for (int ic = 0; ic < 32; ++ic) s[ic] = 0.f;
+#pragma unroll
     for (int t = 0; t < 9; ++t) {
         const int dy = t / 3 - 1, dx = t % 3 - 1;
         const int r = i - dy;
         int q = j - dx;
         q = q < 0 ? q + np : (q >= np ? q - np : q);
-        if (r >= 0 && r < nt) s = __fmaf_rn(a.g4[fb + (size_t)r * np + q], a.w4[t * 32 + ic], s);
-        if (i == 1 && dy == -1) s = __fmaf_rn(a.g4[fb + q], a.w4[t * 32 + ic], s);
-        if (i == nt - 2 && dy == 1) s = __fmaf_rn(a.g4[fb + (size_t)(nt - 1) * np + q], a.w4[t * 32 + ic], s);
+        const float gm = r >= 0 && r < nt ? a.g4[fb + (size_t)r * np + q] : 0.f;
+        const bool xt = i == 1 && dy == -1, xb = i == nt - 2 && dy == 1;
+        const float ge = xt ? a.g4[fb + q] : xb ? a.g4[fb + (size_t)(nt - 1) * np + q] : 0.f;
+        const bool has_m = r >= 0 && r < nt;
+#pragma unroll
+        for (int ic = 0; ic < 32; ++ic) {
+            if (has_m) s[ic] = __fmaf_rn(gm, sw[t * 32 + ic], s[ic]);
+            if (xt || xb) s[ic] = __fmaf_rn(ge, sw[t * 32 + ic], s[ic]);
+        }
     }
-    a.g3[c * 32 + ic] = __float2bfloat16_rn(__fmul_rn(s, act_grad(a.act, a.y3[c * 32 + ic])));
+    const float4 *yp = reinterpret_cast<const float4 *>(a.y3 + c * 32);
+    uint4 *gp = reinterpret_cast<uint4 *>(a.g3 + c * 32);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float4 y0 = yp[2 * k], y1 = yp[2 * k + 1];
+        const float v[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
+        uint32_t w[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+            w[e] = pack2(__fmul_rn(s[8 * k + 2 * e], act_grad(a.act, v[2 * e])),
+                         __fmul_rn(s[8 * k + 2 * e + 1], act_grad(a.act, v[2 * e + 1])));
+        gp[k] = make_uint4(w[0], w[1], w[2], w[3]);
+    }
 }
 
 // sum of partial rows (fixed order) scattered into the canonical parameter layout
@@ -609,26 +497,11 @@ __global__ void masked_err_kernel(const float *a, size_t pa, const float *b, siz
     }
 }
 
-template <int CIN, bool BWD>
-size_t conv_smem() {
-    constexpr int KC = 9 * CIN / 8 + (CIN == 8 ? 1 : 0);
-    return (size_t)4 * kRowCells * CIN * 2 + (size_t)32 * (KC * 8 + 8) * 2;
-}
-
 template <int CIN>
 size_t wgrad_smem() {
     return (size_t)3 * kRowCells * CIN * 2 + (size_t)kTileCols * 64;
 }
 
-template <int CIN, bool BWD>
-cudaError_t launch_conv(const ConvArgs &a, int nf, cudaStream_t st) {
-    const size_t sm = conv_smem<CIN, BWD>();
-    cudaError_t e = cudaFuncSetAttribute(conv_kernel<CIN, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-    const unsigned tiles = (unsigned)(a.tiles_x * a.nt * nf);
-    conv_kernel<CIN, BWD><<<tiles, 128, sm, st>>>(a);
-    return cudaGetLastError();
-}
 
 }  // namespace
 
@@ -639,39 +512,6 @@ cudaError_t features(const Fields &fs, int nf, const GridTab &g, bf16 *x, cudaSt
     return cudaGetLastError();
 }
 
-cudaError_t conv_forward(int layer, const bf16 *in, const Packed &p, float *y, bf16 *a, int nf, int nt, int np,
-                         cudaStream_t st) {
-    ConvArgs c{};
-    c.in = in;
-    c.yout = y;
-    c.aout = a;
-    c.nt = nt;
-    c.np = np;
-    c.tiles_x = (np + kTileCols - 1) / kTileCols;
-    c.act = p.act;
-    if (layer == 1) {
-        c.w = p.wf1;
-        c.bias = p.b;
-        return launch_conv<16, false>(c, nf, st);
-    }
-    c.w = layer == 2 ? p.wf2 : p.wf3;
-    c.bias = p.b + 32 * (layer - 1);
-    return launch_conv<32, false>(c, nf, st);
-}
-
-cudaError_t conv_backward_data(int layer, const bf16 *g, const Packed &p, const float *yprev, bf16 *gprev, int nf,
-                               int nt, int np, cudaStream_t st) {
-    ConvArgs c{};
-    c.in = g;
-    c.w = layer == 2 ? p.wb2 : p.wb3;
-    c.yprev = yprev;
-    c.aout = gprev;
-    c.act = p.act;
-    c.nt = nt;
-    c.np = np;
-    c.tiles_x = (np + kTileCols - 1) / kTileCols;
-    return launch_conv<32, true>(c, nf, st);
-}
 
 cudaError_t conv_backward_weight(int layer, const bf16 *g, const bf16 *x, float *partial, int nblocks, float *grad,
                                  int nf, int nt, int np, cudaStream_t st) {
@@ -733,9 +573,8 @@ cudaError_t output_backward(const float *g4, const bf16 *a3, const float *y3, co
     w.a3 = a3;
     w.partial = partial;
     w.g = g;
-    w.cells = cells;
-    w.chunk = (cells + nblocks - 1) / nblocks;
-    wgrad4_kernel<<<nblocks, 320, 0, st>>>(w);
+    w.rows = nf * g.nt;
+    wgrad4_kernel<<<nblocks, 32 * kW4Warps, 0, st>>>(w);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     reduce4_kernel<<<2, 256, 0, st>>>(partial, nblocks, grad + SBS_NN_W4, grad + SBS_NN_B4);
@@ -748,7 +587,7 @@ cudaError_t output_backward(const float *g4, const bf16 *a3, const float *y3, co
     d.g = g;
     d.cells = cells;
     d.act = p.act;
-    dgrad4_kernel<<<(unsigned)((cells + 7) / 8), 256, 0, st>>>(d);
+    dgrad4_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, st>>>(d);
     return cudaGetLastError();
 }
 

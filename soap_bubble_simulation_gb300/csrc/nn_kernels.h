@@ -18,6 +18,7 @@ struct Packed {
     float *w4;  // [9][32]   layer 4, BF16-rounded values in FP32
     float *b;   // [97]      b1 | b2 | b3 | b4
     int act;    // SBS_NN_ACT_* of the network
+    unsigned *err;  // device word: nonzero after a timed-out wait of the tensor-core convolutions
 };
 
 cudaError_t features(const Fields &fs, int nf, const GridTab &g, bf16 *x, cudaStream_t st);

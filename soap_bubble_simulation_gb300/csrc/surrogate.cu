@@ -223,6 +223,23 @@ Fields make_fields(const float *h, const float *c, size_t pitch, size_t field_st
     return fs;
 }
 
+// A timed-out wait of the tensor-core convolutions (herr: the error word, read after the stream
+// drained) becomes SBS_E_TIMEOUT; the word is cleared for the next call.
+int tc_result(sbs_surrogate *s, unsigned herr) {
+    if (!herr) return SBS_OK;
+    SBS_CUDA_TRY(cudaMemsetAsync(s->pk.err, 0, sizeof(unsigned), s->stream));
+    SBS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return set_error(SBS_E_TIMEOUT, "surrogate: a tensor-core convolution wait timed out");
+}
+
+// Reads the error word after the work queued so far (synchronises the stream).
+int tc_status(sbs_surrogate *s) {
+    unsigned herr = 0;
+    SBS_CUDA_TRY(cudaMemcpyAsync(&herr, s->pk.err, sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream));
+    SBS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return tc_result(s, herr);
+}
+
 int layered_forward(sbs_surrogate *s, const Fields &fs, int nf, const GridDev &g) {
     const int nt = g.nt, np = g.np;
     SBS_CUDA_TRY(features(fs, nf, g.tab(), s->x0, s->stream));
@@ -250,13 +267,17 @@ int loss_and_grad(sbs_surrogate *s, const Fields &fs, int nf, const GridDev &g, 
     SBS_CUDA_TRY(conv_backward_weight(1, s->g1, s->x0, s->partial, s->nblocks, s->grad, nf, nt, np, s->stream));
     if (loss) {
         std::vector<double> lp(nlb);
+        unsigned herr = 0;
         SBS_CUDA_TRY(cudaMemcpyAsync(lp.data(), s->loss_part, sizeof(double) * nlb, cudaMemcpyDeviceToHost, s->stream));
+        SBS_CUDA_TRY(cudaMemcpyAsync(&herr, s->pk.err, sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream));
         SBS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        if ((rc = tc_result(s, herr))) return rc;
         double sum = 0.0;
         for (double v : lp) sum += v;
         *loss = sum / nmask;
+        return SBS_OK;
     }
-    return SBS_OK;
+    return tc_status(s);
 }
 
 int check_grid_params(uint32_t nf, const sbs_drainage_params *p) {
@@ -352,7 +373,9 @@ int sbs_surrogate_create(uint64_t seed, sbs_surrogate **out) {
     s->pk.w4 = (float *)(s->pk.wb3 + 32 * 288);
     s->pk.b = s->pk.w4 + 288;
     s->partial = (float *)(pm + (pkb + 255) / 256 * 256);
-    if (cudaMalloc(&s->err2, 16) != cudaSuccess) return fail(set_error(SBS_E_NOMEM, "surrogate allocation failed"));
+    if (cudaMalloc(&s->err2, 16) != cudaSuccess || cudaMemset(s->err2, 0, 16) != cudaSuccess)
+        return fail(set_error(SBS_E_NOMEM, "surrogate allocation failed"));
+    s->pk.err = s->err2 + 2;  // words 0-1: masked_error's result
     // He-normal weights (fan-in 9 * ci), zero biases; the output layer starts small.
     std::vector<float> th(SBS_NN_PARAMS, 0.f);
     uint64_t st = seed;
@@ -491,8 +514,7 @@ int sbs_surrogate_forward(sbs_surrogate *s, uint32_t nf, const float *h, const f
     if ((rc = forward_any(s, make_fields(hd, cd, np, cells1, p, nf), (int)nf, *g, mode, nullptr, 0))) return rc;
     SBS_CUDA_TRY(cudaMemcpyAsync(y, s->y4, sizeof(float) * nf * cells1,
                                  mem == SBS_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s->stream));
-    SBS_CUDA_TRY(cudaStreamSynchronize(s->stream));
-    return SBS_OK;
+    return tc_status(s);
 }
 
 int sbs_surrogate_loss_grad(sbs_surrogate *s, uint32_t nf, const float *h, const float *c,
@@ -725,7 +747,7 @@ int sbs_surrogate_evaluate(sbs_surrogate *s, uint32_t first, uint32_t count, int
     out->loss_identity = sl0 / (double)n;
     out->rel_linf = r;
     out->rel_linf_identity = r0;
-    return SBS_OK;
+    return tc_status(s);
 }
 
 int sbs_surrogate_masked_error(const float *a, const float *b, uint32_t nt, uint32_t np, int mem, double *out) {
@@ -818,7 +840,7 @@ int sbs_surrogate_advance(sbs_surrogate *s, sbs_drainage *d, int mode) {
     int rc = advance_into(s, d, mode, nullptr);
     if (rc) return rc;
     SBS_CUDA_TRY(cudaStreamSynchronize(d->stream));
-    return SBS_OK;
+    return tc_status(s);
 }
 
 int sbs_surrogate_rollout(sbs_surrogate *s, sbs_drainage *d, uint32_t passes, uint32_t check_every, double tol,
@@ -876,7 +898,7 @@ int sbs_surrogate_rollout(sbs_surrogate *s, sbs_drainage *d, uint32_t passes, ui
         st.rollouts++;
     }
     SBS_CUDA_TRY(cudaStreamSynchronize(d->stream));
-    SBS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if ((rc = tc_status(s))) return rc;
     if (stats) *stats = st;
     return SBS_OK;
 }

@@ -142,3 +142,25 @@ def test_blocked_drainage_pole_ring_barrier_times_out_then_recovers(sbs, short_w
         load(s)
         s.step_n(0.001, 16)
     np.testing.assert_array_equal(field(sim), field(fresh))
+
+
+def test_training_convolution_waits_time_out_then_recover(sbs, short_waits):
+    """The tensor-core training convolutions: with their commits withheld the training step reports
+    the timeout; afterwards the same handle trains and its loss falls."""
+    from soap_bubble_simulation_gb300 import synthetic as S
+
+    N = short_waits
+    nt, np_ = 32, 64
+    s = sbs.DrainageSurrogate(seed=3)
+    g = np.random.default_rng(0)
+    for k in range(4):
+        p = sbs.field_params(nt, np_, viscosity=float(10 ** g.uniform(-4, -2)), bubble_radius=0.02)
+        s.add_trajectory(S.smooth_modes(nt, np_, seed=10 + k), S.surfactant_noise(nt, np_, seed=20 + k), p, pairs=2)
+    N.call("sbs_set_stall_injection", N.STALL_TENSOR_COMMITS)
+    with pytest.raises(sbs.SbsError) as e:
+        s.train(4, 3, batch=2, lr=3e-3, seed=1)
+    assert e.value.code == N.SBS_E_TIMEOUT
+    N.call("sbs_set_stall_injection", 0)
+    losses = s.train(4, 60, batch=2, lr=3e-3, seed=1)
+    assert np.isfinite(losses).all() and losses[-10:].mean() < losses[:3].mean()
+    s.close()
