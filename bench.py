@@ -323,6 +323,9 @@ def surrogate_section(sbs, synthetic, h0, c0, torch, activations=("gelu", "hswis
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     tf_peak = float(peaks.get("bf16_tflops", 1900.0))
     flop_cell = 2 * 9 * (16 * 32 + 32 * 32 * 2 + 32 * 1)  # useful multiply-adds x 2 per cell and interval
+    # a training iteration per cell: the forward pass, every layer's weight gradient (as many
+    # multiply-adds as the forward pass) and the input gradients of layers 2-4
+    train_flop_cell = 2 * flop_cell + 2 * 9 * (32 * 32 * 2 + 32 * 1)
     plain_rate = cells * STEPS_PER_RUN / plain_s
     iters = 3000
     results = {}
@@ -368,6 +371,9 @@ def surrogate_section(sbs, synthetic, h0, c0, torch, activations=("gelu", "hswis
                        "frac": tflops / tf_peak, "flop_per_cell": flop_cell, "peak_kind": "measured bf16 burst"},
             "train": {"trajectories": ntrain, "kinds": list(synthetic.SURROGATE_KINDS), "grid": "256 x 512",
                       "pairs_per_trajectory": 4, "iters": iters,
+                      "ms_per_iter": (t2 - t1) * 1e3 / iters,
+                      "tflops": train_flop_cell * 8 * 256 * 512 * iters / (t2 - t1) / 1e12,
+                      "flop_per_cell_iter": train_flop_cell,
                       "batch": 8, "data_s": data_s, "train_s": t2 - t1, "loss_first": float(losses[:10].mean()),
                       "loss_last": float(losses[-50:].mean())},
             "heldout_256": {**ev, "trajectories": nheld, "kinds": ["c1", "mirror"]},
@@ -833,6 +839,7 @@ def summary(line: dict) -> dict:
         if su:
             ho = su.get("heldout_256") or {}
             out[key] = {"x_plain": _r(su["speedup_vs_plain"]), "err": _r(su["masked_rel_linf_vs_plain"], 2),
+                        "train_tflops": _r((su.get("train") or {}).get("tflops")),
                         "id_err": _r(su["identity_rel_linf_vs_plain"], 2), "tc_frac": _r(su["tensor"]["frac"]),
                         "held": _r(ho.get("rel_linf"), 2), "held_id": _r(ho.get("rel_linf_identity"), 2),
                         "fail": (su.get("stats") or {}).get("failed_checks")}

@@ -217,7 +217,9 @@ __global__ void out_kernel(OutArgs a) {
     if (c < cells) {
         const int j = (int)(c % np), i = (int)((c / np) % nt);
         const size_t fb = (c / ((size_t)np * nt)) * nt * np;
-        float y = *a.b4;
+        // four independent partial sums (one per 8-channel chunk) instead of one serial chain of 288
+        float yk[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
         for (int t = 0; t < 9; ++t) {
             const int dy = t / 3 - 1, dx = t % 3 - 1;
             const int r = refl_row(i + dy, nt);
@@ -232,11 +234,12 @@ __global__ void out_kernel(OutArgs a) {
                 for (int e = 0; e < 4; ++e) {
                     const __nv_bfloat162 h2 = *reinterpret_cast<const __nv_bfloat162 *>(&w[e]);
                     const float2 f = __bfloat1622float2(h2);
-                    y = __fmaf_rn(sw[t * 32 + k * 8 + 2 * e], f.x, y);
-                    y = __fmaf_rn(sw[t * 32 + k * 8 + 2 * e + 1], f.y, y);
+                    yk[k] = __fmaf_rn(sw[t * 32 + k * 8 + 2 * e], f.x, yk[k]);
+                    yk[k] = __fmaf_rn(sw[t * 32 + k * 8 + 2 * e + 1], f.y, yk[k]);
                 }
             }
         }
+        const float y = __fadd_rn(*a.b4, __fadd_rn(__fadd_rn(yk[0], yk[1]), __fadd_rn(yk[2], yk[3])));
         a.y4[c] = y;
         if (a.target) {
             const float m = a.g.rows[i].w;
@@ -261,10 +264,11 @@ __global__ void out_kernel(OutArgs a) {
     }
 }
 
-// dW4[tap][ic] = sum g4[cell] a3[src(cell,tap)][ic], db4 = sum g4. Block b takes the rows
-// b, b + nblocks, ... of the batch; its 8 warps split each row into 32-column chunks, lane = ic,
-// nine accumulators per lane (one per tap); g4 of a chunk is loaded once and broadcast by shuffle.
-// One partial row [289] per block, warps summed in a fixed order.
+// dW4[tap][ic] = sum g4[cell] a3[src(cell,tap)][ic], db4 = sum g4. Work item: one output row x one
+// 128-cell segment; block b takes items b, b + nblocks, ... Per item the block stages the three
+// source rows of a3 (130 cells each, phi wrapped, theta reflected) and the row's g4 in shared
+// memory; warp w sums the item's cells w, w + 8, ... with lane = ic and nine accumulators per lane
+// (one per tap). One partial row [289] per block, warps summed in a fixed order.
 struct Wgrad4Args {
     const float *g4;
     const bf16 *a3;
@@ -274,50 +278,49 @@ struct Wgrad4Args {
 };
 
 constexpr int kW4Warps = 8;
+constexpr int kW4Cells = 128;
 
 __global__ void __launch_bounds__(32 * kW4Warps) wgrad4_kernel(Wgrad4Args a) {
+    __shared__ __align__(16) bf16 sa[3][kW4Cells + 2][32];
+    __shared__ float sg[kW4Cells];
     __shared__ float sp[kW4Warps][289];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nt = a.g.nt, np = a.g.np;
+    const int segs = (np + kW4Cells - 1) / kW4Cells, items = a.rows * segs;
     float acc[9];
 #pragma unroll
     for (int t = 0; t < 9; ++t) acc[t] = 0.f;
     float gsum = 0.f;
-    for (int row = blockIdx.x; row < a.rows; row += gridDim.x) {
+    for (int item = blockIdx.x; item < items; item += gridDim.x) {
+        const int row = item / segs, j0 = (item % segs) * kW4Cells;
         const int i = row % nt;
         const size_t fb = (size_t)(row / nt) * nt * np;
-        const bf16 *s0 = a.a3 + (fb + (size_t)refl_row(i - 1, nt) * np) * 32 + lane;  // taps dy = -1
-        const bf16 *s1 = a.a3 + (fb + (size_t)i * np) * 32 + lane;                       // dy = 0
-        const bf16 *s2 = a.a3 + (fb + (size_t)refl_row(i + 1, nt) * np) * 32 + lane;  // dy = +1
-        for (int j0 = 32 * warp; j0 < np; j0 += 32 * kW4Warps) {
-            const float gl = j0 + lane < np ? a.g4[fb + (size_t)i * np + j0 + lane] : 0.f;
-            gsum = __fadd_rn(gsum, gl);
-            const int n = min(32, np - j0);
-            for (int jj = 0; jj < n; ++jj) {
-                const float gv = __shfl_sync(0xffffffffu, gl, jj);
-                if (gv == 0.f) continue;  // masked rows
-                const int j = j0 + jj;
-                const int ql = j == 0 ? np - 1 : j - 1, qr = j + 1 == np ? 0 : j + 1;
-                const size_t ol = (size_t)ql * 32, oc = (size_t)j * 32, orr = (size_t)qr * 32;
-                acc[0] = __fmaf_rn(gv, __bfloat162float(s0[ol]), acc[0]);
-                acc[1] = __fmaf_rn(gv, __bfloat162float(s0[oc]), acc[1]);
-                acc[2] = __fmaf_rn(gv, __bfloat162float(s0[orr]), acc[2]);
-                acc[3] = __fmaf_rn(gv, __bfloat162float(s1[ol]), acc[3]);
-                acc[4] = __fmaf_rn(gv, __bfloat162float(s1[oc]), acc[4]);
-                acc[5] = __fmaf_rn(gv, __bfloat162float(s1[orr]), acc[5]);
-                acc[6] = __fmaf_rn(gv, __bfloat162float(s2[ol]), acc[6]);
-                acc[7] = __fmaf_rn(gv, __bfloat162float(s2[oc]), acc[7]);
-                acc[8] = __fmaf_rn(gv, __bfloat162float(s2[orr]), acc[8]);
-            }
+        const int n = min(kW4Cells, np - j0);
+        __syncthreads();  // the previous item's tiles are read
+        for (int e = tid; e < 3 * (kW4Cells + 2) * 4; e += blockDim.x) {
+            const int d = e / ((kW4Cells + 2) * 4), q = (e / 4) % (kW4Cells + 2), ch = e % 4;
+            int col = (j0 - 1 + q) % np;
+            col = col < 0 ? col + np : col;
+            const size_t src = (fb + (size_t)refl_row(i + d - 1, nt) * np + col) * 32 + ch * 8;
+            *reinterpret_cast<uint4 *>(&sa[d][q][ch * 8]) = *reinterpret_cast<const uint4 *>(a.a3 + src);
+        }
+        for (int e = tid; e < kW4Cells; e += blockDim.x) sg[e] = e < n ? a.g4[fb + (size_t)i * np + j0 + e] : 0.f;
+        __syncthreads();
+        for (int m = warp; m < n; m += kW4Warps) {
+            const float gv = sg[m];
+            if (lane == 0) gsum = __fadd_rn(gsum, gv);
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+#pragma unroll
+                for (int x = 0; x < 3; ++x)
+                    acc[3 * d + x] = __fmaf_rn(gv, __bfloat162float(sa[d][m + x][lane]), acc[3 * d + x]);
         }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) gsum = __fadd_rn(gsum, __shfl_xor_sync(0xffffffffu, gsum, o));
 #pragma unroll
     for (int t = 0; t < 9; ++t) sp[warp][t * 32 + lane] = acc[t];
     if (lane == 0) sp[warp][288] = gsum;
     __syncthreads();
-    for (int k = threadIdx.x; k < 289; k += blockDim.x) {
+    for (int k = tid; k < 289; k += blockDim.x) {
         float v = 0.f;
         for (int w = 0; w < kW4Warps; ++w) v = __fadd_rn(v, sp[w][k]);
         a.partial[(size_t)blockIdx.x * 289 + k] = v;

@@ -6,7 +6,8 @@ Cases: `wgsl` (GPUDrainageSimulator semantics, h + surfactant), `cpu` (DrainageS
 semantics, compensated f32x2), `cpu32` (plain f32), `spectral-tc` / `spectral-fp32` (81-wavelength
 spectral colour of --points seeded points, tensor-core or FP32 contraction), `surrogate-fused` /
 `surrogate-layered` (--steps 64-pass surrogate intervals of the field, untrained seeded weights:
-the same kernels and shapes as a trained network; --activation gelu or hswish), `foam` (the 4096-bubble foam batch, --steps
+the same kernels and shapes as a trained network; --activation gelu or hswish), `train` (--steps
+surrogate training iterations, batch 8 x 256 x 512, on 24 seeded trajectories), `foam` (the 4096-bubble foam batch, --steps
 steps with the default tiles), `shade` (--steps 3840 x 2160 headless frames of the bubble
 fragment shader), `caustics` (--steps caustic maps of the field after 100 WGSL passes),
 `foam-dynamics` (FoamSimulator::step on an FCC foam of --bubbles bubbles: 3 steps, then --steps
@@ -30,6 +31,7 @@ def main(argv=None) -> None:
     p = argparse.ArgumentParser()
     p.add_argument("--case", default="wgsl",
                    choices=["wgsl", "cpu", "cpu32", "spectral-tc", "spectral-fp32", "surrogate-fused", "surrogate-layered",
+                            "train",
                             "foam", "shade", "caustics", "foam-dynamics", "branched"])
     p.add_argument("--points", type=int, default=1 << 20, help="spectral cases: number of points")
     p.add_argument("--res", type=int, default=2048)
@@ -94,6 +96,16 @@ def main(argv=None) -> None:
         print(f"ran {a.steps} foam steps of {len(res)} bubbles")
         return
     h, c = synthetic.bubble_c1(a.res)
+    if a.case == "train":
+        from .surrogate import DrainageSurrogate, field_params
+
+        s = DrainageSurrogate(seed=7, activation=a.activation)
+        for hh, cc, visc, rad in synthetic.surrogate_trajectories(24):
+            s.add_trajectory(hh, cc, field_params(256, 512, viscosity=visc, bubble_radius=rad), pairs=4)
+        s.train(16, a.steps, batch=8, lr=2e-3, seed=5)
+        s.close()
+        print(f"ran {a.steps} training iterations (batch 8 x 256 x 512, {a.activation})")
+        return
     if a.case.startswith("surrogate"):
         from .surrogate import DrainageSurrogate, field_params
 
