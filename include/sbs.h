@@ -636,7 +636,7 @@ int sbs_foam_sim_couple_thickness(sbs_foam_sim *s, sbs_foam *batch);
  * trajectories that the plain solver generates. */
 typedef struct sbs_surrogate sbs_surrogate;
 
-#define SBS_NN_LAYERED 0 /* one kernel per layer (mma.sync tensor cores), activations through HBM */
+#define SBS_NN_LAYERED 0 /* one kernel per layer (tcgen05 convolutions), activations through HBM */
 #define SBS_NN_FUSED 1   /* all four layers in one persistent tcgen05 kernel, activations on chip */
 
 /* New surrogate with He-initialised weights (normal, splitmix64 seed). */

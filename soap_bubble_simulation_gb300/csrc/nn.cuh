@@ -14,7 +14,6 @@ namespace nn {
 
 typedef __nv_bfloat16 bf16;
 
-constexpr int kTileCols = 128;  // output columns per tile of the layered kernels
 constexpr int kMaxFields = 16;  // fields per batched launch
 
 __device__ __forceinline__ float phi_poly(float t, float u, float *p_out) {

@@ -20,6 +20,7 @@
 //
 // Every mbarrier wait is bounded (sbs_set_wait_limit); the block votes on the outcome, so a timeout
 // ends the work of all its threads together, records the error and still releases the TMEM.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -303,6 +304,219 @@ __global__ void __launch_bounds__(kTcThreads) tc_conv_kernel(const TcConvArgs a)
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
 }
 
+// ------------------------------------------------------------------------------------------------
+// Weight gradients of a 3x3 layer: dW[tap][oc][ic] = sum over cells of g[cell][oc] x[src(cell, tap)][ic]
+// (src: theta reflected, phi wrapped) and db[oc] = sum of g[cell][oc], as GEMMs over the cells.
+// A chunk is 64 cells of one output row. With the cells as K, an 8-channel plane with 16 B per cell is
+// an MN-major operand (8 channels x 8 cells per 128-byte core matrix), so the dx taps are start
+// offsets of 16 B. One MMA group per dx: M = 128 rows = (dy, ic) over the 3 x CIN/8 planes of x,
+// a plane of ones (its rows of D are db) and padding, N = 32 output channels (g, staged the same
+// way), K = 16 cells; D[dx] accumulates over all of the CTA's chunks.
+//
+// Roles: one thread of warp 0 stages chunks through a ring of four stages with TMA (one box per
+// plane and source row: 66 cells of x from j0 - 1, 64 cells of g; cells outside the row arrive as
+// zeros, which also zeroes g past a ragged row end); warp 1 writes the two cells of the phi seam
+// (x[np - 1] left of cell 0, x[0] right of cell np - 1) over those zeros once a chunk has landed,
+// and one of its threads issues the chunk's MMAs and commits them to the stage's empty barrier.
+// Every wait is bounded; after a timeout the CTA still waits (bounded) for the copies and MMAs it
+// started before it releases the TMEM. The CTA's sums go to one partial row, reduced over the CTAs
+// in a fixed order afterwards.
+constexpr int kWgCells = 64;                      // cells per chunk
+constexpr int kWgStage = kWgCells + 2;            // staged x cells per plane (one halo cell each side)
+constexpr uint32_t kWgPlaneA = 1152;              // x plane: 66 x 16 B, padded to 128-byte TMA alignment
+constexpr uint32_t kWgPlaneB = kWgCells * 16;     // g plane: 1024 B
+constexpr int kWgStages = 4;
+constexpr int kWgThreads = 128;                   // 4 warps: one per TMEM lane quarter in the epilogue
+
+template <int CIN>
+struct WgLayout {
+    static constexpr int PL = CIN / 8;                // planes per x row
+    static constexpr int ONES = 3 * PL;               // the plane of ones
+    static constexpr uint32_t ABUF = 16 * kWgPlaneA;  // 16 planes = M 128
+    static constexpr uint32_t BBUF = 4 * kWgPlaneB;
+    static constexpr uint32_t OFF_B = kWgStages * ABUF;
+    static constexpr uint32_t OFF_BAR = OFF_B + kWgStages * BBUF;  // full[stages], empty[stages]
+    static constexpr uint32_t OFF_MISC = OFF_BAR + 16 * kWgStages;
+    static constexpr uint32_t SMEM = OFF_MISC + 16 + 128;           // + slack to align the base to 128 B
+    static constexpr uint32_t TX = 3 * PL * kWgStage * 16 + 4 * kWgPlaneB;  // bytes of one chunk's boxes
+};
+
+struct TcWgradArgs {
+    CUtensorMap tx;  // x as [rows][np][CIN/8][8], box 8 x 1 x 66 x 1
+    CUtensorMap tg;  // g as [rows][np][4][8], box 8 x 1 x 64 x 1
+    const bf16 *x;   // [cells][CIN]: the layer's input (the seam cells)
+    float *partial;  // [gridDim.x][32 * 9 * CIN + 32]
+    unsigned *err;
+    long long wait_cycles;
+    int nt, np, cps, nchunks;  // chunks per row, chunks in all
+    int stall;
+};
+
+template <int CIN>
+__global__ void __launch_bounds__(kWgThreads) tc_wgrad_kernel(const __grid_constant__ TcWgradArgs a) {
+    using Lay = WgLayout<CIN>;
+    static_assert(3 * Lay::PL + 1 <= 16, "the dy x channel planes and the ones fit one M = 128 group");
+    extern __shared__ __align__(128) uint8_t smem_raw[];
+    uint8_t *smem = smem_raw + ((128u - (tc::smem_u32(smem_raw) & 127u)) & 127u);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t sb = tc::smem_u32(smem);
+    const uint32_t full0 = sb + Lay::OFF_BAR, empty0 = full0 + 8u * kWgStages;  // stage s: + 8 s
+    volatile uint32_t *s_misc = reinterpret_cast<volatile uint32_t *>(smem + Lay::OFF_MISC);
+    // s_misc: [0] TMEM base, [1] failed, [2] chunks whose copies the MMA warp has seen land
+    const int nt = a.nt, np = a.np;
+    constexpr uint32_t kId = tc::idesc_bf16_m128(32) | (1u << 15) | (1u << 16);  // A and B MN-major
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(
+            tc::smem_u32(const_cast<uint32_t *>(s_misc))));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 32) {
+        for (int s = 0; s < kWgStages; ++s) {
+            tc::mbar_init(full0 + 8u * s, 1);
+            tc::mbar_init(empty0 + 8u * s, 1);
+        }
+        tc::fence_mbar_init();
+        s_misc[1] = 0u;
+        s_misc[2] = 0u;
+    }
+    for (int e = tid; e < kWgStages * (int)(kWgPlaneA / 16); e += kWgThreads) {  // bf16 1.0 pairs
+        const int s = e / (int)(kWgPlaneA / 16), q = e % (int)(kWgPlaneA / 16);
+        *reinterpret_cast<uint4 *>(smem + s * Lay::ABUF + Lay::ONES * kWgPlaneA + q * 16) =
+            make_uint4(0x3F803F80u, 0x3F803F80u, 0x3F803F80u, 0x3F803F80u);
+    }
+    tc::fence_async_smem();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = s_misc[0];
+
+    const int nmine = a.nchunks > (int)blockIdx.x ? (a.nchunks - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    // chunk k of this CTA: first row of its field, row i in the field, first cell j0
+    auto where = [&](int k, int &fr, int &i, int &j0) {
+        const int c = (int)blockIdx.x + k * (int)gridDim.x;
+        const int row = c / a.cps;
+        i = row % nt;
+        fr = row - i;
+        j0 = (c % a.cps) * kWgCells;
+    };
+    auto reflect = [&](int r) { return r < 0 ? 1 : (r >= nt ? nt - 2 : r); };
+
+    int produced = 0;  // producer thread
+    if (warp == 0) {
+        if (lane == 0) {
+            for (int k = 0; k < nmine; ++k) {
+                const int s = k % kWgStages;
+                if (s_misc[1]) break;
+                if (k >= kWgStages && !tc::mbar_wait_n(empty0 + 8u * s, (uint32_t)(k / kWgStages - 1), a.wait_cycles)) {
+                    s_misc[1] = 1u;
+                    break;
+                }
+                int fr, i, j0;
+                where(k, fr, i, j0);
+                const uint32_t bar = full0 + 8u * s;
+                tc::mbar_arrive_expect_tx(bar, Lay::TX);
+                for (int dyi = 0; dyi < 3; ++dyi) {
+                    const int src = fr + reflect(i + dyi - 1);
+                    for (int p = 0; p < Lay::PL; ++p)
+                        tc::tma_load_4d(sb + s * Lay::ABUF + (dyi * Lay::PL + p) * kWgPlaneA, &a.tx, 0, p, j0 - 1, src,
+                                        bar);
+                }
+                for (int p = 0; p < 4; ++p)
+                    tc::tma_load_4d(sb + Lay::OFF_B + s * Lay::BBUF + p * kWgPlaneB, &a.tg, 0, p, j0, fr + i, bar);
+                produced = k + 1;
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        const uint64_t a_desc0 = tc::make_desc(sb, 128, kWgPlaneA);
+        const uint64_t b_desc0 = tc::make_desc(sb + Lay::OFF_B, 128, kWgPlaneB);
+        // seam cells: lane L < 6 PL takes side L / (3 PL) (0: left of cell 0, 1: right of cell np - 1)
+        // and plane P = L % (3 PL) = (dy + 1) PL + p
+        const int side = lane / (3 * Lay::PL), P = lane % (3 * Lay::PL);
+        int issued = 0, seen = 0;
+        for (int k = 0; k < nmine; ++k) {
+            const int s = k % kWgStages;
+            int fr, i, j0;
+            where(k, fr, i, j0);
+            const int n = min(kWgCells, np - j0);
+            bool mine = false;
+            uint4 hv = make_uint4(0u, 0u, 0u, 0u);
+            uint32_t hoff = 0;
+            if (side < 2 && ((side == 0 && j0 == 0) || (side == 1 && j0 + n == np))) {
+                const int src = fr + reflect(i + P / Lay::PL - 1);
+                hv = __ldg(reinterpret_cast<const uint4 *>(a.x + ((size_t)src * np + (side ? 0 : np - 1)) * CIN +
+                                                           (P % Lay::PL) * 8));
+                hoff = s * Lay::ABUF + P * kWgPlaneA + (side ? n + 1 : 0) * 16;
+                mine = true;
+            }
+            const bool ok = tc::mbar_wait_n(full0 + 8u * s, (uint32_t)(k / kWgStages), a.wait_cycles);
+            if (__any_sync(0xffffffffu, !ok || s_misc[1] != 0u)) {  // one decision for the warp
+                if (lane == 0) s_misc[1] = 1u;
+                break;
+            }
+            seen = k + 1;
+            if (mine) *reinterpret_cast<uint4 *>(smem + hoff) = hv;
+            tc::fence_async_smem();
+            __syncwarp();
+            if (lane == 0 && !a.stall) {
+                tc::fence_after();
+                const uint64_t ab = a_desc0 + (uint64_t)((s * Lay::ABUF) >> 4);
+                const uint64_t bd = b_desc0 + (uint64_t)((s * Lay::BBUF) >> 4);
+#pragma unroll
+                for (int kk = 0; kk < kWgCells / 16; ++kk)
+#pragma unroll
+                    for (int dx = 0; dx < 3; ++dx)  // start cell kk * 16 + dx of the staged plane
+                        tc::mma_bf16(tmem + 32u * dx, ab + (uint64_t)(kk * 16 + dx), bd + (uint64_t)(kk * 16), kId,
+                                     !(k == 0 && kk == 0));
+                tc::commit(empty0 + 8u * s);
+            }
+            issued = a.stall ? 0 : k + 1;
+            __syncwarp();
+        }
+        // the last commit covers every MMA of this CTA; wait for it even after a failure (the MMAs
+        // read this CTA's shared memory and write its TMEM)
+        if (lane == 0 && issued > 0 &&
+            !tc::mbar_wait_n(empty0 + 8u * ((issued - 1) % kWgStages), (uint32_t)((issued - 1) / kWgStages),
+                             a.wait_cycles))
+            s_misc[1] = 1u;
+        if (lane == 0) s_misc[2] = (uint32_t)seen;
+        __syncwarp();
+    }
+    __syncthreads();
+    const bool failed = s_misc[1] != 0u;
+    if (failed && warp == 0 && lane == 0)  // copies still in flight land before the CTA leaves
+        for (int k = (int)s_misc[2]; k < produced; ++k)
+            tc::mbar_wait_n(full0 + 8u * (k % kWgStages), (uint32_t)(k / kWgStages), a.wait_cycles);
+    tc::fence_after();
+
+    float *out = a.partial + (size_t)blockIdx.x * (32 * 9 * CIN + 32);
+    const bool have = nmine > 0 && !failed;  // block-uniform
+    const int m = warp * 32 + lane, P = m / 8;
+    for (int dx = 0; dx < 3; ++dx) {
+        uint32_t v[32];
+        if (have) {
+            tc::tld32(tmem + ((uint32_t)(warp * 32) << 16) + 32u * dx, v);
+            tc::wait_ld();
+#pragma unroll
+            for (int c = 0; c < 32; ++c) tc::pin(v[c]);
+        }
+        if (P < 3 * Lay::PL) {
+            const int t = (P / Lay::PL) * 3 + dx, ic = (P % Lay::PL) * 8 + m % 8;
+#pragma unroll
+            for (int oc = 0; oc < 32; ++oc) out[oc * 9 * CIN + t * CIN + ic] = have ? __uint_as_float(v[oc]) : 0.f;
+        } else if (dx == 1 && m == 8 * Lay::ONES) {
+#pragma unroll
+            for (int oc = 0; oc < 32; ++oc) out[32 * 9 * CIN + oc] = have ? __uint_as_float(v[oc]) : 0.f;
+        }
+    }
+    if (failed && tid == 0) atomicOr(a.err, 4u);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+}
+
 template <int CIN, bool BWD>
 cudaError_t launch_tc(TcConvArgs a, int nf, cudaStream_t st) {
     using Lay = TcLayout<CIN, BWD>;
@@ -326,7 +540,71 @@ cudaError_t launch_tc(TcConvArgs a, int nf, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// cuTensorMapEncodeTiled from the driver (the library links only the runtime)
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+    static const EncodeTiledFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return (EncodeTiledFn) nullptr;
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+// a [rows][np][ch/8][8] BF16 tensor (cells of ch channels) in boxes of one 8-channel plane x `cells`
+cudaError_t plane_map(CUtensorMap *map, const bf16 *base, int ch, int np, int rows, int cells) {
+    const EncodeTiledFn enc = encode_tiled();
+    if (!enc) return cudaErrorNotSupported;
+    const cuuint64_t dim[4] = {8, (cuuint64_t)(ch / 8), (cuuint64_t)np, (cuuint64_t)rows};
+    const cuuint64_t stride[3] = {16, (cuuint64_t)ch * 2, (cuuint64_t)np * ch * 2};
+    const cuuint32_t box[4] = {8, 1, (cuuint32_t)cells, 1};
+    const cuuint32_t one[4] = {1, 1, 1, 1};
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(base), dim, stride, box, one,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+template <int CIN>
+cudaError_t launch_wgrad(const TcWgradArgs &w, int nblocks, cudaStream_t st) {
+    static bool configured = false;  // per template instance and process
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(tc_wgrad_kernel<CIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)WgLayout<CIN>::SMEM);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    tc_wgrad_kernel<CIN><<<nblocks, kWgThreads, WgLayout<CIN>::SMEM, st>>>(w);
+    return cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t wgrad_tc(int cin, const bf16 *g, const bf16 *x, float *partial, int nblocks, unsigned *err, int nf, int nt,
+                     int np, cudaStream_t st) {
+    TcWgradArgs w{};
+    const int rows = nf * nt;
+    cudaError_t e = plane_map(&w.tx, x, cin, np, rows, kWgStage);
+    if (e == cudaSuccess) e = plane_map(&w.tg, g, 32, np, rows, kWgCells);
+    if (e != cudaSuccess) return e;
+    w.x = x;
+    w.partial = partial;
+    w.err = err;
+    w.nt = nt;
+    w.np = np;
+    w.cps = (np + kWgCells - 1) / kWgCells;
+    w.nchunks = rows * w.cps;
+    const WaitConfig wc = wait_config();
+    w.wait_cycles = wc.cycles;
+    w.stall = (wc.stall & SBS_STALL_TENSOR_COMMITS) ? 1 : 0;
+    return cin == 16 ? launch_wgrad<16>(w, nblocks, st) : launch_wgrad<32>(w, nblocks, st);
+}
 
 cudaError_t conv_forward(int layer, const bf16 *in, const Packed &p, float *y, bf16 *a, int nf, int nt, int np,
                          cudaStream_t st) {

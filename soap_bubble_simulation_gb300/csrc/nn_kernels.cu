@@ -1,16 +1,12 @@
 // Training-side kernels of the drainage surrogate (include/sbs_nn.h) and its layered forward
-// pass: features, the weight gradients of the 3x3 convolutions (implicit GEMMs on warp-level
-// mma.sync BF16 x BF16 -> FP32), the one-channel output layer and its gradients on the FP32 pipe,
-// loss, deterministic gradient reduction, Adam, and weight packing. The convolutions themselves
-// (forward and transposed) run on tcgen05 (nn_conv_tc.cu).
+// pass: features, the one-channel output layer and its gradients on the FP32 pipe, loss,
+// deterministic gradient reduction, Adam, and weight packing. The 3x3 convolutions, their input
+// gradients and their weight gradients run on tcgen05 (nn_conv_tc.cu).
 //
 // Layouts (channel-last, cells = fields x nt x np):
 //   features x        BF16 [cells][16]
 //   pre-activations y FP32 [cells][32]       activations a BF16 [cells][32]
 //   output y4 / gradient g4 FP32 [cells]     layer gradients g BF16 [cells][32]
-// A weight-gradient tile is one row segment of kTileCols = 128 cells of one field: the block
-// stages the three input rows it reads (reflected in theta, periodic in phi) in shared memory and
-// gathers MMA fragments with ldmatrix from the shifted rows (no im2col buffer).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -26,39 +22,7 @@ namespace sbs {
 namespace nn {
 namespace {
 
-__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void ldsm_x4_t(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0, %1, %2, %3}, [%4];"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-                 : "r"(addr));
-}
-
-__device__ __forceinline__ void mma16816(float *d, const uint32_t *a, uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
-        "{%0, %1, %2, %3};"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
 __device__ __forceinline__ int refl_row(int i, int nt) { return i < 0 ? 1 : (i >= nt ? nt - 2 : i); }
-
-// Byte offset of 16-byte channel chunk `ch` of staged cell `q` in a row buffer of cells with CIN
-// channels. 16- and 32-channel cells (32 / 64 B) are XOR-swizzled so that the 8 rows of an
-// ldmatrix phase fall into distinct bank groups.
-template <int CIN>
-__device__ __forceinline__ uint32_t cell_off(int q, int ch) {
-    if constexpr (CIN == 8) {
-        return (uint32_t)q * 16u;
-    } else if constexpr (CIN == 16) {
-        return (uint32_t)q * 32u + ((uint32_t)(ch ^ ((q >> 2) & 1)) << 4);
-    } else {
-        return (uint32_t)q * 64u + ((uint32_t)(ch ^ ((q >> 1) & 3)) << 4);
-    }
-}
-
-constexpr int kRowCells = kTileCols + 2;  // staged columns j0-1 .. j0+128
 
 // ----------------------------------------------------------------------------------- features
 __global__ void features_kernel(Fields fs, GridTab g, uint4 *x) {
@@ -76,117 +40,6 @@ __global__ void features_kernel(Fields fs, GridTab g, uint4 *x) {
     uint4 *o = x + (((size_t)b * nt + i) * np + j) * 2;
     o[0] = p0;
     o[1] = p1;
-}
-
-// ------------------------------------------------------- weight gradient of a 3x3 convolution
-// D[oc][tap*CIN + ic] = sum_cells g[cell][oc] * x[src(cell, tap)][ic], db[oc] = sum_cells g.
-// Each block accumulates its strided share of tiles in registers and writes one partial row.
-struct WgradArgs {
-    const bf16 *g;
-    const bf16 *x;
-    float *partial;  // [gridDim.x][32 * 9 * CIN + 32]
-    int nt, np, tiles_x, ntiles;
-};
-
-template <int CIN>
-__global__ void __launch_bounds__(128) wgrad_kernel(WgradArgs a) {
-    constexpr int CPC = CIN / 8;
-    constexpr int CB = CIN * 2;
-    constexpr int ROWB = kRowCells * CB;
-    constexpr int NT = 9 * CIN / 8;         // n8 tiles
-    constexpr int NTW = (NT + 3) / 4;       // per warp
-    extern __shared__ __align__(16) uint8_t smem[];
-    uint8_t *sX = smem;             // 3 rows
-    uint8_t *sG = smem + 3 * ROWB;  // 128 cells
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int nt = a.nt, np = a.np;
-    const int q8 = lane >> 3, r8 = lane & 7;
-    const uint32_t sX_u = smem_addr(sX), sG_u = smem_addr(sG);
-    const int nbeg = warp * NTW, nend = min(NT, nbeg + NTW);
-
-    float acc[2][NTW][4];
-#pragma unroll
-    for (int m = 0; m < 2; ++m)
-#pragma unroll
-        for (int n = 0; n < NTW; ++n)
-#pragma unroll
-            for (int r = 0; r < 4; ++r) acc[m][n][r] = 0.f;
-    float dbias = 0.f;
-
-    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
-        const int tx = tile % a.tiles_x, row_id = tile / a.tiles_x;
-        const int i = row_id % nt, b = row_id / nt, j0 = tx * kTileCols;
-        const int src[3] = {refl_row(i - 1, nt), i, refl_row(i + 1, nt)};
-        const bf16 *xb = a.x + (size_t)b * nt * np * CIN;
-        __syncthreads();  // previous tile's reads done
-        for (int e = tid; e < 3 * kRowCells * CPC; e += 128) {
-            const int rb = e / (kRowCells * CPC), r = e % (kRowCells * CPC);
-            const int q = r / CPC, ch = r % CPC;
-            int col = (j0 - 1 + q) % np;
-            col = col < 0 ? col + np : col;
-            *(uint4 *)(sX + rb * ROWB + cell_off<CIN>(q, ch)) =
-                *(const uint4 *)(xb + ((size_t)src[rb] * np + col) * CIN + ch * 8);
-        }
-        const bf16 *gb = a.g + ((size_t)b * nt + i) * np * 32;
-        for (int e = tid; e < kTileCols * 4; e += 128) {
-            const int m = e >> 2, ch = e & 3;
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (j0 + m < np) v = *(const uint4 *)(gb + (size_t)(j0 + m) * 32 + ch * 8);
-            *(uint4 *)(sG + cell_off<32>(m, ch)) = v;
-        }
-        __syncthreads();
-        if (tid < 32) {
-            float s = 0.f;
-            for (int m = 0; m < kTileCols; ++m) {
-                const bf16 *p = (const bf16 *)(sG + cell_off<32>(m, tid >> 3)) + (tid & 7);
-                s += __bfloat162float(*p);
-            }
-            dbias += s;
-        }
-        if (nbeg < nend) {
-#pragma unroll 1
-            for (int s = 0; s < kTileCols / 16; ++s) {
-                uint32_t af[2][4];
-#pragma unroll
-                for (int mt = 0; mt < 2; ++mt) {
-                    const int ch = 2 * mt + (q8 & 1);
-                    const int m = 16 * s + 8 * (q8 >> 1) + r8;
-                    ldsm_x4_t(sG_u + cell_off<32>(m, ch), af[mt][0], af[mt][1], af[mt][2], af[mt][3]);
-                }
-#pragma unroll
-                for (int jn = 0; jn < NTW; jn += 2) {
-                    // n-tiles nbeg + jn and nbeg + jn + 1 (the second clamped to the first when absent)
-                    int nb = nbeg + jn + (q8 >> 1);
-                    if (nb >= nend) nb = nbeg + jn;
-                    const int t = (nb * 8) / CIN, ch = ((nb * 8) % CIN) / 8;
-                    const int dy = t / 3 - 1, dx = t % 3 - 1;
-                    const int m = 16 * s + 8 * (q8 & 1) + r8;
-                    uint32_t b0, b1, b2, b3;
-                    ldsm_x4_t(sX_u + (dy + 1) * ROWB + cell_off<CIN>(m + dx + 1, ch), b0, b1, b2, b3);
-#pragma unroll
-                    for (int mt = 0; mt < 2; ++mt) {
-                        if (nbeg + jn < nend) mma16816(acc[mt][jn], af[mt], b0, b1);
-                        if (jn + 1 < NTW && nbeg + jn + 1 < nend) mma16816(acc[mt][jn + 1], af[mt], b2, b3);
-                    }
-                }
-            }
-        }
-    }
-    float *out = a.partial + (size_t)blockIdx.x * (32 * 9 * CIN + 32);
-    const int g = lane >> 2, q4 = lane & 3;
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-        for (int jn = 0; jn < NTW; ++jn) {
-            if (nbeg + jn >= nend) continue;
-            const int n = (nbeg + jn) * 8 + 2 * q4;
-#pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                const int oc = 16 * mt + g + 8 * (r >> 1);
-                out[oc * 9 * CIN + n + (r & 1)] = acc[mt][jn][r];
-            }
-        }
-    if (tid < 32) out[32 * 9 * CIN + tid] = dbias;
 }
 
 // ------------------------------------------------------------ output layer (one channel, FP32)
@@ -383,15 +236,33 @@ __global__ void __launch_bounds__(256) dgrad4_kernel(Dgrad4Args a) {
     }
 }
 
-// sum of partial rows (fixed order) scattered into the canonical parameter layout
-// W[tap][oc][ic] (partial column oc * 9 * CIN + tap * CIN + ic) and b[oc].
-__global__ void reduce_partials_kernel(const float *partial, int nblocks, int ci, int co, float *grad_w,
-                                       float *grad_b) {
-    const int ncol = co * 9 * ci + co;
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= ncol) return;
+// Column sums over the blocks' partial rows, in a fixed order: a block of 256 threads takes 32
+// adjacent columns; thread (r, c) sums rows r, r + 8, ... of column c (coalesced 128-byte rows), then
+// the eight partial sums are added in order r = 0..7. Returns the sum in the threads with r = 0.
+constexpr int kRedCols = 32, kRedRows = 8;
+__device__ __forceinline__ float column_sum(const float *partial, int nblocks, int ncol, int col) {
+    __shared__ float s_part[kRedRows][kRedCols];
+    const int c = threadIdx.x % kRedCols, r = threadIdx.x / kRedCols;
     float s = 0.f;
-    for (int k = 0; k < nblocks; ++k) s = __fadd_rn(s, partial[(size_t)k * ncol + e]);
+    if (col < ncol)
+        for (int k = r; k < nblocks; k += kRedRows) s = __fadd_rn(s, partial[(size_t)k * ncol + col]);
+    s_part[r][c] = s;
+    __syncthreads();
+    float t = 0.f;
+    if (r == 0)
+        for (int q = 0; q < kRedRows; ++q) t = __fadd_rn(t, s_part[q][c]);
+    return t;
+}
+
+// sum of partial rows scattered into the canonical parameter layout W[tap][oc][ic] (partial column
+// oc * 9 * CIN + tap * CIN + ic) and b[oc].
+__global__ void __launch_bounds__(kRedCols *kRedRows) reduce_partials_kernel(const float *partial, int nblocks,
+                                                                               int ci, int co, float *grad_w,
+                                                                               float *grad_b) {
+    const int ncol = co * 9 * ci + co;
+    const int e = blockIdx.x * kRedCols + threadIdx.x % kRedCols;
+    const float s = column_sum(partial, nblocks, ncol, e);
+    if (threadIdx.x >= kRedCols || e >= ncol) return;
     if (e < co * 9 * ci) {
         const int oc = e / (9 * ci), r = e % (9 * ci), t = r / ci, ic = r % ci;
         grad_w[((size_t)t * co + oc) * ci + ic] = s;
@@ -401,11 +272,11 @@ __global__ void reduce_partials_kernel(const float *partial, int nblocks, int ci
 }
 
 // layer-4 partial rows are [block][tap*32 + ic] then db4
-__global__ void reduce4_kernel(const float *partial, int nblocks, float *grad_w4, float *grad_b4) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= 289) return;
-    float s = 0.f;
-    for (int k = 0; k < nblocks; ++k) s = __fadd_rn(s, partial[(size_t)k * 289 + e]);
+__global__ void __launch_bounds__(kRedCols *kRedRows) reduce4_kernel(const float *partial, int nblocks,
+                                                                       float *grad_w4, float *grad_b4) {
+    const int e = blockIdx.x * kRedCols + threadIdx.x % kRedCols;
+    const float s = column_sum(partial, nblocks, 289, e);
+    if (threadIdx.x >= kRedCols || e >= 289) return;
     if (e < 288)
         grad_w4[e] = s;
     else
@@ -500,11 +371,6 @@ __global__ void masked_err_kernel(const float *a, size_t pa, const float *b, siz
     }
 }
 
-template <int CIN>
-size_t wgrad_smem() {
-    return (size_t)3 * kRowCells * CIN * 2 + (size_t)kTileCols * 64;
-}
-
 
 }  // namespace
 
@@ -517,33 +383,15 @@ cudaError_t features(const Fields &fs, int nf, const GridTab &g, bf16 *x, cudaSt
 
 
 cudaError_t conv_backward_weight(int layer, const bf16 *g, const bf16 *x, float *partial, int nblocks, float *grad,
-                                 int nf, int nt, int np, cudaStream_t st) {
-    WgradArgs w{};
-    w.g = g;
-    w.x = x;
-    w.partial = partial;
-    w.nt = nt;
-    w.np = np;
-    w.tiles_x = (np + kTileCols - 1) / kTileCols;
-    w.ntiles = w.tiles_x * nt * nf;
+                                 unsigned *err, int nf, int nt, int np, cudaStream_t st) {
     const int ci = layer == 1 ? 16 : 32;
     const int ow = layer == 1 ? SBS_NN_W1 : (layer == 2 ? SBS_NN_W2 : SBS_NN_W3);
     const int ob = layer == 1 ? SBS_NN_B1 : (layer == 2 ? SBS_NN_B2 : SBS_NN_B3);
-    cudaError_t e;
-    if (ci == 16) {
-        const size_t sm = wgrad_smem<16>();
-        e = cudaFuncSetAttribute(wgrad_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (e != cudaSuccess) return e;
-        wgrad_kernel<16><<<nblocks, 128, sm, st>>>(w);
-    } else {
-        const size_t sm = wgrad_smem<32>();
-        e = cudaFuncSetAttribute(wgrad_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (e != cudaSuccess) return e;
-        wgrad_kernel<32><<<nblocks, 128, sm, st>>>(w);
-    }
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    cudaError_t e = wgrad_tc(ci, g, x, partial, nblocks, err, nf, nt, np, st);
+    if (e != cudaSuccess) return e;
     const int ncol = 32 * 9 * ci + 32;
-    reduce_partials_kernel<<<(ncol + 255) / 256, 256, 0, st>>>(partial, nblocks, ci, 32, grad + ow, grad + ob);
+    reduce_partials_kernel<<<(ncol + kRedCols - 1) / kRedCols, kRedCols * kRedRows, 0, st>>>(partial, nblocks, ci, 32,
+                                                                                         grad + ow, grad + ob);
     return cudaGetLastError();
 }
 
@@ -580,7 +428,8 @@ cudaError_t output_backward(const float *g4, const bf16 *a3, const float *y3, co
     wgrad4_kernel<<<nblocks, 32 * kW4Warps, 0, st>>>(w);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    reduce4_kernel<<<2, 256, 0, st>>>(partial, nblocks, grad + SBS_NN_W4, grad + SBS_NN_B4);
+    reduce4_kernel<<<(289 + kRedCols - 1) / kRedCols, kRedCols * kRedRows, 0, st>>>(partial, nblocks, grad + SBS_NN_W4,
+                                                                                 grad + SBS_NN_B4);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     Dgrad4Args d{};
     d.g4 = g4;

@@ -27,7 +27,11 @@ cudaError_t conv_forward(int layer, const bf16 *in, const Packed &p, float *y, b
 cudaError_t conv_backward_data(int layer, const bf16 *g, const Packed &p, const float *yprev, bf16 *gprev, int nf,
                                int nt, int np, cudaStream_t st);
 cudaError_t conv_backward_weight(int layer, const bf16 *g, const bf16 *x, float *partial, int nblocks, float *grad,
-                                 int nf, int nt, int np, cudaStream_t st);
+                                 unsigned *err, int nf, int nt, int np, cudaStream_t st);
+// tcgen05 weight gradients of a 3x3 layer with cin input channels: one partial row per block
+// (nblocks of them, [32 * 9 * cin + 32] each) for the fixed-order reduction (nn_conv_tc.cu)
+cudaError_t wgrad_tc(int cin, const bf16 *g, const bf16 *x, float *partial, int nblocks, unsigned *err, int nf, int nt,
+                     int np, cudaStream_t st);
 // target == null: forward only (y4). Otherwise also g4 and per-block loss partials; *nblocks_out
 // receives the number of loss partials.
 cudaError_t output_layer(const bf16 *a3, const Packed &p, float *y4, const float *target, float *g4,

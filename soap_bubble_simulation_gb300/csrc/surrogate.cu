@@ -260,11 +260,14 @@ int loss_and_grad(sbs_surrogate *s, const Fields &fs, int nf, const GridDev &g, 
                               s->stream, &nlb));
     SBS_CUDA_TRY(output_backward(s->g4, s->a3, s->y3, s->pk, s->g3, s->partial, s->nblocks, s->grad, g.tab(), nf,
                                  s->stream));
-    SBS_CUDA_TRY(conv_backward_weight(3, s->g3, s->a2, s->partial, s->nblocks, s->grad, nf, nt, np, s->stream));
+    SBS_CUDA_TRY(conv_backward_weight(3, s->g3, s->a2, s->partial, s->nblocks, s->grad, s->pk.err, nf, nt, np,
+                                      s->stream));
     SBS_CUDA_TRY(conv_backward_data(3, s->g3, s->pk, s->y2, s->g2, nf, nt, np, s->stream));
-    SBS_CUDA_TRY(conv_backward_weight(2, s->g2, s->a1, s->partial, s->nblocks, s->grad, nf, nt, np, s->stream));
+    SBS_CUDA_TRY(conv_backward_weight(2, s->g2, s->a1, s->partial, s->nblocks, s->grad, s->pk.err, nf, nt, np,
+                                      s->stream));
     SBS_CUDA_TRY(conv_backward_data(2, s->g2, s->pk, s->y1, s->g1, nf, nt, np, s->stream));
-    SBS_CUDA_TRY(conv_backward_weight(1, s->g1, s->x0, s->partial, s->nblocks, s->grad, nf, nt, np, s->stream));
+    SBS_CUDA_TRY(conv_backward_weight(1, s->g1, s->x0, s->partial, s->nblocks, s->grad, s->pk.err, nf, nt, np,
+                                      s->stream));
     if (loss) {
         std::vector<double> lp(nlb);
         unsigned herr = 0;

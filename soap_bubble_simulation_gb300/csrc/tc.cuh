@@ -1,5 +1,5 @@
-// Small wrappers of the Blackwell tensor-core (tcgen05), mbarrier and cp.async instructions used by
-// the surrogate's training convolutions (nn_conv_tc.cu).
+// Small wrappers of the Blackwell tensor-core (tcgen05), mbarrier, TMA and cp.async instructions used
+// by the surrogate's training convolutions (nn_conv_tc.cu).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -69,6 +69,23 @@ __device__ __forceinline__ bool mbar_wait_n(uint32_t bar, uint32_t n, long long 
     while (!mbar_try_wait(bar, n & 1u, 20000u))
         if (clock64() - t0 > limit) return false;
     return true;
+}
+
+// Arrives on the barrier and adds `bytes` to the transaction count its current phase waits for.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// TMA: one box of a 4-D tensor map (a __grid_constant__ kernel parameter) at coordinates c0..c3
+// (innermost first) into shared memory at dst; its bytes complete on the barrier. Elements outside
+// the tensor arrive as zeros.
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const void *map, int c0, int c1, int c2, int c3,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+        : "memory");
 }
 
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }

@@ -90,8 +90,10 @@ def test_forward_matches_oracle(sbs, orc, net, nt, np_, nf):
     check_y(y, want)
 
 
-def test_gradients_match_oracle(sbs, orc, net):
-    nt, np_, nf = 16, 40, 2
+# 40 columns: one ragged chunk of the weight gradient per row with both phi seams; 136: three
+# chunks, the last ragged; 128: two full chunks, the seam after a full one
+@pytest.mark.parametrize("nt,np_,nf", [(16, 40, 2), (12, 136, 2), (10, 128, 1)])
+def test_gradients_match_oracle(sbs, orc, net, nt, np_, nf):
     h, c = fields(nf, nt, np_, seed=3)
     ps = params_list(sbs, nf, nt, np_, seed=4)
     target = np.random.default_rng(9).standard_normal((nf, nt, np_)).astype(np.float32)
