@@ -307,8 +307,10 @@ def surrogate_section(sbs, synthetic, h0, c0, torch, activations=("gelu", "hswis
         return sim
 
     # plain reference run (same stream semantics as the rollout's plain intervals, no volume checks)
+    # every timed run is first run once untimed on the same handle (graph captures, scratch, first
+    # kernel loads), then restarted from the same fields
     ref = fresh()
-    ref.run(64)
+    ref.run(STEPS_PER_RUN)
     ref.set_thickness_array(h0)
     ref.set_concentration_array(c0)
     torch.cuda.synchronize()
@@ -352,6 +354,10 @@ def surrogate_section(sbs, synthetic, h0, c0, torch, activations=("gelu", "hswis
         sim.close()
         # the checked rollout: 156 intervals (9,984 passes) + 16 plain passes = 10,000 steps
         sim = fresh()
+        s.rollout(sim, STEPS_PER_RUN // 64 * 64, check_every=8, tol=1e-3, mode="fused")
+        sim.run(STEPS_PER_RUN % 64)
+        sim.set_thickness_array(h0)
+        sim.set_concentration_array(c0)
         torch.cuda.synchronize()
         ta = time.perf_counter()
         st = s.rollout(sim, STEPS_PER_RUN // 64 * 64, check_every=8, tol=1e-3, mode="fused")

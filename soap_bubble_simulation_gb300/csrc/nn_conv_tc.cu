@@ -520,13 +520,10 @@ __global__ void __launch_bounds__(kWgThreads) tc_wgrad_kernel(const __grid_const
 template <int CIN, bool BWD>
 cudaError_t launch_tc(TcConvArgs a, int nf, cudaStream_t st) {
     using Lay = TcLayout<CIN, BWD>;
-    static bool configured = false;  // per template instance and process
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(tc_conv_kernel<CIN, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)Lay::SMEM);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    // set on every launch (about a microsecond): the attribute belongs to the current device's context
+    cudaError_t e = cudaFuncSetAttribute(tc_conv_kernel<CIN, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)Lay::SMEM);
+    if (e != cudaSuccess) return e;
     a.segs = (a.np + kTcCells - 1) / kTcCells;
     a.nrb = (a.nt + kTcRows - 1) / kTcRows;
     a.nitems = nf * a.segs * a.nrb;
@@ -573,13 +570,10 @@ cudaError_t plane_map(CUtensorMap *map, const bf16 *base, int ch, int np, int ro
 
 template <int CIN>
 cudaError_t launch_wgrad(const TcWgradArgs &w, int nblocks, cudaStream_t st) {
-    static bool configured = false;  // per template instance and process
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(tc_wgrad_kernel<CIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)WgLayout<CIN>::SMEM);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    // set on every launch, like the convolution's: the attribute belongs to the current device's context
+    cudaError_t e = cudaFuncSetAttribute(tc_wgrad_kernel<CIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)WgLayout<CIN>::SMEM);
+    if (e != cudaSuccess) return e;
     tc_wgrad_kernel<CIN><<<nblocks, kWgThreads, WgLayout<CIN>::SMEM, st>>>(w);
     return cudaGetLastError();
 }
