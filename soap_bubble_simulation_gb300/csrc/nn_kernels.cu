@@ -58,27 +58,40 @@ struct OutArgs {
     int nf;
 };
 
-__global__ void out_kernel(OutArgs a) {
+// One block per item (an output row x a 128-cell segment): the three source rows of a3 (130 cells
+// each, phi wrapped, theta reflected) are staged in shared memory with 80 bytes per cell (16-byte
+// reads of consecutive cells fall in distinct banks), then one thread per cell.
+constexpr int kOutCells = 128;
+constexpr int kOutStride = 40;  // BF16 values per staged cell (32 + 8)
+
+__global__ void __launch_bounds__(kOutCells) out_kernel(OutArgs a) {
     __shared__ float sw[9 * 32];
-    __shared__ double sred[8];
-    for (int e = threadIdx.x; e < 9 * 32; e += blockDim.x) sw[e] = a.w4[e];
-    __syncthreads();
+    __shared__ __align__(16) bf16 sa[3][kOutCells + 2][kOutStride];
+    __shared__ double sred[kOutCells / 32];
     const int nt = a.g.nt, np = a.g.np;
-    const size_t cells = (size_t)a.nf * nt * np;
-    const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int segs = (np + kOutCells - 1) / kOutCells;
+    const int row = (int)(blockIdx.x / segs), j0 = (int)(blockIdx.x % segs) * kOutCells;
+    const int i = row % nt;
+    const size_t fb = (size_t)(row / nt) * nt * np;
+    for (int e = threadIdx.x; e < 9 * 32; e += blockDim.x) sw[e] = a.w4[e];
+    for (int e = threadIdx.x; e < 3 * (kOutCells + 2) * 4; e += blockDim.x) {
+        const int d = e / ((kOutCells + 2) * 4), q = (e / 4) % (kOutCells + 2), ch = e % 4;
+        int col = (j0 - 1 + q) % np;
+        col = col < 0 ? col + np : col;
+        const size_t src = (fb + (size_t)refl_row(i + d - 1, nt) * np + col) * 32 + ch * 8;
+        *reinterpret_cast<uint4 *>(&sa[d][q][ch * 8]) = *reinterpret_cast<const uint4 *>(a.a3 + src);
+    }
+    __syncthreads();
+    const int m = threadIdx.x, j = j0 + m;
     double l = 0.0;
-    if (c < cells) {
-        const int j = (int)(c % np), i = (int)((c / np) % nt);
-        const size_t fb = (c / ((size_t)np * nt)) * nt * np;
+    if (j < np) {
+        const size_t c = fb + (size_t)i * np + j;
         // four independent partial sums (one per 8-channel chunk) instead of one serial chain of 288
         float yk[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
         for (int t = 0; t < 9; ++t) {
-            const int dy = t / 3 - 1, dx = t % 3 - 1;
-            const int r = refl_row(i + dy, nt);
-            int q = j + dx;
-            q = q < 0 ? q + np : (q >= np ? q - np : q);
-            const uint4 *p = (const uint4 *)(a.a3 + (fb + (size_t)r * np + q) * 32);
+            const int d = t / 3, x = t % 3;  // source row i + d - 1 (reflected when staged), cell j + x - 1
+            const uint4 *p = reinterpret_cast<const uint4 *>(&sa[d][m + x][0]);
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const uint4 v = p[k];
@@ -95,12 +108,12 @@ __global__ void out_kernel(OutArgs a) {
         const float y = __fadd_rn(*a.b4, __fadd_rn(__fadd_rn(yk[0], yk[1]), __fadd_rn(yk[2], yk[3])));
         a.y4[c] = y;
         if (a.target) {
-            const float m = a.g.rows[i].w;
+            const float mk = a.g.rows[i].w;
             float gr = 0.f;
-            if (m != 0.f) {
-                const float d = __fsub_rn(y, a.target[c]);
-                l = (double)d * (double)d;
-                gr = __fmul_rn(d, a.inv_nmask2);
+            if (mk != 0.f) {
+                const float dd = __fsub_rn(y, a.target[c]);
+                l = (double)dd * (double)dd;
+                gr = __fmul_rn(dd, a.inv_nmask2);
             }
             a.g4[c] = gr;
         }
@@ -110,9 +123,9 @@ __global__ void out_kernel(OutArgs a) {
         if ((threadIdx.x & 31) == 0) sred[threadIdx.x >> 5] = l;
         __syncthreads();
         if (threadIdx.x == 0) {
-            double s = 0.0;
-            for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sred[k];
-            a.loss_part[blockIdx.x] = s;
+            double sum = 0.0;
+            for (int k = 0; k < kOutCells / 32; ++k) sum += sred[k];
+            a.loss_part[blockIdx.x] = sum;
         }
     }
 }
@@ -121,7 +134,9 @@ __global__ void out_kernel(OutArgs a) {
 // 128-cell segment; block b takes items b, b + nblocks, ... Per item the block stages the three
 // source rows of a3 (130 cells each, phi wrapped, theta reflected) and the row's g4 in shared
 // memory; warp w sums the item's cells w, w + 8, ... with lane = ic and nine accumulators per lane
-// (one per tap). One partial row [289] per block, warps summed in a fixed order.
+// (one per tap). One partial row [289] per block, warps summed in a fixed order. An item's rows are
+// loaded and then used with nothing else in flight, so the grid is sized for six blocks per SM
+// (kW4BlocksPerSm): other blocks' loads cover each block's wait.
 struct Wgrad4Args {
     const float *g4;
     const bf16 *a3;
@@ -132,6 +147,7 @@ struct Wgrad4Args {
 
 constexpr int kW4Warps = 8;
 constexpr int kW4Cells = 128;
+constexpr int kW4BlocksPerSm = 6;  // 34.7 KB of shared memory and 40 registers a thread each
 
 __global__ void __launch_bounds__(32 * kW4Warps) wgrad4_kernel(Wgrad4Args a) {
     __shared__ __align__(16) bf16 sa[3][kW4Cells + 2][32];
@@ -236,21 +252,23 @@ __global__ void __launch_bounds__(256) dgrad4_kernel(Dgrad4Args a) {
     }
 }
 
-// Column sums over the blocks' partial rows, in a fixed order: a block of 256 threads takes 32
-// adjacent columns; thread (r, c) sums rows r, r + 8, ... of column c (coalesced 128-byte rows), then
-// the eight partial sums are added in order r = 0..7. Returns the sum in the threads with r = 0.
-constexpr int kRedCols = 32, kRedRows = 8;
+// Column sums over the blocks' partial rows, in a fixed order: a block of 32 x ROWS threads takes
+// 32 adjacent columns; thread (r, c) sums rows r, r + ROWS, ... of column c (coalesced 128-byte
+// rows), then the ROWS partial sums are added in order r = 0, 1, ... Returns the sum in the threads
+// with r = 0.
+constexpr int kRedCols = 32, kRedRows = 8, kRed4Rows = 32;
+template <int ROWS>
 __device__ __forceinline__ float column_sum(const float *partial, int nblocks, int ncol, int col) {
-    __shared__ float s_part[kRedRows][kRedCols];
+    __shared__ float s_part[ROWS][kRedCols];
     const int c = threadIdx.x % kRedCols, r = threadIdx.x / kRedCols;
     float s = 0.f;
     if (col < ncol)
-        for (int k = r; k < nblocks; k += kRedRows) s = __fadd_rn(s, partial[(size_t)k * ncol + col]);
+        for (int k = r; k < nblocks; k += ROWS) s = __fadd_rn(s, partial[(size_t)k * ncol + col]);
     s_part[r][c] = s;
     __syncthreads();
     float t = 0.f;
     if (r == 0)
-        for (int q = 0; q < kRedRows; ++q) t = __fadd_rn(t, s_part[q][c]);
+        for (int q = 0; q < ROWS; ++q) t = __fadd_rn(t, s_part[q][c]);
     return t;
 }
 
@@ -261,7 +279,7 @@ __global__ void __launch_bounds__(kRedCols *kRedRows) reduce_partials_kernel(con
                                                                                float *grad_b) {
     const int ncol = co * 9 * ci + co;
     const int e = blockIdx.x * kRedCols + threadIdx.x % kRedCols;
-    const float s = column_sum(partial, nblocks, ncol, e);
+    const float s = column_sum<kRedRows>(partial, nblocks, ncol, e);
     if (threadIdx.x >= kRedCols || e >= ncol) return;
     if (e < co * 9 * ci) {
         const int oc = e / (9 * ci), r = e % (9 * ci), t = r / ci, ic = r % ci;
@@ -272,10 +290,10 @@ __global__ void __launch_bounds__(kRedCols *kRedRows) reduce_partials_kernel(con
 }
 
 // layer-4 partial rows are [block][tap*32 + ic] then db4
-__global__ void __launch_bounds__(kRedCols *kRedRows) reduce4_kernel(const float *partial, int nblocks,
-                                                                       float *grad_w4, float *grad_b4) {
+__global__ void __launch_bounds__(kRedCols *kRed4Rows) reduce4_kernel(const float *partial, int nblocks,
+                                                                        float *grad_w4, float *grad_b4) {
     const int e = blockIdx.x * kRedCols + threadIdx.x % kRedCols;
-    const float s = column_sum(partial, nblocks, 289, e);
+    const float s = column_sum<kRed4Rows>(partial, nblocks, 289, e);
     if (threadIdx.x >= kRedCols || e >= 289) return;
     if (e < 288)
         grad_w4[e] = s;
@@ -409,9 +427,8 @@ cudaError_t output_layer(const bf16 *a3, const Packed &p, float *y4, const float
     o.g = g;
     o.nf = nf;
     o.b4 = p.b + 96;
-    const size_t cells = (size_t)nf * g.nt * g.np;
-    const int nb = (int)((cells + 255) / 256);
-    out_kernel<<<nb, 256, 0, st>>>(o);
+    const int nb = nf * g.nt * ((g.np + kOutCells - 1) / kOutCells);  // one block per row segment
+    out_kernel<<<nb, kOutCells, 0, st>>>(o);
     if (nblocks_out) *nblocks_out = nb;
     return cudaGetLastError();
 }
@@ -425,11 +442,15 @@ cudaError_t output_backward(const float *g4, const bf16 *a3, const float *y3, co
     w.partial = partial;
     w.g = g;
     w.rows = nf * g.nt;
-    wgrad4_kernel<<<nblocks, 32 * kW4Warps, 0, st>>>(w);
+    // nblocks is two per SM (the 3x3 layers' partial rows); six per SM here, whose rows of 289
+    // floats fit the same buffer of nblocks x (32 x 9 x 32 + 32) floats
+    static_assert(kW4BlocksPerSm * 289 <= 2 * (32 * 9 * 32 + 32), "layer-4 partial rows fit the buffer");
+    const int nb4 = nblocks / 2 * kW4BlocksPerSm;
+    wgrad4_kernel<<<nb4, 32 * kW4Warps, 0, st>>>(w);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    reduce4_kernel<<<(289 + kRedCols - 1) / kRedCols, kRedCols * kRedRows, 0, st>>>(partial, nblocks, grad + SBS_NN_W4,
-                                                                                 grad + SBS_NN_B4);
+    reduce4_kernel<<<(289 + kRedCols - 1) / kRedCols, kRedCols * kRed4Rows, 0, st>>>(partial, nb4, grad + SBS_NN_W4,
+                                                                                  grad + SBS_NN_B4);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     Dgrad4Args d{};
     d.g4 = g4;

@@ -192,7 +192,9 @@ int ensure_ws(sbs_surrogate *s, size_t cells) {
     s->g4 = (float *)take(4 * cells);
     s->tgt = (float *)take(4 * cells);
     s->cap = cells;
-    const size_t lp = (cells + 255) / 256;
+    // one loss partial per 128-cell row segment of the output layer: rows have at least 3 cells,
+    // so there are at most cells / 3 segments
+    const size_t lp = cells / 3 + 1;
     if (lp > s->loss_cap) {
         cudaFree(s->loss_part);
         s->loss_part = nullptr;
