@@ -91,8 +91,9 @@ def test_forward_matches_oracle(sbs, orc, net, nt, np_, nf):
 
 
 # 40 columns: one ragged chunk of the weight gradient per row with both phi seams; 136: three
-# chunks, the last ragged; 128: two full chunks, the seam after a full one
-@pytest.mark.parametrize("nt,np_,nf", [(16, 40, 2), (12, 136, 2), (10, 128, 1)])
+# chunks, the last ragged; 128: two full chunks, the seam after a full one; 4 x 3: the smallest
+# grid (both poles reflect into the same interior rows, three cells between the seams)
+@pytest.mark.parametrize("nt,np_,nf", [(16, 40, 2), (12, 136, 2), (10, 128, 1), (4, 3, 2)])
 def test_gradients_match_oracle(sbs, orc, net, nt, np_, nf):
     h, c = fields(nf, nt, np_, seed=3)
     ps = params_list(sbs, nf, nt, np_, seed=4)
