@@ -77,10 +77,43 @@ __device__ __forceinline__ float2 hswish2(float2 x) {
     return __fmul2_rn(x, s);
 }
 
+// Two GELU derivatives with packed FP32x2 arithmetic: the operations of gelu_grad() (the
+// derivative term is formed for both halves and then selected), so bitwise two gelu_grad() calls.
+__device__ __forceinline__ float2 gelu_grad2(float2 x) {
+    const float2 t = make_float2(fminf(fmaxf(x.x, -3.f), 3.f), fminf(fmaxf(x.y, -3.f), 3.f));
+    const float2 u = __fmul2_rn(t, t);
+    float2 p = __ffma2_rn(make_float2(SBS_NN_Q4, SBS_NN_Q4), u, make_float2(SBS_NN_Q3, SBS_NN_Q3));
+    p = __ffma2_rn(p, u, make_float2(SBS_NN_Q2, SBS_NN_Q2));
+    p = __ffma2_rn(p, u, make_float2(SBS_NN_Q1, SBS_NN_Q1));
+    p = __ffma2_rn(p, u, make_float2(SBS_NN_Q0, SBS_NN_Q0));
+    const float2 phi = __ffma2_rn(t, p, make_float2(0.5f, 0.5f));
+    float2 dp = __ffma2_rn(make_float2(SBS_NN_Q4X4, SBS_NN_Q4X4), u, make_float2(SBS_NN_Q3X3, SBS_NN_Q3X3));
+    dp = __ffma2_rn(dp, u, make_float2(SBS_NN_Q2X2, SBS_NN_Q2X2));
+    dp = __ffma2_rn(dp, u, make_float2(SBS_NN_Q1, SBS_NN_Q1));
+    const float2 d = __ffma2_rn(__fadd2_rn(u, u), dp, p);
+    const float2 dphi = make_float2(fabsf(x.x) < 3.f ? d.x : 0.f, fabsf(x.y) < 3.f ? d.y : 0.f);
+    return __ffma2_rn(x, dphi, phi);
+}
+
+// Two hard-swish derivatives: bitwise two hswish_grad() calls.
+__device__ __forceinline__ float2 hswish_grad2(float2 x) {
+    const float2 r = __ffma2_rn(x, make_float2(SBS_NN_HS_SLOPE, SBS_NN_HS_SLOPE), make_float2(0.5f, 0.5f));
+    const float2 s = make_float2(__saturatef(r.x), __saturatef(r.y));
+    const float2 g = __ffma2_rn(x, make_float2(SBS_NN_HS_SLOPE, SBS_NN_HS_SLOPE), s);
+    return make_float2((r.x > 0.f && r.x < 1.f) ? g.x : s.x, (r.y > 0.f && r.y < 1.f) ? g.y : s.y);
+}
+
 // The network's activation (SBS_NN_ACT_*), chosen by a value that is uniform over the launch.
 __device__ __forceinline__ float act(int kind, float x) { return kind == SBS_NN_ACT_HSWISH ? hswish(x) : gelu(x); }
 __device__ __forceinline__ float act_grad(int kind, float x) {
     return kind == SBS_NN_ACT_HSWISH ? hswish_grad(x) : gelu_grad(x);
+}
+// The same for two values at once (packed FP32x2), bitwise two scalar calls.
+__device__ __forceinline__ float2 act2(int kind, float2 x) {
+    return kind == SBS_NN_ACT_HSWISH ? hswish2(x) : gelu2(x);
+}
+__device__ __forceinline__ float2 act_grad2(int kind, float2 x) {
+    return kind == SBS_NN_ACT_HSWISH ? hswish_grad2(x) : gelu_grad2(x);
 }
 
 __device__ __forceinline__ uint32_t pack2(float lo, float hi) {

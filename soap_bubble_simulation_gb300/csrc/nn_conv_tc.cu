@@ -197,11 +197,15 @@ __global__ void __launch_bounds__(kTcThreads) tc_conv_kernel(const TcConvArgs a)
 #pragma unroll
                 for (int k = 0; k < 4; ++k) yp[k] = make_float4(y[4 * k], y[4 * k + 1], y[4 * k + 2], y[4 * k + 3]);
 #pragma unroll
-                for (int k = 0; k < 2; ++k)
-                    ap[k] = make_uint4(pack2(act(a.act, y[8 * k]), act(a.act, y[8 * k + 1])),
-                                       pack2(act(a.act, y[8 * k + 2]), act(a.act, y[8 * k + 3])),
-                                       pack2(act(a.act, y[8 * k + 4]), act(a.act, y[8 * k + 5])),
-                                       pack2(act(a.act, y[8 * k + 6]), act(a.act, y[8 * k + 7])));
+                for (int k = 0; k < 2; ++k) {
+                    uint32_t w4[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const float2 g = act2(a.act, make_float2(y[8 * k + 2 * e], y[8 * k + 2 * e + 1]));
+                        w4[e] = pack2(g.x, g.y);
+                    }
+                    ap[k] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+                }
             } else {
                 const float4 *yp =
                     reinterpret_cast<const float4 *>(s_y + ((r - r0) & 1) * kTcCells * kTcYS + m * kTcYS + c0);
@@ -213,8 +217,9 @@ __global__ void __launch_bounds__(kTcThreads) tc_conv_kernel(const TcConvArgs a)
 #pragma unroll
                     for (int e = 0; e < 4; ++e) {
                         const int n = 8 * k + 2 * e;
-                        w4[e] = pack2(__fmul_rn(__uint_as_float(v[n]), act_grad(a.act, y[2 * e])),
-                                      __fmul_rn(__uint_as_float(v[n + 1]), act_grad(a.act, y[2 * e + 1])));
+                        const float2 g = __fmul2_rn(make_float2(__uint_as_float(v[n]), __uint_as_float(v[n + 1])),
+                                                    act_grad2(a.act, make_float2(y[2 * e], y[2 * e + 1])));
+                        w4[e] = pack2(g.x, g.y);
                     }
                     ap[k] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
                 }

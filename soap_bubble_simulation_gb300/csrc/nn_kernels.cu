@@ -245,9 +245,11 @@ __global__ void __launch_bounds__(256) dgrad4_kernel(Dgrad4Args a) {
         const float v[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
         uint32_t w[4];
 #pragma unroll
-        for (int e = 0; e < 4; ++e)
-            w[e] = pack2(__fmul_rn(s[8 * k + 2 * e], act_grad(a.act, v[2 * e])),
-                         __fmul_rn(s[8 * k + 2 * e + 1], act_grad(a.act, v[2 * e + 1])));
+        for (int e = 0; e < 4; ++e) {
+            const float2 g = __fmul2_rn(make_float2(s[8 * k + 2 * e], s[8 * k + 2 * e + 1]),
+                                        act_grad2(a.act, make_float2(v[2 * e], v[2 * e + 1])));
+            w[e] = pack2(g.x, g.y);
+        }
         gp[k] = make_uint4(w[0], w[1], w[2], w[3]);
     }
 }
