@@ -58,14 +58,40 @@ struct OutArgs {
     int nf;
 };
 
+// The three source rows i - 1, i, i + 1 (theta reflected) of a3 for cells j0 - 1 .. j0 + 128 (phi
+// wrapped) into dst[row][cell][0..31], one 16-byte copy per thread and step. For rows of at least
+// 128 cells one correction wraps a column (the cells span less than two row lengths).
+constexpr int kSegCells = 128;  // cells per row segment of the layer-4 kernels
+template <int STRIDE>
+__device__ __forceinline__ void stage_rows3(bf16 (*dst)[kSegCells + 2][STRIDE], const bf16 *a3, size_t fb, int i,
+                                            int nt, int np, int j0) {
+    const int ru = refl_row(i - 1, nt), rd = refl_row(i + 1, nt);
+    const bool wide = np >= kSegCells;
+    for (int e = threadIdx.x; e < 3 * (kSegCells + 2) * 4; e += blockDim.x) {
+        const int d = e / ((kSegCells + 2) * 4), rem = e - d * ((kSegCells + 2) * 4), q = rem >> 2, ch = rem & 3;
+        int col = j0 - 1 + q;
+        if (wide) {
+            col = col < 0 ? col + np : (col >= np ? col - np : col);
+        } else {
+            col %= np;
+            col = col < 0 ? col + np : col;
+        }
+        const int r = d == 0 ? ru : (d == 1 ? i : rd);
+        *reinterpret_cast<uint4 *>(&dst[d][q][ch * 8]) =
+            *reinterpret_cast<const uint4 *>(a3 + (fb + (size_t)r * np + col) * 32 + ch * 8);
+    }
+}
+
 // One block per item (an output row x a 128-cell segment): the three source rows of a3 (130 cells
 // each, phi wrapped, theta reflected) are staged in shared memory with 80 bytes per cell (16-byte
-// reads of consecutive cells fall in distinct banks), then one thread per cell.
-constexpr int kOutCells = 128;
+// reads of consecutive cells fall in distinct banks), then one thread per cell. The four chunk sums
+// of a cell run as two packed FP32x2 pairs (chunks 0, 1 and 2, 3): each half performs its chunk's
+// multiply-adds in the original order, so y is bitwise that of four scalar chains.
+constexpr int kOutCells = kSegCells;
 constexpr int kOutStride = 40;  // BF16 values per staged cell (32 + 8)
 
-__global__ void __launch_bounds__(kOutCells) out_kernel(OutArgs a) {
-    __shared__ float sw[9 * 32];
+__global__ void __launch_bounds__(kOutCells, 7) out_kernel(OutArgs a) {  // 7 blocks: the shared-memory limit
+    __shared__ float2 swp[9][2][8];  // tap, chunk pair: (W4[tap][16 kp + c], W4[tap][16 kp + 8 + c])
     __shared__ __align__(16) bf16 sa[3][kOutCells + 2][kOutStride];
     __shared__ double sred[kOutCells / 32];
     const int nt = a.g.nt, np = a.g.np;
@@ -73,39 +99,38 @@ __global__ void __launch_bounds__(kOutCells) out_kernel(OutArgs a) {
     const int row = (int)(blockIdx.x / segs), j0 = (int)(blockIdx.x % segs) * kOutCells;
     const int i = row % nt;
     const size_t fb = (size_t)(row / nt) * nt * np;
-    for (int e = threadIdx.x; e < 9 * 32; e += blockDim.x) sw[e] = a.w4[e];
-    for (int e = threadIdx.x; e < 3 * (kOutCells + 2) * 4; e += blockDim.x) {
-        const int d = e / ((kOutCells + 2) * 4), q = (e / 4) % (kOutCells + 2), ch = e % 4;
-        int col = (j0 - 1 + q) % np;
-        col = col < 0 ? col + np : col;
-        const size_t src = (fb + (size_t)refl_row(i + d - 1, nt) * np + col) * 32 + ch * 8;
-        *reinterpret_cast<uint4 *>(&sa[d][q][ch * 8]) = *reinterpret_cast<const uint4 *>(a.a3 + src);
+    for (int e = threadIdx.x; e < 9 * 16; e += blockDim.x) {
+        const int t = e >> 4, kp = (e >> 3) & 1, c = e & 7;
+        swp[t][kp][c] = make_float2(a.w4[t * 32 + 16 * kp + c], a.w4[t * 32 + 16 * kp + 8 + c]);
     }
+    stage_rows3<kOutStride>(sa, a.a3, fb, i, nt, np, j0);
     __syncthreads();
     const int m = threadIdx.x, j = j0 + m;
     double l = 0.0;
     if (j < np) {
         const size_t c = fb + (size_t)i * np + j;
-        // four independent partial sums (one per 8-channel chunk) instead of one serial chain of 288
-        float yk[4] = {0.f, 0.f, 0.f, 0.f};
+        // four independent partial sums (one per 8-channel chunk), as the pairs (0, 1) and (2, 3)
+        float2 y01 = make_float2(0.f, 0.f), y23 = y01;
 #pragma unroll
         for (int t = 0; t < 9; ++t) {
             const int d = t / 3, x = t % 3;  // source row i + d - 1 (reflected when staged), cell j + x - 1
             const uint4 *p = reinterpret_cast<const uint4 *>(&sa[d][m + x][0]);
+            const uint4 v0 = p[0], v1 = p[1], v2 = p[2], v3 = p[3];
+            const uint32_t u0[4] = {v0.x, v0.y, v0.z, v0.w}, u1[4] = {v1.x, v1.y, v1.z, v1.w};
+            const uint32_t u2[4] = {v2.x, v2.y, v2.z, v2.w}, u3[4] = {v3.x, v3.y, v3.z, v3.w};
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const uint4 v = p[k];
-                const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const __nv_bfloat162 h2 = *reinterpret_cast<const __nv_bfloat162 *>(&w[e]);
-                    const float2 f = __bfloat1622float2(h2);
-                    yk[k] = __fmaf_rn(sw[t * 32 + k * 8 + 2 * e], f.x, yk[k]);
-                    yk[k] = __fmaf_rn(sw[t * 32 + k * 8 + 2 * e + 1], f.y, yk[k]);
-                }
+            for (int e = 0; e < 4; ++e) {
+                const float2 f0 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u0[e]));
+                const float2 f1 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u1[e]));
+                const float2 f2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u2[e]));
+                const float2 f3 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u3[e]));
+                y01 = __ffma2_rn(swp[t][0][2 * e], make_float2(f0.x, f1.x), y01);
+                y01 = __ffma2_rn(swp[t][0][2 * e + 1], make_float2(f0.y, f1.y), y01);
+                y23 = __ffma2_rn(swp[t][1][2 * e], make_float2(f2.x, f3.x), y23);
+                y23 = __ffma2_rn(swp[t][1][2 * e + 1], make_float2(f2.y, f3.y), y23);
             }
         }
-        const float y = __fadd_rn(*a.b4, __fadd_rn(__fadd_rn(yk[0], yk[1]), __fadd_rn(yk[2], yk[3])));
+        const float y = __fadd_rn(*a.b4, __fadd_rn(__fadd_rn(y01.x, y01.y), __fadd_rn(y23.x, y23.y)));
         a.y4[c] = y;
         if (a.target) {
             const float mk = a.g.rows[i].w;
@@ -146,10 +171,10 @@ struct Wgrad4Args {
 };
 
 constexpr int kW4Warps = 8;
-constexpr int kW4Cells = 128;
+constexpr int kW4Cells = kSegCells;
 constexpr int kW4BlocksPerSm = 6;  // 34.7 KB of shared memory and 40 registers a thread each
 
-__global__ void __launch_bounds__(32 * kW4Warps) wgrad4_kernel(Wgrad4Args a) {
+__global__ void __launch_bounds__(32 * kW4Warps, kW4BlocksPerSm) wgrad4_kernel(Wgrad4Args a) {
     __shared__ __align__(16) bf16 sa[3][kW4Cells + 2][32];
     __shared__ float sg[kW4Cells];
     __shared__ float sp[kW4Warps][289];
