@@ -86,7 +86,7 @@ __device__ __forceinline__ void stage_rows3(bf16 (*dst)[kSegCells + 2][STRIDE], 
 // each, phi wrapped, theta reflected) are staged in shared memory with 80 bytes per cell (16-byte
 // reads of consecutive cells fall in distinct banks), then one thread per cell. The four chunk sums
 // of a cell run as two packed FP32x2 pairs (chunks 0, 1 and 2, 3): each half performs its chunk's
-// multiply-adds in the original order, so y is bitwise that of four scalar chains.
+// multiply-adds tap by tap and channel by channel, so y is bitwise that of four scalar chains.
 constexpr int kOutCells = kSegCells;
 constexpr int kOutStride = 40;  // BF16 values per staged cell (32 + 8)
 
