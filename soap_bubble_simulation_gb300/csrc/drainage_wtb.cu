@@ -115,7 +115,16 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kMinBlocksPerSm) wtb_wgsl
         ph = __ldg(reinterpret_cast<const float4 *>(w.hin + (size_t)t0 * w.pitch));
         pc = __ldg(reinterpret_cast<const float4 *>(w.cin + (size_t)t0 * w.pitch));
     }
+    // iterations t in [ts, te) are steady (wtb_iter): every level's row t - l inside [r0 - (K - l),
+    // r1 + (K - l)) and in 1..nt-2, the final row t - K in [r0, r1), the prefetched row t + 1 < nt
+    const int ts = w.r0 + K, te = min(w.r1 + K, a.nt - 1);
     for (int t = t0; t < t1; t += 3) {
+        if (!CAU && t >= ts && t + 2 < te) {
+            wtb_iter<K, 0, VOL, MAR, false, false, true>(w, t, wh, wc, ph, pc, vacc, wk);
+            wtb_iter<K, 1, VOL, MAR, false, false, true>(w, t + 1, wh, wc, ph, pc, vacc, wk);
+            wtb_iter<K, 2, VOL, MAR, false, false, true>(w, t + 2, wh, wc, ph, pc, vacc, wk);
+            continue;
+        }
         wtb_iter<K, 0, VOL, MAR, false, CAU>(w, t, wh, wc, ph, pc, vacc, wk);
         if (t + 1 < t1) wtb_iter<K, 1, VOL, MAR, false, CAU>(w, t + 1, wh, wc, ph, pc, vacc, wk);
         if (t + 2 < t1) wtb_iter<K, 2, VOL, MAR, false, CAU>(w, t + 2, wh, wc, ph, pc, vacc, wk);

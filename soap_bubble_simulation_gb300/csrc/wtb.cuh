@@ -55,14 +55,17 @@ __device__ __forceinline__ void wtb_caustic_row(const Wtb &w, int j, const float
 // CAU: the launch also writes the caustic map of its result. Every level then covers one more row
 // on each side (the strip's final rows r0 - 1 and r1 are needed), wk keeps the last three final
 // rows, and map row j is written once final row j + 1 exists (theta clamped at the poles).
-template <int K, int P, bool VOL, bool MAR, bool CG = false, bool CAU = false>
+// STEADY: the caller guarantees that every level's row lies inside the strip's window and the
+// grid, none is a pole row, the final row is one of the strip's own rows and the prefetched row
+// t + 1 exists; the iteration then skips those tests (same arithmetic, same bits).
+template <int K, int P, bool VOL, bool MAR, bool CG = false, bool CAU = false, bool STEADY = false>
 __device__ __forceinline__ void wtb_iter(const Wtb &w, int t, float4 (&wh)[K][3], float4 (&wc)[K][3], float4 &ph,
                                          float4 &pc, double &vacc, float4 *wk = nullptr) {
     constexpr int CUR = (P + 2) % 3, UP = (P + 1) % 3;
     constexpr int E = CAU ? 1 : 0;
     const int tl = SBS_WTB_PREFETCH ? t + 1 : t;
     float4 nh = make_float4(0.f, 0.f, 0.f, 0.f), nc = nh;
-    if (tl >= 0 && tl < w.nt) {
+    if (STEADY || (tl >= 0 && tl < w.nt)) {
         const float4 *ph4 = reinterpret_cast<const float4 *>(w.hin + (size_t)tl * w.pitch);
         const float4 *pc4 = reinterpret_cast<const float4 *>(w.cin + (size_t)tl * w.pitch);
         nh = CG ? __ldcg(ph4) : __ldg(ph4);
@@ -80,11 +83,12 @@ __device__ __forceinline__ void wtb_iter(const Wtb &w, int t, float4 (&wh)[K][3]
 #pragma unroll
     for (int l = 1; l <= K; ++l) {
         const int i = t - l;
-        const bool need = i >= w.r0 - (K - l) - E && i < w.r1 + (K - l) + E && i >= 0 && i < w.nt;  // warp-uniform
+        const bool need =
+            STEADY || (i >= w.r0 - (K - l) - E && i < w.r1 + (K - l) + E && i >= 0 && i < w.nt);  // warp-uniform
         float4 oh = make_float4(0.f, 0.f, 0.f, 0.f), oc = oh;
         if (need) {
             const float4 hc = wh[l - 1][CUR], cc = wc[l - 1][CUR];
-            if (i == 0 || i == w.nt - 1) {  // pole rows are frozen (drainage.wgsl:85-89)
+            if (!STEADY && (i == 0 || i == w.nt - 1)) {  // pole rows are frozen (drainage.wgsl:85-89)
                 oh = hc;
                 oc = cc;
             } else {
@@ -103,7 +107,7 @@ __device__ __forceinline__ void wtb_iter(const Wtb &w, int t, float4 (&wh)[K][3]
             wh[l][P] = oh;
             wc[l][P] = oc;
         } else {
-            if (need && i >= w.r0 && i < w.r1 && w.store) {
+            if (STEADY ? w.store : (need && i >= w.r0 && i < w.r1 && w.store)) {
                 *reinterpret_cast<float4 *>(w.hout + (size_t)i * w.pitch) = oh;
                 *reinterpret_cast<float4 *>(w.cout + (size_t)i * w.pitch) = oc;
                 if (VOL) vacc += ((double)oh.x + (double)oh.y + (double)oh.z + (double)oh.w) * __ldg(w.vol_w + i);
